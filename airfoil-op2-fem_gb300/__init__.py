@@ -1,0 +1,337 @@
+"""GB300-native DG Euler RHS + SSPRK3 step (Airfoil-OP2-FEM hot path).
+
+Python front end over the C ABI of ``lib/libdg_gb300.so`` (include/dg_gb300.h
+for the native fused solver, include/op2_gb300.h for the OP2 drop-in).  The
+compute path is the CUDA library: nothing here computes on the CPU, and every
+entry point raises if the library cannot be loaded.
+
+The directory name is not a Python identifier; load it with
+``importlib`` under the module name ``airfoil_op2_fem_gb300`` (see
+``__graft_entry__.load_package``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libdg_gb300.so")
+
+APP_AIRFOIL, APP_VORTEX = 0, 1
+DT_EVERY_STEP, DT_FROZEN = 0, 1
+ERR_NONPHYSICAL = -200
+
+_lib = None
+
+
+class DGError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (code %d)" % (msg, code))
+        self.code = code
+
+
+class Config(C.Structure):
+    """dg_config_t (include/dg_gb300.h)."""
+    _fields_ = [("N", C.c_int), ("app", C.c_int), ("dt_mode", C.c_int), ("cfl", C.c_double),
+                ("gam", C.c_double), ("mach", C.c_double), ("alpha_deg", C.c_double),
+                ("p_inf", C.c_double), ("rho_inf", C.c_double), ("vortex_x0", C.c_double),
+                ("vortex_y0", C.c_double), ("vortex_beta", C.c_double)]
+
+
+def config(N=3, app=APP_AIRFOIL, dt_mode=DT_EVERY_STEP, cfl=1.0, gam=1.4, mach=0.4,
+           alpha_deg=0.0, p_inf=1.0, rho_inf=1.0, vortex_x0=5.0, vortex_y0=0.0, vortex_beta=5.0):
+    return Config(N, app, dt_mode, cfl, gam, mach, alpha_deg, p_inf, rho_inf, vortex_x0,
+                  vortex_y0, vortex_beta)
+
+
+def build():
+    """Compile the CUDA library in-tree (sm_103a)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_dg_build", os.path.join(HERE, "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build()
+
+
+def lib():
+    """The loaded CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("CUDA library not built: %s (call build())" % LIB_PATH)
+    L = C.CDLL(LIB_PATH)
+    vp, ip, dp, cp = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_char_p
+    sig = {
+        "dg_last_error": (cp, []),
+        "dg_mesh_from_cells": (C.c_int, [C.c_int, dp, C.c_int, ip, C.POINTER(vp)]),
+        "dg_mesh_from_tables": (C.c_int, [C.c_int, dp, C.c_int, ip, C.c_int, ip, ip, C.c_int, ip, ip, ip,
+                                          C.POINTER(vp)]),
+        "dg_mesh_read_vtk": (C.c_int, [cp, C.c_int, C.POINTER(vp)]),
+        "dg_mesh_naca_ogrid": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.POINTER(vp)]),
+        "dg_mesh_vortex_square": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_ulonglong, C.POINTER(vp)]),
+        "dg_mesh_size": (C.c_int, [vp, C.c_int]),
+        "dg_mesh_get": (C.c_int, [vp, cp, vp]),
+        "dg_mesh_set_bedge_type": (C.c_int, [vp, ip]),
+        "dg_mesh_free": (None, [vp]),
+        "dg_operators": (C.c_int, [C.c_int, dp, dp, dp, dp, dp, dp, dp, ip]),
+        "dg_solver_create": (C.c_int, [C.POINTER(Config), vp, C.POINTER(vp)]),
+        "dg_solver_init": (C.c_int, [vp]),
+        "dg_solver_run": (C.c_int, [vp, C.c_int]),
+        "dg_solver_sync": (C.c_int, [vp]),
+        "dg_solver_get": (C.c_int, [vp, cp, dp]),
+        "dg_solver_set": (C.c_int, [vp, cp, dp]),
+        "dg_solver_rhs": (C.c_int, [vp, dp, dp]),
+        "dg_solver_time": (C.c_int, [vp, dp, dp, C.POINTER(C.c_ulonglong)]),
+        "dg_solver_l2_error": (C.c_int, [vp, dp]),
+        "dg_solver_record_dt": (C.c_int, [vp, C.c_int]),
+        "dg_solver_dt_history": (C.c_int, [vp, dp, C.c_int]),
+        "dg_solver_step_host": (C.c_int, [vp, dp, C.c_int, dp]),
+        "dg_solver_device_ptr": (vp, [vp, cp]),
+        "dg_solver_stream": (vp, [vp]),
+        "dg_solver_step_timed": (C.c_int, [vp, C.POINTER(C.c_float)]),
+        "dg_solver_free": (None, [vp]),
+        "dg_host_alloc": (vp, [C.c_size_t]),
+        "dg_host_free": (None, [vp]),
+        "dg_event_create": (vp, []),
+        "dg_event_record": (C.c_int, [vp, vp]),
+        "dg_event_elapsed_ms": (C.c_float, [vp, vp]),
+        "dg_event_destroy": (None, [vp]),
+        "dg_stream_sync": (C.c_int, [vp]),
+        "dg_l2_flush": (C.c_int, [vp]),
+        "dg_fp64_peak_gflops": (C.c_double, []),
+        "dg_kernels_per_step": (C.c_int, []),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != 0:
+        raise DGError(rc, lib().dg_last_error().decode())
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Mesh:
+    """A triangle mesh with the reference's connectivity tables (dg_mesh_t)."""
+
+    def __init__(self, handle):
+        self.h = handle
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.dg_mesh_free(self.h)
+            self.h = None
+
+    @classmethod
+    def from_cells(cls, coords, cells):
+        coords, cells = _f64(coords), _i32(cells)
+        h = C.c_void_p()
+        _check(lib().dg_mesh_from_cells(coords.shape[0], _dp(coords), cells.shape[0], _ip(cells), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_tables(cls, m):
+        a = {k: (_f64(v) if k == "coords" else _i32(v)) for k, v in m.items()}
+        bt = a.get("bedge_type")
+        h = C.c_void_p()
+        _check(lib().dg_mesh_from_tables(
+            a["coords"].shape[0], _dp(a["coords"]), a["cell2nodes"].shape[0], _ip(a["cell2nodes"]),
+            a["edge2cells"].shape[0], _ip(a["edge2cells"]), _ip(a["edgeNum"]), a["bedge2cell"].shape[0],
+            _ip(a["bedge2cell"]), _ip(a["bedgeNum"]), _ip(bt) if bt is not None else None, C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def read_vtk(cls, path, classify_box=True):
+        h = C.c_void_p()
+        _check(lib().dg_mesh_read_vtk(path.encode(), int(classify_box), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def naca_ogrid(cls, n_theta=256, n_r=64, stretch=1.1, radius=20.0, farfield="characteristic"):
+        h = C.c_void_p()
+        _check(lib().dg_mesh_naca_ogrid(n_theta, n_r, stretch, radius,
+                                        1 if farfield == "characteristic" else 0, C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def vortex_square(cls, n=32, lo=-5.0, hi=5.0, seed=20261203):
+        h = C.c_void_p()
+        _check(lib().dg_mesh_vortex_square(n, lo, hi, seed, C.byref(h)))
+        return cls(h)
+
+    def size(self, what):
+        idx = {"nodes": 0, "cells": 1, "edges": 2, "bedges": 3}[what]
+        n = lib().dg_mesh_size(self.h, idx)
+        if n < 0:
+            _check(n)
+        return n
+
+    def arrays(self):
+        nn, nc, ne, nb = (self.size(w) for w in ("nodes", "cells", "edges", "bedges"))
+        shapes = {"coords": (np.float64, (nn, 2)), "cell2nodes": (np.int32, (nc, 3)),
+                  "edge2nodes": (np.int32, (ne, 2)), "edge2cells": (np.int32, (ne, 2)),
+                  "edgeNum": (np.int32, (ne, 2)), "bedge2nodes": (np.int32, (nb, 2)),
+                  "bedge2cell": (np.int32, (nb,)), "bedgeNum": (np.int32, (nb,)),
+                  "bedge_type": (np.int32, (nb,))}
+        out = {}
+        for name, (dt, shp) in shapes.items():
+            a = np.empty(shp, dtype=dt)
+            _check(lib().dg_mesh_get(self.h, name.encode(), a.ctypes.data_as(C.c_void_p)))
+            out[name] = a
+        return out
+
+    def set_bedge_type(self, types):
+        t = _i32(types)
+        _check(lib().dg_mesh_set_bedge_type(self.h, _ip(t)))
+
+
+def operators(N):
+    """Nodal operators of order N (dict like the reference's constants headers)."""
+    np_, nfp = (N + 1) * (N + 2) // 2, N + 1
+    o = {k: np.empty(sz) for k, sz in (("r", np_), ("s", np_), ("Dr", np_ * np_), ("Ds", np_ * np_),
+                                         ("Drw", np_ * np_), ("Dsw", np_ * np_), ("LIFT", np_ * 3 * nfp))}
+    fm = np.empty(3 * nfp, dtype=np.int32)
+    _check(lib().dg_operators(N, *(_dp(o[k]) for k in ("r", "s", "Dr", "Ds", "Drw", "Dsw", "LIFT")), _ip(fm)))
+    o["FMASK"] = fm
+    o.update(N=N, Np=np_, Nfp=nfp)
+    for k in ("Dr", "Ds", "Drw", "Dsw"):
+        o[k] = o[k].reshape(np_, np_)
+    o["LIFT"] = o["LIFT"].reshape(np_, 3 * nfp)
+    return o
+
+
+class Solver:
+    """The native fused solver (dg_solver_t): state stays on the GPU between calls."""
+
+    def __init__(self, mesh: Mesh, cfg: Config):
+        self.mesh = mesh
+        self.cfg = cfg
+        self.N = cfg.N
+        self.Np = (cfg.N + 1) * (cfg.N + 2) // 2
+        self.K = mesh.size("cells")
+        h = C.c_void_p()
+        _check(lib().dg_solver_create(C.byref(cfg), mesh.h, C.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.dg_solver_free(self.h)
+            self.h = None
+
+    def init(self):
+        _check(lib().dg_solver_init(self.h))
+        return self
+
+    def run(self, nsteps):
+        _check(lib().dg_solver_run(self.h, nsteps))
+
+    def sync(self):
+        _check(lib().dg_solver_sync(self.h))
+
+    def get(self, name="q"):
+        n = self.K * 16 if name == "geo" else (self.K * 3 * (self.N + 1) * 4 if name == "flux" else self.K * self.Np * 4)
+        out = np.empty(n)
+        _check(lib().dg_solver_get(self.h, name.encode(), _dp(out)))
+        return out
+
+    def set(self, name, arr):
+        a = _f64(arr).ravel()
+        assert a.size == self.K * self.Np * 4
+        _check(lib().dg_solver_set(self.h, name.encode(), _dp(a)))
+
+    def rhs(self, W):
+        a = _f64(W).ravel()
+        out = np.empty_like(a)
+        _check(lib().dg_solver_rhs(self.h, _dp(a), _dp(out)))
+        return out
+
+    def time(self):
+        t, dt, st = C.c_double(), C.c_double(), C.c_ulonglong()
+        _check(lib().dg_solver_time(self.h, C.byref(t), C.byref(dt), C.byref(st)))
+        return t.value, dt.value, st.value
+
+    def l2_error(self):
+        out = np.empty(4)
+        _check(lib().dg_solver_l2_error(self.h, _dp(out)))
+        return out
+
+    def record_dt(self, max_steps):
+        _check(lib().dg_solver_record_dt(self.h, max_steps))
+
+    def dt_history(self, n):
+        out = np.empty(n)
+        _check(lib().dg_solver_dt_history(self.h, _dp(out), n))
+        return out
+
+    def step_host(self, q_in, nsteps, q_out):
+        _check(lib().dg_solver_step_host(self.h, _dp(q_in) if q_in is not None else None, nsteps,
+                                         _dp(q_out) if q_out is not None else None))
+
+    def step_timed(self):
+        ms = (C.c_float * 7)()
+        _check(lib().dg_solver_step_timed(self.h, ms))
+        return np.array(ms[:], dtype=np.float64)
+
+    @property
+    def stream(self):
+        return lib().dg_solver_stream(self.h)
+
+
+class PinnedArray:
+    """A float64 numpy view of pinned host memory (dg_host_alloc)."""
+
+    def __init__(self, n):
+        self.ptr = lib().dg_host_alloc(n * 8)
+        if not self.ptr:
+            raise MemoryError("pinned allocation failed")
+        self.array = np.ctypeslib.as_array(C.cast(self.ptr, C.POINTER(C.c_double)), shape=(n,))
+
+    def __del__(self):
+        if getattr(self, "ptr", None) and _lib is not None:
+            _lib.dg_host_free(self.ptr)
+            self.ptr = None
+
+
+class Event:
+    def __init__(self):
+        self.h = lib().dg_event_create()
+
+    def record(self, stream):
+        _check(lib().dg_event_record(self.h, stream))
+
+    def elapsed_ms(self, end):
+        return lib().dg_event_elapsed_ms(self.h, end.h)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.dg_event_destroy(self.h)
+
+
+def l2_flush(stream):
+    _check(lib().dg_l2_flush(stream))
+
+
+def fp64_peak_gflops():
+    return lib().dg_fp64_peak_gflops()

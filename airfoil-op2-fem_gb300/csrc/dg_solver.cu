@@ -1,0 +1,704 @@
+// Native DG Euler solver on one GPU: the plain fused path.
+//
+// One SSPRK3 stage is two kernels:
+//   face_kernel  one thread per face node of every interior and boundary edge: gathers both
+//                traces (src/get_neighbour_q.h), builds the boundary ghost state
+//                (src/get_bedge_q.h), evaluates the Roe flux once per face node
+//                (src/euler_rhs.h:120-220) and writes it, scaled by each side's fscale, into
+//                both cells' face slots.  Each slot has exactly one writer: no atomics.
+//   elem_kernel  32 cells x Np node-warps per block: nodal Euler fluxes combined with the
+//                (affine, per-cell) metric terms, one contraction of [Drw | Dsw | -LIFT]
+//                (operators in constant memory, warp-uniform rows) against
+//                [Fr ; Fs ; flux] staged in shared memory (src/euler_rhs.h:226-247,284-286),
+//                then the SSPRK3 stage combine in registers (src/set_workingQ.h,
+//                src/update_Q.h, in Shu-Osher form) and, in the last stage, the calc_dt
+//                maximum (src/calc_dt.h) on the new state.
+// plus a one-thread finalize kernel per step (t += dt; dt = (1/dt1)*cfl).  dt never leaves the
+// device, so a whole step is a fixed launch sequence that is captured once in a CUDA graph.
+//
+// Data layout in HBM (K cells, order N, Np=(N+1)(N+2)/2, Nfp=N+1):
+//   q, W   [K][Np][4] doubles (the reference's AoS, src/airfoil.cpp:171)
+//   flux   [K][3][Nfp][4]
+//   geo    [K][16]: rx, ry, sx, sy, then (nx, ny, fscale) of faces 0..2, 3 pad
+//   edges  int4 {cL, cR, fL | fR << 2 | reverse << 4, 0};  bedges int4 {cell, face, type, 0}
+//   bxy    [nB][Nfp][2] boundary face-node coordinates (vortex boundary)
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "dg_device.cuh"
+#include "dg_mesh.h"
+#include "dg_ops.h"
+#include "dg_solver.h"
+
+namespace dg {
+
+constexpr int np_of(int n) { return (n + 1) * (n + 2) / 2; }
+constexpr int nk_of(int n) { return 2 * np_of(n) + 3 * (n + 1); }
+
+// ---------------------------------------------------------------- operators in constant memory
+__constant__ double c_A1[np_of(1) * nk_of(1)];
+__constant__ double c_A2[np_of(2) * nk_of(2)];
+__constant__ double c_A3[np_of(3) * nk_of(3)];
+__constant__ double c_A4[np_of(4) * nk_of(4)];
+__constant__ double c_A5[np_of(5) * nk_of(5)];
+__constant__ double c_A6[np_of(6) * nk_of(6)];
+// calc_dt face points of each volume node: up to two faces whose fscale multiplies the node's
+// wave speed (-1 = none), after the index rule of src/calc_dt.h:11.
+__constant__ int c_dtf[7][28 * 2];
+// reference-node coordinates (r, s) per order, for node positions.
+__constant__ double c_rs[7][2 * 28];
+
+template <int N>
+__device__ __forceinline__ double opA(int idx) {
+  if constexpr (N == 1) return c_A1[idx];
+  else if constexpr (N == 2) return c_A2[idx];
+  else if constexpr (N == 3) return c_A3[idx];
+  else if constexpr (N == 4) return c_A4[idx];
+  else if constexpr (N == 5) return c_A5[idx];
+  else return c_A6[idx];
+}
+
+__device__ __forceinline__ double2 ld2(const double *p) { return *reinterpret_cast<const double2 *>(p); }
+__device__ __forceinline__ void st2(double *p, double a, double b) {
+  *reinterpret_cast<double2 *>(p) = make_double2(a, b);
+}
+
+// ---------------------------------------------------------------- face kernel
+template <int N>
+__global__ void __launch_bounds__(256) face_kernel(const Inst d, const int stage) {
+  constexpr int Np = np_of(N), Nfp = N + 1;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int total = (d.nE + d.nB) * Nfp;
+  if (tid >= total) return;
+  const int e = tid / Nfp, i = tid - e * Nfp;
+  const Phys &P = d.P;
+  double qm[4], qp[4], f2[4];
+  if (e < d.nE) {
+    const int4 ed = __ldg(&d.edges[e]);
+    const int cL = ed.x, cR = ed.y, fL = ed.z & 3, fR = (ed.z >> 2) & 3;
+    const int iR = (ed.z >> 4) ? Nfp - 1 - i : i;
+    const int nodeL = __ldg(&d.fmask[fL * Nfp + i]), nodeR = __ldg(&d.fmask[fR * Nfp + iR]);
+    const double *wl = d.W + ((size_t)cL * Np + nodeL) * 4;
+    const double *wr = d.W + ((size_t)cR * Np + nodeR) * 4;
+    double2 a = ld2(wl), b = ld2(wl + 2), c = ld2(wr), dd = ld2(wr + 2);
+    qm[0] = a.x; qm[1] = a.y; qm[2] = b.x; qm[3] = b.y;
+    qp[0] = c.x; qp[1] = c.y; qp[2] = dd.x; qp[3] = dd.y;
+    const double *gl = d.geo + (size_t)cL * 16 + 4 + 3 * fL;
+    const double nx = __ldg(gl), ny = __ldg(gl + 1);
+    const double sL = 0.5 * __ldg(gl + 2);
+    const double sR = -0.5 * __ldg(d.geo + (size_t)cR * 16 + 4 + 3 * fR + 2);
+    roe_flux2(qm, qp, nx, ny, P, f2);
+    double *ol = d.flux + (((size_t)cL * 3 + fL) * Nfp + i) * 4;
+    double *orr = d.flux + (((size_t)cR * 3 + fR) * Nfp + iR) * 4;
+    st2(ol, sL * f2[0], sL * f2[1]);
+    st2(ol + 2, sL * f2[2], sL * f2[3]);
+    st2(orr, sR * f2[0], sR * f2[1]);
+    st2(orr + 2, sR * f2[2], sR * f2[3]);
+  } else {
+    const int b = e - d.nE;
+    const int4 bd = __ldg(&d.bedges[b]);
+    const int c = bd.x, f = bd.y, type = bd.z;
+    const int node = __ldg(&d.fmask[f * Nfp + i]);
+    const double *w = d.W + ((size_t)c * Np + node) * 4;
+    double2 a = ld2(w), bb = ld2(w + 2);
+    qm[0] = a.x; qm[1] = a.y; qm[2] = bb.x; qm[3] = bb.y;
+    const double *g = d.geo + (size_t)c * 16 + 4 + 3 * f;
+    const double nx = __ldg(g), ny = __ldg(g + 1), s = 0.5 * __ldg(g + 2);
+    if (d.app == 1) {
+      const double frac = stage == 0 ? 0.0 : (stage == 1 ? 1.0 : 0.5);
+      const double tst = d.st->t + frac * d.st->dt;
+      const double *xy = d.bxy + ((size_t)b * Nfp + i) * 2;
+      vortex_state(xy[0], xy[1], tst, P, qp);
+    } else {
+      bc_state(type, qm, nx, ny, P, qp);
+    }
+    roe_flux2(qm, qp, nx, ny, P, f2);
+    double *o = d.flux + (((size_t)c * 3 + f) * Nfp + i) * 4;
+    st2(o, s * f2[0], s * f2[1]);
+    st2(o + 2, s * f2[2], s * f2[3]);
+  }
+}
+
+// ---------------------------------------------------------------- element kernel
+// stage 0: W = W + dt*L           (W holds q at the start of a step)
+// stage 1: W = 3/4 q + 1/4 (W + dt*L)
+// stage 2: q = W = 1/3 q + 2/3 (W + dt*L), then the calc_dt maximum over the new q
+// stage 3: rhs_out = L (one right-hand side, no combine)
+template <int N>
+__global__ void __launch_bounds__(32 * np_of(N)) elem_kernel(const Inst d, const int stage) {
+  constexpr int Np = np_of(N), Nfp = N + 1, NK = nk_of(N);
+  extern __shared__ double2 X[];  // [NK][32][2] double2 = [NK][32] x 4 doubles
+  const int lane = threadIdx.x, i = threadIdx.y;
+  const int e0 = blockIdx.x * 32;
+  const int e = e0 + lane;
+  const bool live = e < d.K;
+  const Phys &P = d.P;
+
+  double w[4] = {0.0, 0.0, 0.0, 0.0};
+  double g[4] = {0.0, 0.0, 0.0, 0.0};
+  if (live) {
+    const double *wp = d.W + ((size_t)e * Np + i) * 4;
+    double2 a = ld2(wp), b = ld2(wp + 2);
+    w[0] = a.x; w[1] = a.y; w[2] = b.x; w[3] = b.y;
+    double2 ga = ld2(d.geo + (size_t)e * 16), gb = ld2(d.geo + (size_t)e * 16 + 2);
+    g[0] = ga.x; g[1] = ga.y; g[2] = gb.x; g[3] = gb.y;
+  }
+  // Nodal fluxes (src/euler_rhs.h:7-23) combined with the metric terms:
+  //   Fr = rx F + ry G,  Fs = sx F + sy G   (rhs = Drw Fr + Dsw Fs - LIFT flux)
+  {
+    const double rx = g[0], ry = g[1], sx = g[2], sy = g[3];
+    double fr0 = 0, fr1 = 0, fr2 = 0, fr3 = 0, fs0 = 0, fs1 = 0, fs2 = 0, fs3 = 0;
+    if (live) {
+      const double ir = rcp(w[0]);
+      const double u = w[1] * ir, v = w[2] * ir;
+      const double p = P.gm1 * fma(-0.5, fma(w[1], u, w[2] * v), w[3]);
+      const double ep = w[3] + p;
+      const double U = fma(rx, u, ry * v), V = fma(sx, u, sy * v);
+      fr0 = fma(rx, w[1], ry * w[2]);
+      fr1 = fma(w[1], U, rx * p);
+      fr2 = fma(w[2], U, ry * p);
+      fr3 = U * ep;
+      fs0 = fma(sx, w[1], sy * w[2]);
+      fs1 = fma(w[1], V, sx * p);
+      fs2 = fma(w[2], V, sy * p);
+      fs3 = V * ep;
+    }
+    X[(i * 32 + lane) * 2] = make_double2(fr0, fr1);
+    X[(i * 32 + lane) * 2 + 1] = make_double2(fr2, fr3);
+    X[((Np + i) * 32 + lane) * 2] = make_double2(fs0, fs1);
+    X[((Np + i) * 32 + lane) * 2 + 1] = make_double2(fs2, fs3);
+  }
+  // Face fluxes of the block's 32 cells: contiguous in HBM, scattered into [k][cell] order.
+  {
+    const int nthr = 32 * Np, tid = i * 32 + lane;
+    const size_t base = (size_t)e0 * 3 * Nfp;
+    for (int j = tid; j < 32 * 3 * Nfp * 2; j += nthr) {
+      const int slot = j >> 1, h = j & 1;
+      const int el = slot / (3 * Nfp), f = slot - el * (3 * Nfp);
+      double2 v = make_double2(0.0, 0.0);
+      if (e0 + el < d.K) v = ld2(d.flux + (base + slot) * 4 + 2 * h);
+      X[((2 * Np + f) * 32 + el) * 2 + h] = v;
+    }
+  }
+  __syncthreads();
+  // Contraction: row i of [Drw | Dsw | -LIFT] against the staged columns.
+  double r0 = 0.0, r1 = 0.0, r2 = 0.0, r3 = 0.0;
+#pragma unroll
+  for (int k = 0; k < NK; k++) {
+    const double c = opA<N>(i * NK + k);
+    const double2 x01 = X[(k * 32 + lane) * 2], x23 = X[(k * 32 + lane) * 2 + 1];
+    r0 = fma(c, x01.x, r0);
+    r1 = fma(c, x01.y, r1);
+    r2 = fma(c, x23.x, r2);
+    r3 = fma(c, x23.y, r3);
+  }
+  // Stage combine.  Lanes past the last cell keep running (no early return) so that every lane
+  // reaches the warp reduction below.
+  const size_t off = ((size_t)(live ? e : 0) * Np + i) * 4;
+  double *wp = d.W + off;
+  if (stage == 3) {
+    if (live) {
+      double *o = d.rhs_out + off;
+      st2(o, r0, r1);
+      st2(o + 2, r2, r3);
+    }
+    return;
+  }
+  const double dt = d.st->dt;
+  double n0 = fma(dt, r0, w[0]), n1 = fma(dt, r1, w[1]), n2 = fma(dt, r2, w[2]), n3 = fma(dt, r3, w[3]);
+  if (stage == 0) {
+    if (live) {
+      st2(wp, n0, n1);
+      st2(wp + 2, n2, n3);
+    }
+    return;
+  }
+  double *qp = d.q + off;
+  double2 qa = make_double2(0.0, 0.0), qb = make_double2(0.0, 0.0);
+  if (live) {
+    qa = ld2(qp);
+    qb = ld2(qp + 2);
+  }
+  if (stage == 1) {
+    if (live) {
+      n0 = fma(0.25, n0, 0.75 * qa.x);
+      n1 = fma(0.25, n1, 0.75 * qa.y);
+      n2 = fma(0.25, n2, 0.75 * qb.x);
+      n3 = fma(0.25, n3, 0.75 * qb.y);
+      st2(wp, n0, n1);
+      st2(wp + 2, n2, n3);
+    }
+    return;
+  }
+  const double third = 1.0 / 3.0, two_third = 2.0 / 3.0;
+  n0 = fma(two_third, n0, third * qa.x);
+  n1 = fma(two_third, n1, third * qa.y);
+  n2 = fma(two_third, n2, third * qb.x);
+  n3 = fma(two_third, n3, third * qb.y);
+  if (live) {
+    st2(qp, n0, n1);
+    st2(qp + 2, n2, n3);
+    st2(wp, n0, n1);
+    st2(wp + 2, n2, n3);
+    if (bad_density(n0)) atomicOr(&d.st->err, 1u);
+  }
+  if (d.dt_mode == 0) {
+    // src/calc_dt.h: (N+1)^2 * 0.5 * fscale * (|v| + c) at the face points of this node.
+    const int fa = c_dtf[N][2 * i], fb = c_dtf[N][2 * i + 1];
+    unsigned long long best = 0ull;
+    if (live && fa >= 0) {
+      const double ir = rcp(n0);
+      const double u = n1 * ir, v = n2 * ir;
+      const double v2 = fma(u, u, v * v);
+      const double p = P.gm1 * fma(-0.5 * n0, v2, n3);
+      const double cs = sqrt(fabs(P.gam * p * ir));
+      const double spd = ((N + 1) * (N + 1) * 0.5) * (sqrt(v2) + cs);
+      const double *ge = d.geo + (size_t)e * 16 + 6;
+      const double fs = fb >= 0 ? fmax(ge[3 * fa], ge[3 * fb]) : ge[3 * fa];
+      best = (unsigned long long)__double_as_longlong(spd * fs);
+    }
+    // warp max on the bit patterns of non-negative doubles (all 32 lanes take part)
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long x = __shfl_xor_sync(0xffffffffu, best, o);
+      best = x > best ? x : best;
+    }
+    if (lane == 0 && best) atomicMax(&d.st->dt1_bits, best);
+  }
+}
+
+// ---------------------------------------------------------------- per-step finalize
+__global__ void finalize_kernel(StepState *st, int dt_mode, double *dt_hist, unsigned long long dt_hist_len) {
+  if (threadIdx.x | blockIdx.x) return;
+  if (dt_hist && st->step < dt_hist_len) dt_hist[st->step] = st->dt;
+  st->t += st->dt;
+  st->step += 1;
+  if (dt_mode == 0) {
+    const double dt1 = __longlong_as_double((long long)st->dt1_bits);
+    st->dt = (1.0 / dt1) * st->cfl;
+    st->dt1_bits = 0ull;
+  }
+}
+
+// ---------------------------------------------------------------- set-up kernels
+// Affine geometry from the vertices: x = -(r+s)/2 x0 + (1+r)/2 x1 + (1+s)/2 x2, so
+// xr = (x1-x0)/2, xs = (x2-x0)/2; J = xr ys - xs yr; rx = ys/J, sx = -yr/J, ry = -xs/J,
+// sy = xr/J; face normals as src/init_grid.h:81-105 with fscale = sJ/J.  Explicit rounding
+// intrinsics keep the result independent of FMA contraction.
+__global__ void geometry_kernel(int K, const double *coords, const int *cells, double *geo) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= K) return;
+  const int a = cells[3 * c], b = cells[3 * c + 1], e = cells[3 * c + 2];
+  const double x0 = coords[2 * a], y0 = coords[2 * a + 1];
+  const double xr = __dmul_rn(0.5, __dsub_rn(coords[2 * b], x0));
+  const double yr = __dmul_rn(0.5, __dsub_rn(coords[2 * b + 1], y0));
+  const double xs = __dmul_rn(0.5, __dsub_rn(coords[2 * e], x0));
+  const double ys = __dmul_rn(0.5, __dsub_rn(coords[2 * e + 1], y0));
+  const double J = __dadd_rn(__dmul_rn(-xs, yr), __dmul_rn(xr, ys));
+  double *g = geo + (size_t)c * 16;
+  g[0] = __ddiv_rn(ys, J);
+  g[1] = __ddiv_rn(-xs, J);
+  g[2] = __ddiv_rn(-yr, J);
+  g[3] = __ddiv_rn(xr, J);
+  const double fnx[3] = {yr, __dsub_rn(ys, yr), -ys};
+  const double fny[3] = {-xr, __dsub_rn(xr, xs), xs};
+  for (int f = 0; f < 3; f++) {
+    const double sJ = __dsqrt_rn(__dadd_rn(__dmul_rn(fnx[f], fnx[f]), __dmul_rn(fny[f], fny[f])));
+    g[4 + 3 * f] = __ddiv_rn(fnx[f], sJ);
+    g[5 + 3 * f] = __ddiv_rn(fny[f], sJ);
+    g[6 + 3 * f] = __ddiv_rn(sJ, J);
+  }
+  g[13] = g[14] = g[15] = 0.0;
+}
+
+// Node position with the operation order of src/init_grid.h:19-54 (cblas dcopy/daxpy/dscal).
+__device__ __forceinline__ double node_coord(double v0, double v1, double v2, double r, double s) {
+  double x = __dmul_rn(__dmul_rn(0.5, v1), __dadd_rn(1.0, r));
+  x = __dadd_rn(x, __dmul_rn(__dmul_rn(0.5, v2), __dadd_rn(1.0, s)));
+  x = __dadd_rn(x, __dmul_rn(__dmul_rn(-0.5, v0), __dadd_rn(s, r)));
+  return x;
+}
+
+// Initial state: freestream (src/set_ic.h) or the isentropic vortex at t=0
+// (vortex/src/set_ic.h).  One thread per (cell, node).
+template <int N>
+__global__ void set_ic_kernel(const Inst d, const double *coords, const int *cells) {
+  constexpr int Np = np_of(N);
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= (long long)d.K * Np) return;
+  const int c = (int)(tid / Np), i = (int)(tid - (long long)c * Np);
+  double q[4];
+  if (d.app == 1) {
+    const int a = cells[3 * c], b = cells[3 * c + 1], e = cells[3 * c + 2];
+    const double r = c_rs[N][i], s = c_rs[N][Np + i];
+    const double x = node_coord(coords[2 * a], coords[2 * b], coords[2 * e], r, s);
+    const double y = node_coord(coords[2 * a + 1], coords[2 * b + 1], coords[2 * e + 1], r, s);
+    vortex_state(x, y, 0.0, d.P, q);
+  } else {
+    q[0] = d.P.rinf;
+    q[1] = d.P.rinf * d.P.uinf;
+    q[2] = d.P.rinf * d.P.vinf;
+    q[3] = d.P.einf;
+  }
+  double *qp = d.q + (size_t)tid * 4, *wp = d.W + (size_t)tid * 4;
+  st2(qp, q[0], q[1]); st2(qp + 2, q[2], q[3]);
+  st2(wp, q[0], q[1]); st2(wp + 2, q[2], q[3]);
+}
+
+// Boundary face-node coordinates for the vortex boundary state.
+template <int N>
+__global__ void bxy_kernel(const Inst d, const double *coords, const int *cells, double *bxy) {
+  constexpr int Nfp = N + 1, Np = np_of(N);
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= d.nB * Nfp) return;
+  const int b = tid / Nfp, i = tid - b * Nfp;
+  const int4 bd = d.bedges[b];
+  const int c = bd.x, node = d.fmask[bd.y * Nfp + i];
+  const int a = cells[3 * c], bb = cells[3 * c + 1], e = cells[3 * c + 2];
+  const double r = c_rs[N][node], s = c_rs[N][Np + node];
+  bxy[2 * tid] = node_coord(coords[2 * a], coords[2 * bb], coords[2 * e], r, s);
+  bxy[2 * tid + 1] = node_coord(coords[2 * a + 1], coords[2 * bb + 1], coords[2 * e + 1], r, s);
+}
+
+// calc_dt over the current q into st->dt1_bits (src/calc_dt.h, seeded from 0 as
+// src/airfoil.cpp:231).
+template <int N>
+__global__ void calc_dt_kernel(const Inst d) {
+  constexpr int Np = np_of(N);
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long best = 0ull;
+  if (tid < (long long)d.K * Np) {
+    const int c = (int)(tid / Np), i = (int)(tid - (long long)c * Np);
+    const int fa = c_dtf[N][2 * i], fb = c_dtf[N][2 * i + 1];
+    if (fa >= 0) {
+      const double *qp = d.q + (size_t)tid * 4;
+      const double ir = rcp(qp[0]);
+      const double u = qp[1] * ir, v = qp[2] * ir;
+      const double v2 = fma(u, u, v * v);
+      const double p = d.P.gm1 * fma(-0.5 * qp[0], v2, qp[3]);
+      const double cs = sqrt(fabs(d.P.gam * p * ir));
+      const double spd = ((N + 1) * (N + 1) * 0.5) * (sqrt(v2) + cs);
+      const double fs = fb >= 0 ? fmax(d.geo[(size_t)c * 16 + 6 + 3 * fa], d.geo[(size_t)c * 16 + 6 + 3 * fb])
+                                : d.geo[(size_t)c * 16 + 6 + 3 * fa];
+      best = (unsigned long long)__double_as_longlong(spd * fs);
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    const unsigned long long o = __shfl_xor_sync(0xffffffffu, best, off);
+    best = o > best ? o : best;
+  }
+  if ((threadIdx.x & 31) == 0 && best) atomicMax(&d.st->dt1_bits, best);
+}
+
+// Sums of squared nodal errors against the analytic vortex (vortex/src/l2_error.h:3-29),
+// one partial per cell so the host can add them in cell order.
+template <int N>
+__global__ void l2_error_kernel(const Inst d, const double *coords, const int *cells, double *part) {
+  constexpr int Np = np_of(N);
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= d.K) return;
+  const int a = cells[3 * c], b = cells[3 * c + 1], e = cells[3 * c + 2];
+  double acc[4] = {0, 0, 0, 0};
+  const double t = d.st->t;
+  for (int i = 0; i < Np; i++) {
+    const double r = c_rs[N][i], s = c_rs[N][Np + i];
+    const double x = node_coord(coords[2 * a], coords[2 * b], coords[2 * e], r, s);
+    const double y = node_coord(coords[2 * a + 1], coords[2 * b + 1], coords[2 * e + 1], r, s);
+    double ex[4];
+    vortex_state(x, y, t, d.P, ex);
+    const double *qp = d.q + ((size_t)c * Np + i) * 4;
+    for (int k = 0; k < 4; k++) acc[k] += (qp[k] - ex[k]) * (qp[k] - ex[k]);
+  }
+  for (int k = 0; k < 4; k++) part[4 * (size_t)c + k] = acc[k];
+}
+
+// ---------------------------------------------------------------- launch helpers
+template <int N>
+static void launch_face(const Inst &d, int stage, cudaStream_t s) {
+  const int nf = (d.nE + d.nB) * (N + 1);
+  face_kernel<N><<<(nf + 255) / 256, 256, 0, s>>>(d, stage);
+}
+
+template <int N>
+static void launch_elem(const Inst &d, int stage, cudaStream_t s) {
+  constexpr int Np = np_of(N), NK = nk_of(N);
+  const size_t smem = (size_t)NK * 32 * 4 * sizeof(double);
+  elem_kernel<N><<<(d.K + 31) / 32, dim3(32, Np), smem, s>>>(d, stage);
+}
+
+template <int N>
+static void launch_stage(const Inst &d, int stage, cudaStream_t s) {
+  launch_face<N>(d, stage, s);
+  launch_elem<N>(d, stage, s);
+}
+
+template <int N>
+static cudaError_t set_smem_attr() {
+  const size_t smem = (size_t)nk_of(N) * 32 * 4 * sizeof(double);
+  return cudaFuncSetAttribute(elem_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+#define DG_DISPATCH(N_, CALL)            \
+  switch (N_) {                          \
+    case 1: { constexpr int NN = 1; CALL; } break; \
+    case 2: { constexpr int NN = 2; CALL; } break; \
+    case 3: { constexpr int NN = 3; CALL; } break; \
+    case 4: { constexpr int NN = 4; CALL; } break; \
+    case 5: { constexpr int NN = 5; CALL; } break; \
+    default: { constexpr int NN = 6; CALL; } break; \
+  }
+
+// ---------------------------------------------------------------- operator upload
+static int g_ops_loaded[7] = {0};
+static std::string g_ops_err;
+
+int load_order_constants(int N, std::string &err) {
+  if (N < 1 || N > 6) { err = "order N must be in 1..6"; return -1; }
+  if (g_ops_loaded[N]) return 0;
+  Operators o;
+  if (build_operators(N, o)) { err = "operator construction failed"; return -2; }
+  const int Np = o.Np, Nfp = o.Nfp, NK = 2 * Np + 3 * Nfp;
+  std::vector<double> A((size_t)Np * NK);
+  for (int i = 0; i < Np; i++) {
+    for (int k = 0; k < Np; k++) {
+      A[(size_t)i * NK + k] = o.Drw[(size_t)i * Np + k];
+      A[(size_t)i * NK + Np + k] = o.Dsw[(size_t)i * Np + k];
+    }
+    for (int k = 0; k < 3 * Nfp; k++) A[(size_t)i * NK + 2 * Np + k] = -o.LIFT[(size_t)i * 3 * Nfp + k];
+  }
+  const void *syms[7] = {nullptr, c_A1, c_A2, c_A3, c_A4, c_A5, c_A6};
+  cudaError_t ce = cudaMemcpyToSymbol(syms[N], A.data(), A.size() * sizeof(double));
+  // calc_dt face points: for node i, the faces f of face points k with FMASK[k] == i; the
+  // fscale index follows src/calc_dt.h:11 (fscale[FMASK[k]], read as face FMASK[k] / Nfp while
+  // Np <= 3 Nfp, i.e. N <= 4) or the face point's own face k / Nfp for N >= 5.
+  int dtf[28 * 2];
+  for (int i = 0; i < 28 * 2; i++) dtf[i] = -1;
+  for (int k = 0; k < 3 * Nfp; k++) {
+    const int node = o.FMASK[k];
+    const int face = (Np <= 3 * Nfp) ? node / Nfp : k / Nfp;
+    if (dtf[2 * node] < 0) dtf[2 * node] = face;
+    else if (dtf[2 * node] != face && dtf[2 * node + 1] < 0) dtf[2 * node + 1] = face;
+  }
+  if (ce == cudaSuccess) ce = cudaMemcpyToSymbol(c_dtf, dtf, sizeof(dtf), (size_t)N * sizeof(dtf));
+  double rs[2 * 28] = {0};
+  for (int i = 0; i < Np; i++) {
+    rs[i] = o.r[i];
+    rs[Np + i] = o.s[i];
+  }
+  if (ce == cudaSuccess) ce = cudaMemcpyToSymbol(c_rs, rs, sizeof(rs), (size_t)N * sizeof(rs));
+  if (ce == cudaSuccess) {
+    DG_DISPATCH(N, ce = set_smem_attr<NN>());
+  }
+  if (ce != cudaSuccess) { err = std::string("constant upload: ") + cudaGetErrorString(ce); return -3; }
+  g_ops_loaded[N] = 1;
+  return 0;
+}
+
+// ---------------------------------------------------------------- Solver (host)
+#define CK(x)                                                                  \
+  do {                                                                         \
+    cudaError_t e_ = (x);                                                      \
+    if (e_ != cudaSuccess) {                                                   \
+      err = std::string(#x) + ": " + cudaGetErrorString(e_);                   \
+      return -100;                                                             \
+    }                                                                          \
+  } while (0)
+
+Solver::~Solver() {
+  if (graph_exec) cudaGraphExecDestroy(graph_exec);
+  if (graph) cudaGraphDestroy(graph);
+  for (void *p : allocs) cudaFree(p);
+  if (stream) cudaStreamDestroy(stream);
+}
+
+void *Solver::dalloc(size_t bytes) {
+  void *p = nullptr;
+  if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) return nullptr;
+  allocs.push_back(p);
+  return p;
+}
+
+int Solver::create(const Config &c, const Mesh &m, std::string &err) {
+  cfg = c;
+  if (int rc = validate(m, err)) return rc;
+  if (int rc = load_order_constants(c.N, err)) return rc;
+  CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  const int N = c.N, Np = np_of(N), Nfp = N + 1;
+  Operators o;
+  build_operators(N, o);
+  K = m.n_cells();
+  d = Inst();
+  d.N = N;
+  d.K = K;
+  d.nE = m.n_edges();
+  d.nB = m.n_bedges();
+  d.app = c.app;
+  d.dt_mode = c.dt_mode;
+  const double gam = c.gam;
+  d.P.gam = gam;
+  d.P.gm1 = gam - 1.0;
+  // Freestream as src/airfoil.cpp:79-99.
+  double u, v, e;
+  if (c.alpha_deg != 0.0) {
+    u = std::sin((M_PI / 2.0) - (c.alpha_deg * M_PI / 180.0)) * std::sqrt(gam * c.p_inf / c.rho_inf) * c.mach;
+    v = std::cos((M_PI / 2.0) - (c.alpha_deg * M_PI / 180.0)) * std::sqrt(gam * c.p_inf / c.rho_inf) * c.mach;
+    e = c.p_inf / (gam - 1.0) + 0.5 * c.rho_inf * (u * u + v * v);
+  } else {
+    u = std::sqrt(gam * c.p_inf / c.rho_inf) * c.mach;
+    v = 0.0;
+    e = c.p_inf / (gam - 1.0) + 0.5 * c.rho_inf * (u * u);
+  }
+  d.P.rinf = c.rho_inf;
+  d.P.uinf = u;
+  d.P.vinf = v;
+  d.P.pinf = c.p_inf;
+  d.P.einf = e;
+  d.P.vx0 = c.vortex_x0;
+  d.P.vy0 = c.vortex_y0;
+  d.P.vbeta = c.vortex_beta;
+
+  std::vector<int4> edges(d.nE), bedges(d.nB);
+  for (int i = 0; i < d.nE; i++) {
+    const int cL = m.edge2cells[2 * i], cR = m.edge2cells[2 * i + 1];
+    const int fL = m.edgeNum[2 * i], fR = m.edgeNum[2 * i + 1];
+    // src/get_neighbour_q.h:10-34: vertex fL of L against vertex fR of R, exact comparison
+    const int vL = m.cell2nodes[3 * cL + fL], vR = m.cell2nodes[3 * cR + fR];
+    const bool rev = !(m.coords[2 * vL] == m.coords[2 * vR] && m.coords[2 * vL + 1] == m.coords[2 * vR + 1]);
+    edges[i] = make_int4(cL, cR, fL | (fR << 2) | ((rev ? 1 : 0) << 4), 0);
+  }
+  for (int i = 0; i < d.nB; i++)
+    bedges[i] = make_int4(m.bedge2cell[i], m.bedgeNum[i], m.bedge_type.empty() ? 2 : m.bedge_type[i], 0);
+
+  const size_t nq = (size_t)K * Np * 4;
+  d.q = (double *)dalloc(nq * 8);
+  d.W = (double *)dalloc(nq * 8);
+  d.flux = (double *)dalloc((size_t)K * 3 * Nfp * 4 * 8);
+  double *geo = (double *)dalloc((size_t)K * 16 * 8);
+  d.geo = geo;
+  int4 *de = (int4 *)dalloc(sizeof(int4) * d.nE), *db = (int4 *)dalloc(sizeof(int4) * d.nB);
+  d.edges = de;
+  d.bedges = db;
+  int *fm = (int *)dalloc(sizeof(int) * 3 * Nfp);
+  d.fmask = fm;
+  d.st = (StepState *)dalloc(sizeof(StepState));
+  coords_d = (double *)dalloc(m.coords.size() * 8);
+  cells_d = (int *)dalloc(m.cell2nodes.size() * 4);
+  double *bxy = (double *)dalloc((size_t)d.nB * Nfp * 2 * 8);
+  d.bxy = bxy;
+  for (void *p : allocs)
+    if (!p) { err = "cudaMalloc failed"; return -101; }
+  CK(cudaMemcpyAsync(de, edges.data(), sizeof(int4) * d.nE, cudaMemcpyHostToDevice, stream));
+  CK(cudaMemcpyAsync(db, bedges.data(), sizeof(int4) * d.nB, cudaMemcpyHostToDevice, stream));
+  CK(cudaMemcpyAsync(fm, o.FMASK.data(), sizeof(int) * 3 * Nfp, cudaMemcpyHostToDevice, stream));
+  CK(cudaMemcpyAsync(coords_d, m.coords.data(), m.coords.size() * 8, cudaMemcpyHostToDevice, stream));
+  CK(cudaMemcpyAsync(cells_d, m.cell2nodes.data(), m.cell2nodes.size() * 4, cudaMemcpyHostToDevice, stream));
+  CK(cudaMemsetAsync(d.flux, 0, (size_t)K * 3 * Nfp * 4 * 8, stream));
+  geometry_kernel<<<(K + 127) / 128, 128, 0, stream>>>(K, coords_d, cells_d, geo);
+  if (d.nB) DG_DISPATCH(N, (bxy_kernel<NN><<<(d.nB * Nfp + 127) / 128, 128, 0, stream>>>(d, coords_d, cells_d, bxy)));
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(stream));
+  return 0;
+}
+
+int Solver::init(std::string &err) {
+  const int Np = np_of(cfg.N);
+  StepState s0;
+  std::memset(&s0, 0, sizeof(s0));
+  s0.cfl = cfg.cfl;
+  CK(cudaMemcpyAsync(d.st, &s0, sizeof(s0), cudaMemcpyHostToDevice, stream));
+  const long long n = (long long)K * Np;
+  DG_DISPATCH(cfg.N, (set_ic_kernel<NN><<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(d, coords_d, cells_d)));
+  DG_DISPATCH(cfg.N, (calc_dt_kernel<NN><<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(d)));
+  CK(cudaGetLastError());
+  return set_dt_from_max(err);
+}
+
+// dt = (1/dt1)*cfl from the accumulated maximum, then clear it (src/airfoil.cpp:237).
+int Solver::set_dt_from_max(std::string &err) {
+  StepState s;
+  CK(cudaMemcpyAsync(&s, d.st, sizeof(s), cudaMemcpyDeviceToHost, stream));
+  CK(cudaStreamSynchronize(stream));
+  const double dt1 = __builtin_bit_cast(double, s.dt1_bits);
+  if (!(dt1 > 0.0) || !std::isfinite(dt1)) { err = "calc_dt produced a non-positive maximum"; return -5; }
+  s.dt = (1.0 / dt1) * cfg.cfl;
+  s.dt1_bits = 0ull;
+  CK(cudaMemcpyAsync(d.st, &s, sizeof(s), cudaMemcpyHostToDevice, stream));
+  CK(cudaStreamSynchronize(stream));
+  return 0;
+}
+
+void Solver::enqueue_step(cudaStream_t s) {
+  DG_DISPATCH(cfg.N, (launch_stage<NN>(d, 0, s), launch_stage<NN>(d, 1, s), launch_stage<NN>(d, 2, s)));
+  finalize_kernel<<<1, 32, 0, s>>>(d.st, d.dt_mode, d.dt_hist, d.dt_hist_len);
+}
+
+// One step with an event recorded after each of its seven kernels (ev[0] is recorded by the
+// caller before the step).
+void Solver::enqueue_step_events(cudaStream_t s, cudaEvent_t *ev) {
+  for (int stage = 0; stage < 3; stage++) {
+    DG_DISPATCH(cfg.N, launch_face<NN>(d, stage, s));
+    cudaEventRecord(ev[1 + 2 * stage], s);
+    DG_DISPATCH(cfg.N, launch_elem<NN>(d, stage, s));
+    cudaEventRecord(ev[2 + 2 * stage], s);
+  }
+  finalize_kernel<<<1, 32, 0, s>>>(d.st, d.dt_mode, d.dt_hist, d.dt_hist_len);
+  cudaEventRecord(ev[7], s);
+}
+
+int Solver::build_graph(std::string &err) {
+  if (graph_exec) return 0;
+  CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+  enqueue_step(stream);
+  cudaError_t ce = cudaStreamEndCapture(stream, &graph);
+  if (ce != cudaSuccess) { err = std::string("graph capture: ") + cudaGetErrorString(ce); return -6; }
+  CK(cudaGraphInstantiate(&graph_exec, graph, 0));
+  return 0;
+}
+
+int Solver::step(int nsteps, bool use_graph, std::string &err) {
+  if (use_graph) {
+    if (int rc = build_graph(err)) return rc;
+    for (int i = 0; i < nsteps; i++) CK(cudaGraphLaunch(graph_exec, stream));
+  } else {
+    for (int i = 0; i < nsteps; i++) enqueue_step(stream);
+    CK(cudaGetLastError());
+  }
+  return 0;
+}
+
+int Solver::rhs(double *out_dev, std::string &err) {
+  d.rhs_out = out_dev;
+  DG_DISPATCH(cfg.N, (launch_stage<NN>(d, 3, stream)));
+  d.rhs_out = nullptr;
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int Solver::l2_error(double err4[4], std::string &err) {
+  double *part = nullptr;
+  CK(cudaMallocAsync((void **)&part, (size_t)K * 4 * 8, stream));
+  DG_DISPATCH(cfg.N, (l2_error_kernel<NN><<<(K + 127) / 128, 128, 0, stream>>>(d, coords_d, cells_d, part)));
+  std::vector<double> h((size_t)K * 4);
+  cudaError_t ce = cudaMemcpyAsync(h.data(), part, h.size() * 8, cudaMemcpyDeviceToHost, stream);
+  cudaFreeAsync(part, stream);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(stream);
+  if (ce != cudaSuccess) { err = std::string("l2_error: ") + cudaGetErrorString(ce); return -100; }
+  for (int k = 0; k < 4; k++) err4[k] = 0.0;
+  for (int c = 0; c < K; c++)
+    for (int k = 0; k < 4; k++) err4[k] += h[4 * (size_t)c + k];
+  return 0;
+}
+
+int Solver::state(StepState &s, std::string &err) {
+  CK(cudaMemcpyAsync(&s, d.st, sizeof(s), cudaMemcpyDeviceToHost, stream));
+  CK(cudaStreamSynchronize(stream));
+  return 0;
+}
+
+}  // namespace dg

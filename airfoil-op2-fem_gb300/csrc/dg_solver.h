@@ -1,0 +1,78 @@
+// Native DG Euler solver (host side of dg_solver.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "dg_device.cuh"
+#include "dg_mesh.h"
+
+namespace dg {
+
+struct Config {
+  int N = 3;
+  int app = 0;      // 0 airfoil boundary types, 1 isentropic vortex (analytic boundary and IC)
+  int dt_mode = 0;  // 0 recompute dt after every step (src/airfoil.cpp:321-331), 1 frozen
+  double cfl = 1.0; // dt = (1/dt1) * cfl
+  double gam = 1.4, mach = 0.4, alpha_deg = 0.0, p_inf = 1.0, rho_inf = 1.0;
+  double vortex_x0 = 5.0, vortex_y0 = 0.0, vortex_beta = 5.0;
+};
+
+// Device step state of one instance.
+struct StepState {
+  double dt;                    // current time step
+  double t;                     // current time
+  unsigned long long dt1_bits;  // running calc_dt maximum (bits of a non-negative double)
+  double cfl;
+  unsigned long long step;      // completed steps
+  unsigned err;                 // bit 0: a non-positive or non-finite density was produced
+  unsigned pad;
+};
+
+// Everything a kernel needs about one instance, passed by value.
+struct Inst {
+  int N, K, nE, nB;
+  int app, dt_mode;
+  const int4 *edges;
+  const int4 *bedges;
+  const int *fmask;
+  const double *bxy;
+  const double *geo;
+  double *q, *W, *flux;
+  double *rhs_out;
+  StepState *st;
+  double *dt_hist;
+  unsigned long long dt_hist_len;
+  Phys P;
+};
+
+int load_order_constants(int N, std::string &err);
+
+struct Solver {
+  Config cfg;
+  Inst d{};
+  int K = 0;
+  cudaStream_t stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  double *coords_d = nullptr;
+  int *cells_d = nullptr;
+  std::vector<void *> allocs;
+
+  ~Solver();
+  void *dalloc(size_t bytes);
+  int create(const Config &c, const Mesh &m, std::string &err);
+  int init(std::string &err);
+  int set_dt_from_max(std::string &err);
+  void enqueue_step(cudaStream_t s);
+  void enqueue_step_events(cudaStream_t s, cudaEvent_t *ev);
+  int build_graph(std::string &err);
+  int step(int nsteps, bool use_graph, std::string &err);
+  int rhs(double *out_dev, std::string &err);
+  int l2_error(double err4[4], std::string &err);
+  int state(StepState &s, std::string &err);
+  size_t q_count() const { return (size_t)K * (cfg.N + 1) * (cfg.N + 2) / 2 * 4; }
+};
+
+}  // namespace dg

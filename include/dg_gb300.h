@@ -1,0 +1,127 @@
+/* dg_gb300 — native C ABI of the GB300 DG Euler solver (plain fused path).
+ *
+ * The reference runs its hot path as OP2 loops driven from main()
+ * (src/airfoil.cpp:204-334).  This header is the fused, device-resident form
+ * of the same computation: a mesh handle (the tables src/load_mesh.cpp
+ * produces), a solver handle owning the dats on the GPU, and a step call that
+ * advances whole SSPRK3 steps without returning to the host.  The drop-in
+ * OP2 surface is in op2_gb300.h.
+ *
+ * Conventions: every function returns 0 on success or a negative code, with
+ * a message in dg_last_error() (thread-local).  Host arrays are plain C
+ * arrays in the reference's layouts:
+ *   q, workingQ   [n_cells][Np][4] doubles (src/airfoil.cpp:126,171)
+ *   maps          row-major int32, 0-based (src/load_mesh.cpp:112-146).
+ * Nothing here takes ownership of caller memory. */
+#ifndef DG_GB300_H
+#define DG_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  DG_OK = 0,
+  DG_ERR_ARG = -1,
+  DG_ERR_CUDA = -100,
+  DG_ERR_NONPHYSICAL = -200 /* a kernel saw a non-positive or non-finite density */
+};
+
+const char *dg_last_error(void);
+
+/* ------------------------------------------------------------------ meshes */
+typedef struct dg_mesh_t dg_mesh_t;
+
+/* Cells + coordinates -> edge tables with the conventions of tools/vtk2CGNS.cpp:112-199
+ * (counter-clockwise fix, face j = (v_j, v_j+1), edges in sorted-vertex-pair order). */
+int dg_mesh_from_cells(int n_nodes, const double *coords, int n_cells, const int *cell2nodes,
+                       dg_mesh_t **out);
+/* Tables as src/load_mesh.cpp:36-192 returns them (replaces load_mesh's outputs). */
+int dg_mesh_from_tables(int n_nodes, const double *coords, int n_cells, const int *cell2nodes,
+                        int n_edges, const int *edge2cells, const int *edgeNum, int n_bedges,
+                        const int *bedge2cell, const int *bedgeNum, const int *bedge_type,
+                        dg_mesh_t **out);
+/* Gmsh legacy VTK (the reference's naca0012.vtk); classify_box=1 applies
+ * src/load_mesh.cpp:147-171's boundary typing. */
+int dg_mesh_read_vtk(const char *path, int classify_box, dg_mesh_t **out);
+/* O-grid around NACA 0012; farfield 0: inflow/outflow by face-midpoint x<0, 1: characteristic. */
+int dg_mesh_naca_ogrid(int n_theta, int n_r, double stretch, double radius, int farfield,
+                       dg_mesh_t **out);
+/* [lo,hi]^2 in n x n squares cut along diagonals drawn from std::mt19937_64(seed). */
+int dg_mesh_vortex_square(int n, double lo, double hi, unsigned long long seed, dg_mesh_t **out);
+enum { DG_MESH_NODES = 0, DG_MESH_CELLS = 1, DG_MESH_EDGES = 2, DG_MESH_BEDGES = 3 };
+int dg_mesh_size(const dg_mesh_t *m, int what);
+/* name: coords (double), cell2nodes, edge2nodes, edge2cells, edgeNum, bedge2nodes,
+ * bedge2cell, bedgeNum, bedge_type (int). */
+int dg_mesh_get(const dg_mesh_t *m, const char *name, void *out);
+int dg_mesh_set_bedge_type(dg_mesh_t *m, const int *types);
+void dg_mesh_free(dg_mesh_t *m);
+
+/* Nodal operators of order N (1..6) on the reference triangle, the tables of
+ * src/constants/constant_*.h for N=4.  Any output pointer may be NULL. */
+int dg_operators(int N, double *r, double *s, double *Dr, double *Ds, double *Drw, double *Dsw,
+                 double *LIFT, int *FMASK);
+
+/* ------------------------------------------------------------------ solver */
+typedef struct {
+  int N;          /* polynomial order 1..6 */
+  int app;        /* 0: airfoil boundary types (src/get_bedge_q.h); 1: isentropic vortex */
+  int dt_mode;    /* 0: dt recomputed after every step (src/airfoil.cpp:321-331); 1: frozen */
+  double cfl;     /* dt = (1/dt1) * cfl; 1.0 in src/airfoil.cpp:237, 0.1 in vortex.cpp:223 */
+  double gam, mach, alpha_deg, p_inf, rho_inf; /* freestream (src/airfoil.cpp:79-99) */
+  double vortex_x0, vortex_y0, vortex_beta;    /* vortex/src/constants/constant_util.h:6-8 */
+} dg_config_t;
+
+typedef struct dg_solver_t dg_solver_t;
+
+int dg_solver_create(const dg_config_t *cfg, const dg_mesh_t *mesh, dg_solver_t **out);
+/* set_ic + calc_dt (src/airfoil.cpp:224-237). */
+int dg_solver_init(dg_solver_t *s);
+/* Enqueue nsteps SSPRK3 steps (src/airfoil.cpp:252-334) on the solver's stream; returns
+ * without waiting.  Each step is one launch of a captured CUDA graph. */
+int dg_solver_run(dg_solver_t *s, int nsteps);
+/* Wait for the solver's stream; DG_ERR_NONPHYSICAL if the density guard fired. */
+int dg_solver_sync(dg_solver_t *s);
+/* Copy a dat to/from the host: "q", "workingQ" ([K][Np][4]), "geo" ([K][16], get only). */
+int dg_solver_get(dg_solver_t *s, const char *name, double *host);
+int dg_solver_set(dg_solver_t *s, const char *name, const double *host);
+/* One right-hand side L(W) (get_neighbour_q + get_bedge_q + euler_rhs of one stage) for the
+ * given stage state; the vortex boundary uses the current time. */
+int dg_solver_rhs(dg_solver_t *s, const double *host_W, double *host_rhs);
+int dg_solver_time(dg_solver_t *s, double *t, double *dt, unsigned long long *step);
+/* Vortex: per-variable sums of squared nodal errors vs the analytic state (vortex/src/l2_error.h). */
+int dg_solver_l2_error(dg_solver_t *s, double *err4);
+/* Record the dt of each of the next max_steps steps; read them with dg_solver_dt_history. */
+int dg_solver_record_dt(dg_solver_t *s, int max_steps);
+int dg_solver_dt_history(dg_solver_t *s, double *out, int n);
+/* End-to-end call with host buffers: q_in -> device, nsteps steps, device -> q_out.
+ * Either pointer may be NULL to skip that copy.  Synchronous. */
+int dg_solver_step_host(dg_solver_t *s, const double *q_in, int nsteps, double *q_out);
+void *dg_solver_device_ptr(dg_solver_t *s, const char *name);
+void *dg_solver_stream(dg_solver_t *s);
+/* Launch one step as separate kernels with an event between each, wait, and write the seven
+ * kernel durations (face, elem x 3 stages, finalize) in milliseconds. */
+int dg_solver_step_timed(dg_solver_t *s, float *ms7);
+void dg_solver_free(dg_solver_t *s);
+
+/* ------------------------------------------------------------------ measurement helpers */
+void *dg_host_alloc(size_t bytes); /* pinned */
+void dg_host_free(void *p);
+void *dg_event_create(void);
+int dg_event_record(void *ev, void *stream);
+float dg_event_elapsed_ms(void *start, void *stop);
+void dg_event_destroy(void *ev);
+int dg_stream_sync(void *stream);
+/* Overwrite a device buffer larger than L2 on the stream (cache flush between timed steps). */
+int dg_l2_flush(void *stream);
+/* Measured FP64 DFMA throughput of this GPU, GFLOP/s (FMA = 2 flops). */
+double dg_fp64_peak_gflops(void);
+/* Number of kernels one dg_solver_run step launches. */
+int dg_kernels_per_step(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
