@@ -77,10 +77,13 @@ __global__ void __launch_bounds__(256) face_kernel(const Inst d, const int stage
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int total = (d.nE + d.nB) * Nfp;
   if (tid >= total) return;
-  const int e = tid / Nfp, i = tid - e * Nfp;
+  // Boundary face nodes come first: their ghost states (farfield pow, vortex exp/pow) cost
+  // several times an interior node, and last they would leave a tail on a near-idle GPU.
+  const int nbf = d.nB * Nfp;
   const Phys &P = d.P;
   double qm[4], qp[4], f2[4];
-  if (e < d.nE) {
+  if (tid >= nbf) {
+    const int e = (tid - nbf) / Nfp, i = (tid - nbf) - e * Nfp;
     const int4 ed = __ldg(&d.edges[e]);
     const int cL = ed.x, cR = ed.y, fL = ed.z & 3, fR = (ed.z >> 2) & 3;
     const int iR = (ed.z >> 4) ? Nfp - 1 - i : i;
@@ -102,7 +105,7 @@ __global__ void __launch_bounds__(256) face_kernel(const Inst d, const int stage
     st2(orr, sR * f2[0], sR * f2[1]);
     st2(orr + 2, sR * f2[2], sR * f2[3]);
   } else {
-    const int b = e - d.nE;
+    const int b = tid / Nfp, i = tid - b * Nfp;
     const int4 bd = __ldg(&d.bedges[b]);
     const int c = bd.x, f = bd.y, type = bd.z;
     const int node = __ldg(&d.fmask[f * Nfp + i]);

@@ -1,0 +1,333 @@
+"""Benchmark: DOF-stage updates/s of the FP64 DG Euler RHS + SSPRK3 step on one GB300.
+
+Workload (the plain-method airfoil case): NACA 0012 O-grid, 256 x 64 cells
+layers (K = 2*256*64 = 32768 triangles), polynomial order N = 3 (Np = 10),
+Mach 0.4, alpha 0, slip wall + characteristic farfield, SSPRK3 at CFL 0.5 with
+dt recomputed after every step.  One bench step = one SSPRK3 time step (three
+RHS evaluations) over the whole mesh; DOF = one conserved variable at one node,
+so a step is 3 * 4 * K * Np DOF-stage updates.  Synthetic mesh and freestream
+initial state (the reference publishes no benchmark data set).
+
+  python bench.py [--steps K] [--warmup W] [--gpus N] [--impl gb300|reference]
+
+value   device-resident: CUDA events around each step's graph launch on the
+        solver stream, L2 flushed (512 MB write) between steps outside the events.
+e2e     the C-ABI call dg_solver_step_host with pinned host buffers: H2D of q,
+        one step, D2H of q, timed with events on the same stream.
+roofline  FP64-bound: algorithmic flops of the dominant kernel per launch over
+        its event-timed launch duration (dg_solver_step_timed), against the DFMA
+        peak measured live on this GPU.
+--impl reference  the CPU oracle (the reference's user kernels, restated, driven
+        OP2-openmp style on all host cores) on the same workload.
+Multi-GPU: replicas only (the path is one mesh per GPU); each rank runs the
+workload, times are maxed over ranks, value = total DOF-stages / time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_ORDER = 3
+N_THETA, N_R = 256, 64
+MACH, ALPHA, CFL = 0.4, 0.0, 0.5
+METRIC = "DOF-stage updates/s FP64 on 1 GB300 (plain vs batched); adjoint/forward time at 1e-11"
+WORKLOAD = "naca0012_ogrid_256x64_K32768_N3_M0.4_a0_cfl0.5"
+
+
+def np_of(n):
+    return (n + 1) * (n + 2) // 2
+
+
+def elem_flops(n):
+    """Algorithmic FP64 flops of elem_kernel per cell and stage (FMA = 2):
+    volume contraction [Drw|Dsw] on metric-combined fluxes 16 Np^2, lift 24 Np Nfp,
+    nodal flux + metric combine 36 Np, SSPRK3 combine 16 Np."""
+    p, f = np_of(n), n + 1
+    return 16 * p * p + 24 * p * f + 36 * p + 16 * p
+
+
+def face_flops(n):
+    """Algorithmic flops of face_kernel per face node: Roe flux (rotation, Roe averages,
+    wave strengths, dissipation, rotation back; rsqrt/rcp counted as 1) plus fscale scaling."""
+    return 150
+
+
+def survey_flops(n):
+    """The reference algorithm's flops per cell-stage (4-GEMV volume form, Roe on every
+    cell face): 32 Np^2 + 24 Np Nfp + 60 Np + 330 Nfp."""
+    p, f = np_of(n), n + 1
+    return 32 * p * p + 24 * p * f + 60 * p + 330 * f
+
+
+def algo_bytes(n):
+    """Algorithmic HBM bytes per cell-stage of the fused path: 8 (32 Np/3 + 12 Nfp + 16)."""
+    p, f = np_of(n), n + 1
+    return 8 * (32 * p / 3 + 12 * f + 16)
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.proc = None
+        self.gpu = gpu_index
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world <= 1:
+        return None, 0, 1
+    import torch.distributed as dist
+    backend = "gloo"
+    dist.init_process_group(backend=backend)
+    return dist, dist.get_rank(), world
+
+
+def dist_max(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def cpu_oracle_rate(steps, nthreads, warmup=1):
+    """DOF-stage/s of the CPU oracle on the bench workload (bounded sample of `steps` steps)."""
+    import __graft_entry__ as g
+    orc, om, oo = g.load_oracle()
+    if not os.path.exists(orc.PORT_LIB):
+        orc.build(ref=False)
+    m = om.naca_ogrid(N_THETA, N_R, farfield="characteristic")
+    o = orc.Oracle(m, oo.operators(N_ORDER), orc.freestream(MACH, ALPHA), kind="port")
+    o.init(CFL)
+    if warmup:
+        o.run(warmup, nthreads=nthreads)
+    t0 = time.perf_counter()
+    o.run(steps, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    K = o.K
+    return 3 * 4 * K * np_of(N_ORDER) * steps / dt, dt
+
+
+def run_reference(args):
+    """The reference arm: the reference's user kernels (restated; the reference's own build is
+    N=4-only and cannot run this N=3 workload) on all host cores."""
+    dist, rank, world = dist_init()
+    if rank != 0:
+        return 0
+    import __graft_entry__ as g
+    orc, om, oo = g.load_oracle()
+    if not os.path.exists(orc.PORT_LIB):
+        orc.build(ref=False)
+    nthreads = os.cpu_count() or 1
+    m = om.naca_ogrid(N_THETA, N_R, farfield="characteristic")
+    o = orc.Oracle(m, oo.operators(N_ORDER), orc.freestream(MACH, ALPHA), kind="port")
+    o.init(CFL)
+    o.run(args.warmup, nthreads=nthreads)
+    t0 = time.perf_counter()
+    o.run(args.steps, nthreads=nthreads)
+    el = time.perf_counter() - t0
+    K = o.K
+    value = 3 * 4 * K * np_of(N_ORDER) * args.steps / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "DOF-stage/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "cells": K, "order": N_ORDER, "l2": "cpu (n/a)"},
+        "cpu_baseline": {"value": value, "unit": "DOF-stage/s", "cores": nthreads, "kind": "port",
+                         "sample": "%d SSPRK3 steps of the full K=%d N=3 workload" % (args.steps, K)},
+        "e2e": {"value": value, "unit": "DOF-stage/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-steps", type=int, default=40, help="CPU-baseline sample size (steps)")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+
+    dist, rank, world = dist_init()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:  # replicas: one GPU per rank
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+        devs = vis.split(",") if vis else [str(i) for i in range(world)]
+        os.environ["CUDA_VISIBLE_DEVICES"] = devs[local % len(devs)]
+    import __graft_entry__ as g
+    pkg = g.load_package()
+    pkg.lib()
+
+    mesh = pkg.Mesh.naca_ogrid(N_THETA, N_R, farfield="characteristic")
+    cfg = pkg.config(N=N_ORDER, cfl=CFL, mach=MACH, alpha_deg=ALPHA)
+    s = pkg.Solver(mesh, cfg).init()
+    K, Np = s.K, np_of(N_ORDER)
+    dof_stage_per_step = 3 * 4 * K * Np
+    stream = s.stream
+    peak_gflops = pkg.fp64_peak_gflops()
+
+    # warm-up (graph capture happens on the first run)
+    s.run(args.warmup)
+    s.sync()
+
+    # timed region: device-resident steps, L2 flushed between steps outside the events
+    evs = [(pkg.Event(), pkg.Event()) for _ in range(args.steps)]
+    barrier(dist)
+    clocks = Clocks(local)
+    for i in range(args.steps):
+        pkg.l2_flush(stream)
+        evs[i][0].record(stream)
+        s.run(1)
+        evs[i][1].record(stream)
+    s.sync()
+    clk = clocks.stop()
+    step_ms = [a.elapsed_ms(b) for a, b in evs]
+    total_ms = dist_max(dist, sum(step_ms))
+    barrier(dist)
+    ms_per_step = total_ms / args.steps
+    value = world * dof_stage_per_step * args.steps / (total_ms * 1e-3)
+
+    # per-kernel durations (same workload, separate launches with events between kernels)
+    nk = min(args.steps, 50)
+    kt = np.zeros(7)
+    for _ in range(nk):
+        pkg.l2_flush(stream)
+        kt += s.step_timed()
+    kt /= nk
+    face_ms = float(np.mean(kt[[0, 2, 4]]))
+    elem_ms = float(np.mean(kt[[1, 3, 5]]))
+    nf = (mesh.size("edges") + mesh.size("bedges")) * (N_ORDER + 1)
+    elem_tf = elem_flops(N_ORDER) * K / (elem_ms * 1e-3) * 1e-12
+    face_tf = face_flops(N_ORDER) * nf / (face_ms * 1e-3) * 1e-12
+    step_tf = survey_flops(N_ORDER) * K / ((face_ms + elem_ms) * 1e-3) * 1e-12
+    dominant = "elem_kernel" if elem_ms >= face_ms else "face_kernel"
+    peak_tf = peak_gflops * 1e-3
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            hbm_peak = float(json.load(f)["hbm_gbs"])
+        hbm_src = "measured (MEASURED_PEAKS.json)"
+    except (OSError, KeyError, ValueError):
+        hbm_peak, hbm_src = 6800.0, "fallback"
+    stage_bytes = algo_bytes(N_ORDER) * K
+    hbm_gbs = stage_bytes / ((face_ms + elem_ms) * 1e-3) * 1e-9
+
+    # end to end through the C ABI with pinned host buffers
+    nq = K * Np * 4
+    h_in, h_out = pkg.PinnedArray(nq), pkg.PinnedArray(nq)
+    h_in.array[:] = s.get("q")
+    e2e_steps = min(args.steps, 100)
+    e2e_ms = 0.0
+    for i in range(e2e_steps):
+        pkg.l2_flush(stream)
+        a, b = pkg.Event(), pkg.Event()
+        a.record(stream)
+        s.step_host(h_in.array, 1, h_out.array)
+        b.record(stream)
+        e2e_ms += a.elapsed_ms(b)
+    e2e_ms = dist_max(dist, e2e_ms)
+    e2e_value = world * dof_stage_per_step * e2e_steps / (e2e_ms * 1e-3)
+    s.sync()
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "DOF-stage/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (generated O-grid, freestream start)",
+        "config": {"workload": WORKLOAD, "cells": K, "order": N_ORDER, "np": Np,
+                   "dof_stage_per_step": dof_stage_per_step, "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "flushed between timed steps (512 MB write outside the events)",
+                   "graph": "one CUDA graph launch per step (7 kernels)"},
+        "gpu_launches": 7 * args.steps,
+        "roofline": {"bound": "fp64", "kernel": dominant, "achieved": elem_tf if dominant == "elem_kernel" else face_tf,
+                     "peak": peak_tf, "unit": "TFLOP/s",
+                     "frac": (elem_tf if dominant == "elem_kernel" else face_tf) / peak_tf,
+                     "traffic": None,
+                     "peak_source": "DFMA throughput measured live on this GPU (MEASURED_PEAKS.json has no FP64 figure)",
+                     "flops_per_unit": elem_flops(N_ORDER) if dominant == "elem_kernel" else face_flops(N_ORDER),
+                     "unit_def": "cell-stage" if dominant == "elem_kernel" else "face node",
+                     "kernel_ms": {"face": face_ms, "elem": elem_ms, "elem_stage2": float(kt[5]),
+                                   "finalize": float(kt[6])},
+                     "face_kernel_tflops": face_tf,
+                     "step_tflops_survey_count": step_tf,
+                     "hbm": {"achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_gbs / hbm_peak,
+                             "peak_source": hbm_src}},
+        "e2e": {"value": e2e_value, "unit": "DOF-stage/s", "h2d_bytes_per_step": nq * 8,
+                "d2h_bytes_per_step": nq * 8, "steps": e2e_steps,
+                "call": "dg_solver_step_host (pinned host q in/out, 1 step per call)"},
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu:
+        nthreads = os.cpu_count() or 1
+        rate, secs = cpu_oracle_rate(args.cpu_steps, nthreads)
+        line["cpu_baseline"] = {"value": rate, "unit": "DOF-stage/s", "cores": nthreads, "kind": "port",
+                                "sample": "%d SSPRK3 steps of the full workload (%.1f s)" % (args.cpu_steps, secs)}
+    if rank == 0:
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

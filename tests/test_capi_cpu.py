@@ -1,0 +1,49 @@
+"""The C-ABI libraries load on a host without a GPU and export every symbol their headers
+declare; calls that need a device fail with an error code, not a crash."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions(header):
+    text = open(os.path.join(ROOT, "include", header)).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    names = set()
+    for m in re.finditer(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\(", text):
+        name = m.group(1)
+        if name.startswith(("dg_", "op_")) and not name.endswith("_t"):
+            names.add(name)
+    return names
+
+
+def test_dg_header_symbols_exported(pkg):
+    lib = ctypes.CDLL(pkg.LIB_PATH)
+    names = declared_functions("dg_gb300.h")
+    assert len(names) > 30
+    missing = [n for n in sorted(names) if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_no_device_is_an_error_not_a_crash(pkg):
+    import __graft_entry__ as g
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    mesh = pkg.Mesh.vortex_square(4)
+    with pytest.raises(pkg.DGError):
+        pkg.Solver(mesh, pkg.config())
+
+
+def test_bad_config_rejected(pkg):
+    mesh = pkg.Mesh.vortex_square(4)
+    for cfg in (pkg.config(N=0), pkg.config(N=7), pkg.config(cfl=0.0), pkg.config(gam=1.0), pkg.config(app=5)):
+        with pytest.raises(pkg.DGError):
+            pkg.Solver(mesh, cfg)
