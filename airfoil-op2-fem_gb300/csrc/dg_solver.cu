@@ -36,6 +36,7 @@
 #include "dg_mesh.h"
 #include "dg_ops.h"
 #include "dg_solver.h"
+#include "../../include/dg_gb300.h"
 
 namespace dg {
 
@@ -705,3 +706,146 @@ int Solver::state(StepState &s, std::string &err) {
 }
 
 }  // namespace dg
+
+// ---------------------------------------------------------------- allocation-free RHS
+// dg_rhs_noalloc (include/dg_gb300.h): one right-hand side with no device allocation, for
+// callers that must not call cudaMalloc (a memory pool owned by another runtime, a fixed
+// budget, code that may run while another library is capturing a CUDA graph).  The face-flux
+// scratch that Solver allocates per mesh lives here in one file-scope device array instead:
+// kNoAllocScratchBytes (32 MiB) on every GPU that loads this library, held until the process
+// exits.  Every call shares it, so calls that overlap on the GPU race; the used part is
+// cleared at the start of each call.
+namespace dg {
+
+constexpr size_t kNoAllocScratchBytes = 32ull << 20;
+static __device__ __align__(256) double g_noalloc_flux[kNoAllocScratchBytes / sizeof(double)];
+static __device__ __align__(256) int g_noalloc_fmask[7][3 * 7];
+
+struct NoAllocDevice {
+  bool ready = false;
+  double *flux = nullptr;
+  int *fmask = nullptr;  // [7][21]
+  bool fmask_loaded[7] = {};
+};
+static NoAllocDevice g_noalloc[64];
+
+// Per device, once, with that device current: the device addresses of the scratch arrays
+// (a host-side name of a __device__ array is not a device address).
+static int noalloc_setup(int dev, int N, std::string &err) {
+  if (dev < 0 || dev >= 64) { err = "device ordinal out of range"; return -1; }
+  NoAllocDevice &nd = g_noalloc[dev];
+  if (!nd.ready) {
+    cudaError_t ce = cudaGetSymbolAddress((void **)&nd.flux, g_noalloc_flux);
+    if (ce != cudaSuccess) { err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(ce); return -100; }
+    ce = cudaGetSymbolAddress((void **)&nd.fmask, g_noalloc_fmask);
+    if (ce != cudaSuccess) { err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(ce); return -100; }
+    nd.ready = true;
+  }
+  if (int rc = load_order_constants(N, err)) return rc;
+  if (!nd.fmask_loaded[N]) {
+    Operators o;
+    if (build_operators(N, o)) { err = "operator construction failed"; return -2; }
+    cudaError_t ce = cudaMemcpyToSymbol(g_noalloc_fmask, o.FMASK.data(), o.FMASK.size() * sizeof(int),
+                                        (size_t)N * 3 * 7 * sizeof(int));
+    if (ce != cudaSuccess) { err = std::string("cudaMemcpyToSymbol: ") + cudaGetErrorString(ce); return -100; }
+    nd.fmask_loaded[N] = true;
+  }
+  return 0;
+}
+
+int rhs_noalloc(const Config &c, int K, int nE, int nB, const double *W, const double *geo,
+                const int4 *edges, const int4 *bedges, double *rhs, cudaStream_t stream,
+                std::string &err) {
+  const int N = c.N, Nfp = N + 1;
+  const size_t need = (size_t)K * 3 * Nfp * 4 * sizeof(double);
+  if (need > kNoAllocScratchBytes) {
+    err = "mesh too large for the allocation-free path: " + std::to_string(need) + " bytes of face-flux scratch > " +
+          std::to_string(kNoAllocScratchBytes);
+    return -3;
+  }
+  int dev = 0;
+  cudaError_t ce = cudaGetDevice(&dev);
+  if (ce != cudaSuccess) { err = std::string("cudaGetDevice: ") + cudaGetErrorString(ce); return -100; }
+  if (int rc = noalloc_setup(dev, N, err)) return rc;
+  const NoAllocDevice &nd = g_noalloc[dev];
+  Inst d{};
+  d.N = N;
+  d.K = K;
+  d.nE = nE;
+  d.nB = nB;
+  d.app = 0;
+  d.dt_mode = 1;
+  d.edges = edges;
+  d.bedges = bedges;
+  d.fmask = nd.fmask + N * 3 * 7;
+  d.geo = geo;
+  d.W = const_cast<double *>(W);  // read only in the RHS stage
+  d.flux = nd.flux;
+  d.rhs_out = rhs;
+  const double gam = c.gam;
+  double u, v, e;
+  if (c.alpha_deg != 0.0) {
+    u = std::sin((M_PI / 2.0) - (c.alpha_deg * M_PI / 180.0)) * std::sqrt(gam * c.p_inf / c.rho_inf) * c.mach;
+    v = std::cos((M_PI / 2.0) - (c.alpha_deg * M_PI / 180.0)) * std::sqrt(gam * c.p_inf / c.rho_inf) * c.mach;
+    e = c.p_inf / (gam - 1.0) + 0.5 * c.rho_inf * (u * u + v * v);
+  } else {
+    u = std::sqrt(gam * c.p_inf / c.rho_inf) * c.mach;
+    v = 0.0;
+    e = c.p_inf / (gam - 1.0) + 0.5 * c.rho_inf * (u * u);
+  }
+  d.P.gam = gam;
+  d.P.gm1 = gam - 1.0;
+  d.P.rinf = c.rho_inf;
+  d.P.uinf = u;
+  d.P.vinf = v;
+  d.P.pinf = c.p_inf;
+  d.P.einf = e;
+  ce = cudaMemsetAsync(nd.flux, 0, need, stream);
+  if (ce != cudaSuccess) { err = std::string("cudaMemsetAsync: ") + cudaGetErrorString(ce); return -100; }
+  DG_DISPATCH(N, (launch_stage<NN>(d, 3, stream)));
+  ce = cudaGetLastError();
+  if (ce != cudaSuccess) { err = std::string("launch: ") + cudaGetErrorString(ce); return -100; }
+  return 0;
+}
+
+}  // namespace dg
+
+namespace {
+thread_local std::string g_noalloc_err;
+}
+
+extern "C" const char *dg_rhs_noalloc_error(void) { return g_noalloc_err.c_str(); }
+
+extern "C" int dg_rhs_noalloc(const dg_config_t *cfg, int n_cells, int n_edges, int n_bedges,
+                              const double *W, const double *geo, const int *edges,
+                              const int *bedges, double *rhs, void *stream) {
+  if (!cfg || n_cells <= 0 || n_edges < 0 || n_bedges < 0 || !W || !geo || !rhs || (n_edges && !edges) ||
+      (n_bedges && !bedges)) {
+    g_noalloc_err = "bad arguments";
+    return DG_ERR_ARG;
+  }
+  if (cfg->N < 1 || cfg->N > 6 || cfg->app != 0 || !(cfg->gam > 1.0) || !(cfg->rho_inf > 0.0) || !(cfg->p_inf > 0.0)) {
+    g_noalloc_err = "config: N must be 1..6, app 0 (airfoil boundary types), gam > 1, rho_inf and p_inf > 0";
+    return DG_ERR_ARG;
+  }
+  if (((uintptr_t)W | (uintptr_t)geo | (uintptr_t)rhs | (uintptr_t)edges | (uintptr_t)bedges) & 15u) {
+    g_noalloc_err = "device arrays must be 16-byte aligned";
+    return DG_ERR_ARG;
+  }
+  dg::Config c;
+  c.N = cfg->N;
+  c.gam = cfg->gam;
+  c.mach = cfg->mach;
+  c.alpha_deg = cfg->alpha_deg;
+  c.p_inf = cfg->p_inf;
+  c.rho_inf = cfg->rho_inf;
+  std::string err;
+  const int rc = dg::rhs_noalloc(c, n_cells, n_edges, n_bedges, W, geo, (const int4 *)edges,
+                                 (const int4 *)bedges, rhs, (cudaStream_t)stream, err);
+  if (rc) {
+    g_noalloc_err = err;
+    return rc <= -100 ? DG_ERR_CUDA : DG_ERR_ARG;
+  }
+  return 0;
+}
+

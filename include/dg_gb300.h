@@ -106,6 +106,27 @@ void *dg_solver_stream(dg_solver_t *s);
 int dg_solver_step_timed(dg_solver_t *s, float *ms7);
 void dg_solver_free(dg_solver_t *s);
 
+/* ------------------------------------------------------------------ allocation-free RHS
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc — the device
+ * memory belongs to another runtime's pool or budget, or the call may happen while another
+ * library is capturing a CUDA graph: one right-hand side L(W) of the airfoil case
+ * (app 0 boundary types), as dg_solver_rhs computes it, that allocates nothing.  Inputs and
+ * output are device arrays the caller owns, in dg_solver's layouts:
+ *   W, rhs  [n_cells][Np][4] doubles;  geo [n_cells][16] (rx, ry, sx, sy, then nx, ny, fscale
+ *   of faces 0..2; dg_solver_get(s, "geo") gives it);  edges [n_edges][4] ints
+ *   {cL, cR, fL | fR << 2 | reverse << 4, 0};  bedges [n_bedges][4] ints {cell, face, type, 0};
+ *   all 16-byte aligned; every cell face covered by exactly one edge or boundary edge.
+ * The face-flux scratch is a file-scope device array of 32 MiB that every GPU loading the
+ * library holds until the process exits: meshes needing more (n_cells * 3 * (N+1) * 32 bytes)
+ * are rejected with DG_ERR_ARG.  The first call on a device, with that device current, looks
+ * up the scratch's device address and uploads the order's operators; make that first call
+ * before any stream capture.  All calls share the scratch (cleared at the start of each
+ * call): calls that overlap on the GPU race.  stream may be NULL (the legacy default stream).
+ * Errors: dg_rhs_noalloc_error(). */
+int dg_rhs_noalloc(const dg_config_t *cfg, int n_cells, int n_edges, int n_bedges, const double *W,
+                   const double *geo, const int *edges, const int *bedges, double *rhs, void *stream);
+const char *dg_rhs_noalloc_error(void);
+
 /* ------------------------------------------------------------------ measurement helpers */
 void *dg_host_alloc(size_t bytes); /* pinned */
 void dg_host_free(void *p);
