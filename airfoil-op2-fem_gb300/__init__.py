@@ -103,6 +103,7 @@ def lib():
         "dg_l2_flush": (C.c_int, [vp]),
         "dg_fp64_peak_gflops": (C.c_double, []),
         "dg_kernels_per_step": (C.c_int, []),
+        "dg_set_elem_variant": (None, [C.c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

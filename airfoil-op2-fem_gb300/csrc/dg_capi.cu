@@ -409,5 +409,6 @@ double dg_fp64_peak_gflops(void) {
   return 16.0 * iters * (double)blocks * threads / (ms * 1e-3) * 1e-9;
 }
 int dg_kernels_per_step(void) { return 7; }
+void dg_set_elem_variant(int variant) { dg::set_elem_variant(variant); }
 
 }  // extern "C"

@@ -38,6 +38,16 @@
 #include "dg_solver.h"
 #include "../../include/dg_gb300.h"
 
+#define DG_DISPATCH(N_, CALL)            \
+  switch (N_) {                          \
+    case 1: { constexpr int NN = 1; CALL; } break; \
+    case 2: { constexpr int NN = 2; CALL; } break; \
+    case 3: { constexpr int NN = 3; CALL; } break; \
+    case 4: { constexpr int NN = 4; CALL; } break; \
+    case 5: { constexpr int NN = 5; CALL; } break; \
+    default: { constexpr int NN = 6; CALL; } break; \
+  }
+
 namespace dg {
 
 constexpr int np_of(int n) { return (n + 1) * (n + 2) / 2; }
@@ -50,6 +60,26 @@ __constant__ double c_A3[np_of(3) * nk_of(3)];
 __constant__ double c_A4[np_of(4) * nk_of(4)];
 __constant__ double c_A5[np_of(5) * nk_of(5)];
 __constant__ double c_A6[np_of(6) * nk_of(6)];
+// Even/odd (reflection r <-> s) form of the same operator, per order: even rows (NRe x NUe)
+// then odd rows (NRo x NUo); staging slot of each input column; per node its even row, odd
+// row (-1 if on the symmetry axis) and sign.  See sym_tables().
+template <int N> struct Sym;
+template <> struct Sym<1> { static constexpr int NUe = 6, NUo = 6, NRe = 2, NRo = 1; };
+template <> struct Sym<2> { static constexpr int NUe = 11, NUo = 10, NRe = 4, NRo = 2; };
+template <> struct Sym<3> { static constexpr int NUe = 16, NUo = 16, NRe = 6, NRo = 4; };
+template <> struct Sym<4> { static constexpr int NUe = 23, NUo = 22, NRe = 9, NRo = 6; };
+template <> struct Sym<5> { static constexpr int NUe = 30, NUo = 30, NRe = 12, NRo = 9; };
+template <> struct Sym<6> { static constexpr int NUe = 39, NUo = 38, NRe = 16, NRo = 12; };
+constexpr int sym_size(int NUe, int NUo, int NRe, int NRo) { return NRe * NUe + NRo * NUo; }
+__constant__ double c_S1[sym_size(6, 6, 2, 1)];
+__constant__ double c_S2[sym_size(11, 10, 4, 2)];
+__constant__ double c_S3[sym_size(16, 16, 6, 4)];
+__constant__ double c_S4[sym_size(23, 22, 9, 6)];
+__constant__ double c_S5[sym_size(30, 30, 12, 9)];
+__constant__ double c_S6[sym_size(39, 38, 16, 12)];
+__constant__ int c_pos[7][77];      // staging slot of input column k (Fr 0..Np-1, Fs Np.., faces 2Np..)
+__constant__ int c_out[7][28 * 3];  // per node: even row, odd row or -1, sign (+1 / -1)
+
 // calc_dt face points of each volume node: up to two faces whose fscale multiplies the node's
 // wave speed (-1 = none), after the index rule of src/calc_dt.h:11.
 __constant__ int c_dtf[7][28 * 2];
@@ -64,6 +94,16 @@ __device__ __forceinline__ double opA(int idx) {
   else if constexpr (N == 4) return c_A4[idx];
   else if constexpr (N == 5) return c_A5[idx];
   else return c_A6[idx];
+}
+
+template <int N>
+__device__ __forceinline__ double opS(int idx) {
+  if constexpr (N == 1) return c_S1[idx];
+  else if constexpr (N == 2) return c_S2[idx];
+  else if constexpr (N == 3) return c_S3[idx];
+  else if constexpr (N == 4) return c_S4[idx];
+  else if constexpr (N == 5) return c_S5[idx];
+  else return c_S6[idx];
 }
 
 __device__ __forceinline__ double2 ld2(const double *p) { return *reinterpret_cast<const double2 *>(p); }
@@ -127,6 +167,86 @@ __global__ void __launch_bounds__(256) face_kernel(const Inst d, const int stage
     double *o = d.flux + (((size_t)c * 3 + f) * Nfp + i) * 4;
     st2(o, s * f2[0], s * f2[1]);
     st2(o + 2, s * f2[2], s * f2[3]);
+  }
+}
+
+// SSPRK3 stage combine of one node's right-hand side (r0..r3), and in the last stage the
+// calc_dt maximum.  Lanes past the last cell call it too (every lane reaches the warp max).
+template <int N>
+__device__ __forceinline__ void stage_combine(const Inst &d, const int stage, const int e, const bool live,
+                                              const int i, const int lane, const double w[4], double r0,
+                                              double r1, double r2, double r3) {
+  constexpr int Np = np_of(N);
+  const Phys &P = d.P;
+  const size_t off = ((size_t)(live ? e : 0) * Np + i) * 4;
+  double *wp = d.W + off;
+  if (stage == 3) {
+    if (live) {
+      double *o = d.rhs_out + off;
+      st2(o, r0, r1);
+      st2(o + 2, r2, r3);
+    }
+    return;
+  }
+  const double dt = d.st->dt;
+  double n0 = fma(dt, r0, w[0]), n1 = fma(dt, r1, w[1]), n2 = fma(dt, r2, w[2]), n3 = fma(dt, r3, w[3]);
+  if (stage == 0) {
+    if (live) {
+      st2(wp, n0, n1);
+      st2(wp + 2, n2, n3);
+    }
+    return;
+  }
+  double *qp = d.q + off;
+  double2 qa = make_double2(0.0, 0.0), qb = make_double2(0.0, 0.0);
+  if (live) {
+    qa = ld2(qp);
+    qb = ld2(qp + 2);
+  }
+  if (stage == 1) {
+    if (live) {
+      n0 = fma(0.25, n0, 0.75 * qa.x);
+      n1 = fma(0.25, n1, 0.75 * qa.y);
+      n2 = fma(0.25, n2, 0.75 * qb.x);
+      n3 = fma(0.25, n3, 0.75 * qb.y);
+      st2(wp, n0, n1);
+      st2(wp + 2, n2, n3);
+    }
+    return;
+  }
+  const double third = 1.0 / 3.0, two_third = 2.0 / 3.0;
+  n0 = fma(two_third, n0, third * qa.x);
+  n1 = fma(two_third, n1, third * qa.y);
+  n2 = fma(two_third, n2, third * qb.x);
+  n3 = fma(two_third, n3, third * qb.y);
+  if (live) {
+    st2(qp, n0, n1);
+    st2(qp + 2, n2, n3);
+    st2(wp, n0, n1);
+    st2(wp + 2, n2, n3);
+    if (bad_density(n0)) atomicOr(&d.st->err, 1u);
+  }
+  if (d.dt_mode == 0) {
+    // src/calc_dt.h: (N+1)^2 * 0.5 * fscale * (|v| + c) at the face points of this node.
+    const int fa = c_dtf[N][2 * i], fb = c_dtf[N][2 * i + 1];
+    unsigned long long best = 0ull;
+    if (live && fa >= 0) {
+      const double ir = rcp(n0);
+      const double u = n1 * ir, v = n2 * ir;
+      const double v2 = fma(u, u, v * v);
+      const double p = P.gm1 * fma(-0.5 * n0, v2, n3);
+      const double cs = sqrt(fabs(P.gam * p * ir));
+      const double spd = ((N + 1) * (N + 1) * 0.5) * (sqrt(v2) + cs);
+      const double *ge = d.geo + (size_t)e * 16 + 6;
+      const double fs = fb >= 0 ? fmax(ge[3 * fa], ge[3 * fb]) : ge[3 * fa];
+      best = (unsigned long long)__double_as_longlong(spd * fs);
+    }
+    // warp max on the bit patterns of non-negative doubles (all 32 lanes take part)
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long x = __shfl_xor_sync(0xffffffffu, best, o);
+      best = x > best ? x : best;
+    }
+    if (lane == 0 && best) atomicMax(&d.st->dt1_bits, best);
   }
 }
 
@@ -203,78 +323,127 @@ __global__ void __launch_bounds__(32 * np_of(N)) elem_kernel(const Inst d, const
     r2 = fma(c, x23.x, r2);
     r3 = fma(c, x23.y, r3);
   }
-  // Stage combine.  Lanes past the last cell keep running (no early return) so that every lane
-  // reaches the warp reduction below.
-  const size_t off = ((size_t)(live ? e : 0) * Np + i) * 4;
-  double *wp = d.W + off;
-  if (stage == 3) {
-    if (live) {
-      double *o = d.rhs_out + off;
-      st2(o, r0, r1);
-      st2(o + 2, r2, r3);
-    }
-    return;
-  }
-  const double dt = d.st->dt;
-  double n0 = fma(dt, r0, w[0]), n1 = fma(dt, r1, w[1]), n2 = fma(dt, r2, w[2]), n3 = fma(dt, r3, w[3]);
-  if (stage == 0) {
-    if (live) {
-      st2(wp, n0, n1);
-      st2(wp + 2, n2, n3);
-    }
-    return;
-  }
-  double *qp = d.q + off;
-  double2 qa = make_double2(0.0, 0.0), qb = make_double2(0.0, 0.0);
+  stage_combine<N>(d, stage, e, live, i, lane, w, r0, r1, r2, r3);
+}
+
+// The element kernel in even/odd form.  The reflection sigma: (r,s) -> (s,r) of the reference
+// triangle permutes the nodes (P) and the face points (Q: face 0 <-> face 2 reversed, face 1
+// reversed), maps Drw to Dsw (P Drw P = Dsw) and leaves LIFT invariant (P LIFT Q = LIFT).  So
+// A = [Drw | Dsw | -LIFT] commutes with the input permutation Pi = (Fr_i <-> Fs_P(i), Q):
+// P A = A Pi.  Splitting the staged inputs into sums and differences over the Pi-pairs
+// ("butterfly") makes A block-diagonal: even rows on the sums give y_i + y_P(i), odd rows on the
+// differences give y_i - y_P(i).  The contraction shrinks to 0.55-0.62 of the dense one.
+template <int N>
+__global__ void __launch_bounds__(32 * np_of(N)) elem_kernel_sym(const Inst d, const int stage) {
+  constexpr int Np = np_of(N), Nfp = N + 1, NK = nk_of(N);
+  constexpr int NUe = Sym<N>::NUe, NUo = Sym<N>::NUo, NRe = Sym<N>::NRe;
+  constexpr int NPin = NUo;  // input pairs
+  extern __shared__ double2 X[];  // [NK][32] x 4 doubles, then Y [Np][32] x 4 doubles
+  double2 *Y = X + NK * 32 * 2;
+  const int lane = threadIdx.x, i = threadIdx.y;
+  const int nthr = 32 * Np, tid = i * 32 + lane;
+  const int e0 = blockIdx.x * 32;
+  const int e = e0 + lane;
+  const bool live = e < d.K;
+  const Phys &P = d.P;
+
+  double w[4] = {0.0, 0.0, 0.0, 0.0};
+  double g[4] = {0.0, 0.0, 0.0, 0.0};
   if (live) {
-    qa = ld2(qp);
-    qb = ld2(qp + 2);
+    const double *wp = d.W + ((size_t)e * Np + i) * 4;
+    double2 a = ld2(wp), b = ld2(wp + 2);
+    w[0] = a.x; w[1] = a.y; w[2] = b.x; w[3] = b.y;
+    double2 ga = ld2(d.geo + (size_t)e * 16), gb = ld2(d.geo + (size_t)e * 16 + 2);
+    g[0] = ga.x; g[1] = ga.y; g[2] = gb.x; g[3] = gb.y;
   }
-  if (stage == 1) {
+  {
+    const double rx = g[0], ry = g[1], sx = g[2], sy = g[3];
+    double fr0 = 0, fr1 = 0, fr2 = 0, fr3 = 0, fs0 = 0, fs1 = 0, fs2 = 0, fs3 = 0;
     if (live) {
-      n0 = fma(0.25, n0, 0.75 * qa.x);
-      n1 = fma(0.25, n1, 0.75 * qa.y);
-      n2 = fma(0.25, n2, 0.75 * qb.x);
-      n3 = fma(0.25, n3, 0.75 * qb.y);
-      st2(wp, n0, n1);
-      st2(wp + 2, n2, n3);
+      const double ir = rcp(w[0]);
+      const double u = w[1] * ir, v = w[2] * ir;
+      const double p = P.gm1 * fma(-0.5, fma(w[1], u, w[2] * v), w[3]);
+      const double ep = w[3] + p;
+      const double U = fma(rx, u, ry * v), V = fma(sx, u, sy * v);
+      fr0 = fma(rx, w[1], ry * w[2]);
+      fr1 = fma(w[1], U, rx * p);
+      fr2 = fma(w[2], U, ry * p);
+      fr3 = U * ep;
+      fs0 = fma(sx, w[1], sy * w[2]);
+      fs1 = fma(w[1], V, sx * p);
+      fs2 = fma(w[2], V, sy * p);
+      fs3 = V * ep;
     }
-    return;
+    const int pr = c_pos[N][i], ps = c_pos[N][Np + i];
+    X[(pr * 32 + lane) * 2] = make_double2(fr0, fr1);
+    X[(pr * 32 + lane) * 2 + 1] = make_double2(fr2, fr3);
+    X[(ps * 32 + lane) * 2] = make_double2(fs0, fs1);
+    X[(ps * 32 + lane) * 2 + 1] = make_double2(fs2, fs3);
   }
-  const double third = 1.0 / 3.0, two_third = 2.0 / 3.0;
-  n0 = fma(two_third, n0, third * qa.x);
-  n1 = fma(two_third, n1, third * qa.y);
-  n2 = fma(two_third, n2, third * qb.x);
-  n3 = fma(two_third, n3, third * qb.y);
-  if (live) {
-    st2(qp, n0, n1);
-    st2(qp + 2, n2, n3);
-    st2(wp, n0, n1);
-    st2(wp + 2, n2, n3);
-    if (bad_density(n0)) atomicOr(&d.st->err, 1u);
-  }
-  if (d.dt_mode == 0) {
-    // src/calc_dt.h: (N+1)^2 * 0.5 * fscale * (|v| + c) at the face points of this node.
-    const int fa = c_dtf[N][2 * i], fb = c_dtf[N][2 * i + 1];
-    unsigned long long best = 0ull;
-    if (live && fa >= 0) {
-      const double ir = rcp(n0);
-      const double u = n1 * ir, v = n2 * ir;
-      const double v2 = fma(u, u, v * v);
-      const double p = P.gm1 * fma(-0.5 * n0, v2, n3);
-      const double cs = sqrt(fabs(P.gam * p * ir));
-      const double spd = ((N + 1) * (N + 1) * 0.5) * (sqrt(v2) + cs);
-      const double *ge = d.geo + (size_t)e * 16 + 6;
-      const double fs = fb >= 0 ? fmax(ge[3 * fa], ge[3 * fb]) : ge[3 * fa];
-      best = (unsigned long long)__double_as_longlong(spd * fs);
+  // face fluxes: j = tid + m*nthr, so the face point f = j / 32 is uniform in a warp
+  for (int j = tid; j < 3 * Nfp * 32; j += nthr) {
+    const int f = j >> 5, el = j & 31;
+    double2 a = make_double2(0.0, 0.0), b = make_double2(0.0, 0.0);
+    if (e0 + el < d.K) {
+      const double *fp = d.flux + (((size_t)(e0 + el)) * 3 * Nfp + f) * 4;
+      a = ld2(fp);
+      b = ld2(fp + 2);
     }
-    // warp max on the bit patterns of non-negative doubles (all 32 lanes take part)
-    for (int o = 16; o > 0; o >>= 1) {
-      const unsigned long long x = __shfl_xor_sync(0xffffffffu, best, o);
-      best = x > best ? x : best;
-    }
-    if (lane == 0 && best) atomicMax(&d.st->dt1_bits, best);
+    const int pf = c_pos[N][2 * Np + f];
+    X[(pf * 32 + el) * 2] = a;
+    X[(pf * 32 + el) * 2 + 1] = b;
   }
+  __syncthreads();
+  // butterfly over the input pairs: slot p <- x_a + x_b, slot NUe + p <- x_a - x_b
+  for (int j = tid; j < NPin * 32; j += nthr) {
+    const int p = j >> 5, el = j & 31;
+    double2 *xa = X + (p * 32 + el) * 2, *xb = X + ((NUe + p) * 32 + el) * 2;
+    const double2 a0 = xa[0], a1 = xa[1], b0 = xb[0], b1 = xb[1];
+    xa[0] = make_double2(a0.x + b0.x, a0.y + b0.y);
+    xa[1] = make_double2(a1.x + b1.x, a1.y + b1.y);
+    xb[0] = make_double2(a0.x - b0.x, a0.y - b0.y);
+    xb[1] = make_double2(a1.x - b1.x, a1.y - b1.y);
+  }
+  __syncthreads();
+  double r0 = 0.0, r1 = 0.0, r2 = 0.0, r3 = 0.0;
+  if (i < NRe) {
+#pragma unroll
+    for (int k = 0; k < NUe; k++) {
+      const double c = opS<N>(i * NUe + k);
+      const double2 x01 = X[(k * 32 + lane) * 2], x23 = X[(k * 32 + lane) * 2 + 1];
+      r0 = fma(c, x01.x, r0);
+      r1 = fma(c, x01.y, r1);
+      r2 = fma(c, x23.x, r2);
+      r3 = fma(c, x23.y, r3);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < NUo; k++) {
+      const double c = opS<N>(NRe * NUe + (i - NRe) * NUo + k);
+      const double2 x01 = X[((NUe + k) * 32 + lane) * 2], x23 = X[((NUe + k) * 32 + lane) * 2 + 1];
+      r0 = fma(c, x01.x, r0);
+      r1 = fma(c, x01.y, r1);
+      r2 = fma(c, x23.x, r2);
+      r3 = fma(c, x23.y, r3);
+    }
+  }
+  Y[(i * 32 + lane) * 2] = make_double2(r0, r1);
+  Y[(i * 32 + lane) * 2 + 1] = make_double2(r2, r3);
+  __syncthreads();
+  {
+    const int re = c_out[N][3 * i], ro = c_out[N][3 * i + 1], sg = c_out[N][3 * i + 2];
+    const double2 e01 = Y[(re * 32 + lane) * 2], e23 = Y[(re * 32 + lane) * 2 + 1];
+    r0 = e01.x; r1 = e01.y; r2 = e23.x; r3 = e23.y;
+    if (ro >= 0) {
+      const double2 o01 = Y[(ro * 32 + lane) * 2], o23 = Y[(ro * 32 + lane) * 2 + 1];
+      if (sg > 0) {
+        r0 += o01.x; r1 += o01.y; r2 += o23.x; r3 += o23.y;
+      } else {
+        r0 -= o01.x; r1 -= o01.y; r2 -= o23.x; r3 -= o23.y;
+      }
+    }
+  }
+  stage_combine<N>(d, stage, e, live, i, lane, w, r0, r1, r2, r3);
 }
 
 // ---------------------------------------------------------------- per-step finalize
@@ -429,11 +598,19 @@ static void launch_face(const Inst &d, int stage, cudaStream_t s) {
   face_kernel<N><<<(nf + 255) / 256, 256, 0, s>>>(d, stage);
 }
 
+// 1: even/odd element kernel (default), 0: dense element kernel.
+static int g_elem_variant = 1;
+
 template <int N>
 static void launch_elem(const Inst &d, int stage, cudaStream_t s) {
   constexpr int Np = np_of(N), NK = nk_of(N);
-  const size_t smem = (size_t)NK * 32 * 4 * sizeof(double);
-  elem_kernel<N><<<(d.K + 31) / 32, dim3(32, Np), smem, s>>>(d, stage);
+  if (g_elem_variant) {
+    const size_t smem = (size_t)(NK + Np) * 32 * 4 * sizeof(double);
+    elem_kernel_sym<N><<<(d.K + 31) / 32, dim3(32, Np), smem, s>>>(d, stage);
+  } else {
+    const size_t smem = (size_t)NK * 32 * 4 * sizeof(double);
+    elem_kernel<N><<<(d.K + 31) / 32, dim3(32, Np), smem, s>>>(d, stage);
+  }
 }
 
 template <int N>
@@ -445,18 +622,87 @@ static void launch_stage(const Inst &d, int stage, cudaStream_t s) {
 template <int N>
 static cudaError_t set_smem_attr() {
   const size_t smem = (size_t)nk_of(N) * 32 * 4 * sizeof(double);
-  return cudaFuncSetAttribute(elem_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(elem_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const size_t smem_sym = (size_t)(nk_of(N) + np_of(N)) * 32 * 4 * sizeof(double);
+  return cudaFuncSetAttribute(elem_kernel_sym<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_sym);
 }
 
-#define DG_DISPATCH(N_, CALL)            \
-  switch (N_) {                          \
-    case 1: { constexpr int NN = 1; CALL; } break; \
-    case 2: { constexpr int NN = 2; CALL; } break; \
-    case 3: { constexpr int NN = 3; CALL; } break; \
-    case 4: { constexpr int NN = 4; CALL; } break; \
-    case 5: { constexpr int NN = 5; CALL; } break; \
-    default: { constexpr int NN = 6; CALL; } break; \
+template <int N>
+static void sym_dims(int &NUe, int &NUo, int &NRe, int &NRo) {
+  NUe = Sym<N>::NUe; NUo = Sym<N>::NUo; NRe = Sym<N>::NRe; NRo = Sym<N>::NRo;
+}
+
+// Tables of the even/odd form (see elem_kernel_sym) from the dense rows A = [Drw | Dsw | -LIFT].
+static int sym_tables(const Operators &o, const std::vector<double> &A, std::string &err) {
+  const int N = o.N, Np = o.Np, Nfp = o.Nfp, NK = 2 * Np + 3 * Nfp;
+  std::vector<int> Pn(Np, -1), Pi(NK);
+  for (int i = 0; i < Np; i++)
+    for (int j = 0; j < Np; j++)
+      if (std::fabs(o.r[j] - o.s[i]) + std::fabs(o.s[j] - o.r[i]) < 1e-10) Pn[i] = j;
+  for (int i = 0; i < Np; i++)
+    if (Pn[i] < 0) { err = "node set is not symmetric under r <-> s"; return -4; }
+  for (int i = 0; i < Np; i++) {
+    Pi[i] = Np + Pn[i];
+    Pi[Np + i] = Pn[i];
   }
+  for (int k = 0; k < Nfp; k++) {
+    Pi[2 * Np + k] = 2 * Np + 2 * Nfp + (Nfp - 1 - k);
+    Pi[2 * Np + 2 * Nfp + k] = 2 * Np + (Nfp - 1 - k);
+    Pi[2 * Np + Nfp + k] = 2 * Np + Nfp + (Nfp - 1 - k);
+  }
+  std::vector<std::pair<int, int>> inp, outp;
+  std::vector<int> infix, outfix;
+  for (int a = 0; a < NK; a++) {
+    if (a < Pi[a]) inp.push_back({a, Pi[a]});
+    else if (a == Pi[a]) infix.push_back(a);
+  }
+  for (int i = 0; i < Np; i++) {
+    if (i < Pn[i]) outp.push_back({i, Pn[i]});
+    else if (i == Pn[i]) outfix.push_back(i);
+  }
+  const int NPin = (int)inp.size(), NUe = NPin + (int)infix.size(), NUo = NPin;
+  const int NPo = (int)outp.size(), NRe = NPo + (int)outfix.size(), NRo = NPo;
+  int cNUe, cNUo, cNRe, cNRo;
+  DG_DISPATCH(N, sym_dims<NN>(cNUe, cNUo, cNRe, cNRo));
+  if (NUe != cNUe || NUo != cNUo || NRe != cNRe || NRo != cNRo) { err = "unexpected symmetry dimensions"; return -4; }
+  int pos[77], out[28 * 3];
+  for (int k = 0; k < 77; k++) pos[k] = 0;
+  for (int k = 0; k < 28 * 3; k++) out[k] = 0;
+  for (int p = 0; p < NPin; p++) {
+    pos[inp[p].first] = p;
+    pos[inp[p].second] = NUe + p;
+  }
+  for (size_t j = 0; j < infix.size(); j++) pos[infix[j]] = NPin + (int)j;
+  std::vector<double> S((size_t)NRe * NUe + (size_t)NRo * NUo);
+  for (int r = 0; r < NRe; r++) {
+    const int i = r < NPo ? outp[r].first : outfix[r - NPo];
+    for (int k = 0; k < NUe; k++)
+      S[(size_t)r * NUe + k] = k < NPin ? 0.5 * (A[(size_t)i * NK + inp[k].first] + A[(size_t)i * NK + inp[k].second])
+                                        : A[(size_t)i * NK + infix[k - NPin]];
+  }
+  for (int q = 0; q < NRo; q++) {
+    const int i = outp[q].first;
+    for (int k = 0; k < NUo; k++)
+      S[(size_t)NRe * NUe + (size_t)q * NUo + k] =
+          0.5 * (A[(size_t)i * NK + inp[k].first] - A[(size_t)i * NK + inp[k].second]);
+  }
+  for (int q = 0; q < NPo; q++) {
+    const int a = outp[q].first, b = outp[q].second;
+    out[3 * a] = q; out[3 * a + 1] = NRe + q; out[3 * a + 2] = 1;
+    out[3 * b] = q; out[3 * b + 1] = NRe + q; out[3 * b + 2] = -1;
+  }
+  for (size_t j = 0; j < outfix.size(); j++) {
+    const int a = outfix[j];
+    out[3 * a] = NPo + (int)j; out[3 * a + 1] = -1; out[3 * a + 2] = 1;
+  }
+  const void *syms[7] = {nullptr, c_S1, c_S2, c_S3, c_S4, c_S5, c_S6};
+  cudaError_t ce = cudaMemcpyToSymbol(syms[N], S.data(), S.size() * sizeof(double));
+  if (ce == cudaSuccess) ce = cudaMemcpyToSymbol(c_pos, pos, sizeof(pos), (size_t)N * sizeof(pos));
+  if (ce == cudaSuccess) ce = cudaMemcpyToSymbol(c_out, out, sizeof(out), (size_t)N * sizeof(out));
+  if (ce != cudaSuccess) { err = std::string("constant upload: ") + cudaGetErrorString(ce); return -3; }
+  return 0;
+}
 
 // ---------------------------------------------------------------- operator upload
 static int g_ops_loaded[7] = {0};
@@ -478,6 +724,9 @@ int load_order_constants(int N, std::string &err) {
   }
   const void *syms[7] = {nullptr, c_A1, c_A2, c_A3, c_A4, c_A5, c_A6};
   cudaError_t ce = cudaMemcpyToSymbol(syms[N], A.data(), A.size() * sizeof(double));
+  if (ce == cudaSuccess) {
+    if (int rc = sym_tables(o, A, err)) return rc;
+  }
   // calc_dt face points: for node i, the faces f of face points k with FMASK[k] == i; the
   // fscale index follows src/calc_dt.h:11 (fscale[FMASK[k]], read as face FMASK[k] / Nfp while
   // Np <= 3 Nfp, i.e. N <= 4) or the face point's own face k / Nfp for N >= 5.
@@ -503,6 +752,8 @@ int load_order_constants(int N, std::string &err) {
   g_ops_loaded[N] = 1;
   return 0;
 }
+
+void set_elem_variant(int v) { g_elem_variant = v ? 1 : 0; }
 
 // ---------------------------------------------------------------- Solver (host)
 #define CK(x)                                                                  \

@@ -48,6 +48,8 @@ struct Inst {
 };
 
 int load_order_constants(int N, std::string &err);
+// Element kernel form for launches enqueued from now on: 1 even/odd (default), 0 dense.
+void set_elem_variant(int v);
 
 struct Solver {
   Config cfg;

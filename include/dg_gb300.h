@@ -141,6 +141,9 @@ int dg_l2_flush(void *stream);
 double dg_fp64_peak_gflops(void);
 /* Number of kernels one dg_solver_run step launches. */
 int dg_kernels_per_step(void);
+/* Element-kernel form for launches and graphs built from now on: 1 even/odd split of
+ * [Drw | Dsw | -LIFT] (default), 0 dense rows.  Both compute the same right-hand side. */
+void dg_set_elem_variant(int variant);
 
 #ifdef __cplusplus
 }

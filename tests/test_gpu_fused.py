@@ -164,3 +164,25 @@ def test_nonphysical_state_is_reported(pkg, omesh):
     t = pkg.Solver(pkg.Mesh.from_tables(m), pkg.config(N=3, cfl=0.5)).init()
     t.run(2)
     t.sync()
+
+
+@pytest.mark.parametrize("N", [1, 2, 3, 4, 5, 6])
+def test_even_odd_form_equals_dense_form(pkg, orc, omesh, N):
+    """The even/odd element kernel (default) and the dense one compute the same RHS and steps."""
+    m = omesh.naca_ogrid(32, 8, farfield="characteristic")
+    rng = np.random.default_rng(100 + N)
+    out = []
+    for variant in (0, 1):
+        pkg.lib().dg_set_elem_variant(variant)
+        try:
+            s = pkg.Solver(pkg.Mesh.from_tables(m), pkg.config(N=N, cfl=0.5)).init()
+            q = s.get("q")
+            W = q * (1.0 + 0.05 * np.random.default_rng(N).standard_normal(q.size))
+            r = s.rhs(W)
+            s.run(20)
+            s.sync()
+            out.append((r, s.get("q")))
+        finally:
+            pkg.lib().dg_set_elem_variant(1)
+    assert orc.rel_l2(out[1][0], out[0][0]) < 1e-13
+    assert orc.rel_l2(out[1][1], out[0][1]) < 1e-13
