@@ -227,18 +227,39 @@ __device__ __forceinline__ void stage_combine(const Inst &d, const int stage, co
     if (bad_density(n0)) atomicOr(&d.st->err, 1u);
   }
   if (d.dt_mode == 0) {
-    // src/calc_dt.h: (N+1)^2 * 0.5 * fscale * (|v| + c) at the face points of this node.
+    // src/calc_dt.h: (N+1)^2 * 0.5 * fscale * (|v| + c) at the face points of this node, maximised
+    // over the block.  A single-precision estimate finds the block's candidates first; only
+    // those within 1e-4 of the block's estimated maximum are evaluated in FP64.  The FP32
+    // estimate is within ~1e-6 of the FP64 value, so the block's true maximum is always a
+    // candidate and the result equals the all-FP64 maximum.
+    __shared__ float s_wmax[32];
     const int fa = c_dtf[N][2 * i], fb = c_dtf[N][2 * i + 1];
-    unsigned long long best = 0ull;
+    const double *ge = d.geo + (size_t)(live ? e : 0) * 16 + 6;
+    float est = 0.0f;
+    double fs = 0.0;
     if (live && fa >= 0) {
+      fs = fb >= 0 ? fmax(ge[3 * fa], ge[3 * fb]) : ge[3 * fa];
+      const float rho = (float)n0, ir = 1.0f / rho, u = (float)n1 * ir, v = (float)n2 * ir;
+      const float v2 = u * u + v * v;
+      const float p = (float)P.gm1 * ((float)n3 - 0.5f * rho * v2);
+      const float cs = sqrtf(fabsf((float)P.gam * p * ir));
+      est = ((N + 1) * (N + 1) * 0.5f) * (sqrtf(v2) + cs) * (float)fs;
+      if (!(est == est) || est > 3.0e38f) est = 3.0e38f;  // non-finite: always a candidate
+    }
+    float wm = est;
+    for (int o = 16; o > 0; o >>= 1) wm = fmaxf(wm, __shfl_xor_sync(0xffffffffu, wm, o));
+    if (lane == 0) s_wmax[i] = wm;
+    __syncthreads();
+    float bm = 0.0f;
+    for (int k = 0; k < Np; k++) bm = fmaxf(bm, s_wmax[k]);
+    unsigned long long best = 0ull;
+    if (live && fa >= 0 && est >= bm * 0.9999f) {
       const double ir = rcp(n0);
       const double u = n1 * ir, v = n2 * ir;
       const double v2 = fma(u, u, v * v);
       const double p = P.gm1 * fma(-0.5 * n0, v2, n3);
       const double cs = sqrt(fabs(P.gam * p * ir));
       const double spd = ((N + 1) * (N + 1) * 0.5) * (sqrt(v2) + cs);
-      const double *ge = d.geo + (size_t)e * 16 + 6;
-      const double fs = fb >= 0 ? fmax(ge[3 * fa], ge[3 * fb]) : ge[3 * fa];
       best = (unsigned long long)__double_as_longlong(spd * fs);
     }
     // warp max on the bit patterns of non-negative doubles (all 32 lanes take part)
