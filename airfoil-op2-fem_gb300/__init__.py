@@ -104,6 +104,19 @@ def lib():
         "dg_fp64_peak_gflops": (C.c_double, []),
         "dg_kernels_per_step": (C.c_int, []),
         "dg_set_elem_variant": (None, [C.c_int]),
+        "dg_batch_create": (C.c_int, [C.c_int, C.POINTER(Config), C.POINTER(vp), C.POINTER(vp)]),
+        "dg_batch_init": (C.c_int, [vp]),
+        "dg_batch_autotune": (C.c_int, [vp, C.c_int, dp]),
+        "dg_batch_run": (C.c_int, [vp, C.c_int]),
+        "dg_batch_sync": (C.c_int, [vp]),
+        "dg_batch_get": (C.c_int, [vp, C.c_int, cp, dp]),
+        "dg_batch_time": (C.c_int, [vp, C.c_int, dp, dp, C.POINTER(C.c_ulonglong)]),
+        "dg_batch_shape": (C.c_int, [vp, ip, ip, ip, ip]),
+        "dg_batch_uses_graph": (C.c_int, [vp]),
+        "dg_batch_stream": (vp, [vp]),
+        "dg_batch_free": (None, [vp]),
+        "dg_batch_last_error": (cp, []),
+        "dg_sweep_config": (C.c_int, [C.c_int, C.c_ulonglong, ip, ip, ip, dp, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -298,6 +311,75 @@ class Solver:
     @property
     def stream(self):
         return lib().dg_solver_stream(self.h)
+
+
+class Batch:
+    """Many instances advanced together by one persistent kernel per RK stage (dg_batch_t)."""
+
+    def __init__(self, meshes, cfgs):
+        assert len(meshes) == len(cfgs) and meshes
+        self.meshes, self.cfgs = list(meshes), list(cfgs)
+        arr = (Config * len(cfgs))(*cfgs)
+        hs = (C.c_void_p * len(meshes))(*[m.h for m in meshes])
+        h = C.c_void_p()
+        self._check(lib().dg_batch_create(len(cfgs), arr, hs, C.byref(h)))
+        self.h = h
+
+    @staticmethod
+    def _check(rc):
+        if rc != 0:
+            raise DGError(rc, lib().dg_batch_last_error().decode())
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.dg_batch_free(self.h)
+            self.h = None
+
+    def init(self):
+        self._check(lib().dg_batch_init(self.h))
+        return self
+
+    def autotune(self, steps=2):
+        ms = C.c_double()
+        self._check(lib().dg_batch_autotune(self.h, steps, C.byref(ms)))
+        return ms.value
+
+    def run(self, nsteps):
+        self._check(lib().dg_batch_run(self.h, nsteps))
+
+    def sync(self):
+        self._check(lib().dg_batch_sync(self.h))
+
+    def get(self, k, name="q"):
+        N = self.cfgs[k].N
+        n = self.meshes[k].size("cells") * (N + 1) * (N + 2) // 2 * 4
+        out = np.empty(n)
+        self._check(lib().dg_batch_get(self.h, k, name.encode(), _dp(out)))
+        return out
+
+    def time(self, k):
+        t, dt, st = C.c_double(), C.c_double(), C.c_ulonglong()
+        self._check(lib().dg_batch_time(self.h, k, C.byref(t), C.byref(dt), C.byref(st)))
+        return t.value, dt.value, st.value
+
+    def shape(self):
+        v = [C.c_int() for _ in range(4)]
+        self._check(lib().dg_batch_shape(self.h, *[C.byref(x) for x in v]))
+        return dict(variant=v[0].value, block=v[1].value, face_tile=v[2].value, grid=v[3].value,
+                    graph=bool(lib().dg_batch_uses_graph(self.h)))
+
+    @property
+    def stream(self):
+        return lib().dg_batch_stream(self.h)
+
+
+def sweep_config(n=64, seed=20261203):
+    """The batched sweep's per-instance (n_theta, n_r, order, alpha_deg, mach)."""
+    nt, nr, od = (np.empty(n, dtype=np.int32) for _ in range(3))
+    al, ma = np.empty(n), np.empty(n)
+    _check(lib().dg_sweep_config(n, seed, _ip(nt), _ip(nr), _ip(od), _dp(al), _dp(ma)))
+    return [dict(n_theta=int(nt[i]), n_r=int(nr[i]), N=int(od[i]), alpha_deg=float(al[i]), mach=float(ma[i]))
+            for i in range(n)]
 
 
 class PinnedArray:

@@ -9,18 +9,8 @@
 #include "../../include/dg_gb300.h"
 #include "dg_mesh.h"
 #include "dg_ops.h"
+#include "dg_handles.h"
 #include "dg_solver.h"
-
-struct dg_mesh_t {
-  dg::Mesh m;
-};
-struct dg_solver_t {
-  dg::Solver s;
-  double *dt_hist = nullptr;
-  int dt_hist_len = 0;
-  double *rhs_buf = nullptr;
-  cudaEvent_t ev[8] = {};
-};
 
 namespace {
 thread_local std::string g_err;
@@ -159,6 +149,13 @@ int dg_mesh_set_bedge_type(dg_mesh_t *m, const int *types) {
 }
 
 void dg_mesh_free(dg_mesh_t *m) { delete m; }
+
+int dg_sweep_config(int n, unsigned long long seed, int *n_theta, int *n_r, int *order, double *alpha_deg,
+                    double *mach) {
+  if (n < 2 || !n_theta || !n_r || !order || !alpha_deg || !mach) return fail(DG_ERR_ARG, "bad arguments");
+  dg::sweep_config(n, seed, n_theta, n_r, order, alpha_deg, mach);
+  return 0;
+}
 
 int dg_operators(int N, double *r, double *s, double *Dr, double *Ds, double *Drw, double *Dsw,
                  double *LIFT, int *FMASK) {

@@ -193,6 +193,18 @@ int vortex_square(int n, double lo, double hi, uint64_t seed, Mesh &m, std::stri
   return 0;
 }
 
+void sweep_config(int n, uint64_t seed, int *n_theta, int *n_r, int *order, double *alpha_deg, double *mach) {
+  std::mt19937_64 rng(seed);
+  for (int i = 0; i < n; i++) {
+    const double u1 = (double)(rng() >> 11) * 0x1.0p-53, u2 = (double)(rng() >> 11) * 0x1.0p-53;
+    alpha_deg[i] = -4.0 + 12.0 * u1;
+    mach[i] = 0.3 + 0.3 * u2;
+    n_theta[i] = (int)std::lround(128.0 + 256.0 * i / (n - 1));
+    n_r[i] = (int)std::lround(32.0 + 64.0 * i / (n - 1));
+    order[i] = (i % 2) ? 4 : 3;
+  }
+}
+
 int validate(const Mesh &m, std::string &err) {
   const int nc = m.n_cells(), nn = m.n_nodes();
   if (nc <= 0) { err = "mesh has no cells"; return -1; }

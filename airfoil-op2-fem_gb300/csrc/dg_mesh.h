@@ -44,6 +44,11 @@ int naca_ogrid(int n_theta, int n_r, double stretch, double radius, int farfield
 // [lo,hi]^2 in n x n squares, each cut along a diagonal drawn from std::mt19937_64(seed).
 int vortex_square(int n, double lo, double hi, uint64_t seed, Mesh &m, std::string &err);
 
+// The batched sweep: n instances, alpha ~ U[-4, 8] deg and Mach ~ U[0.3, 0.6] drawn from
+// std::mt19937_64(seed) (53-bit uniforms, alpha then Mach per instance), O-grids running
+// linearly from 128 x 32 to 384 x 96, order 3 for even and 4 for odd instances.
+void sweep_config(int n, uint64_t seed, int *n_theta, int *n_r, int *order, double *alpha_deg, double *mach);
+
 // Checks ranges and that every (cell, face) slot is covered by exactly one edge or boundary
 // edge.  The hot path depends on this single-writer property.
 int validate(const Mesh &m, std::string &err);

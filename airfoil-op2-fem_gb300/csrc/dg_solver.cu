@@ -112,12 +112,10 @@ __device__ __forceinline__ void st2(double *p, double a, double b) {
 }
 
 // ---------------------------------------------------------------- face kernel
+// One face node (tid in [0, (nB + nE) * Nfp)): boundary face nodes come first.
 template <int N>
-__global__ void __launch_bounds__(256) face_kernel(const Inst d, const int stage) {
+__device__ __forceinline__ void face_node(const Inst &d, const int stage, const int tid) {
   constexpr int Np = np_of(N), Nfp = N + 1;
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int total = (d.nE + d.nB) * Nfp;
-  if (tid >= total) return;
   // Boundary face nodes come first: their ghost states (farfield pow, vortex exp/pow) cost
   // several times an interior node, and last they would leave a tail on a near-idle GPU.
   const int nbf = d.nB * Nfp;
@@ -170,15 +168,24 @@ __global__ void __launch_bounds__(256) face_kernel(const Inst d, const int stage
   }
 }
 
-// SSPRK3 stage combine of one node's right-hand side (r0..r3), and in the last stage the
-// calc_dt maximum.  Lanes past the last cell call it too (every lane reaches the warp max).
 template <int N>
-__device__ __forceinline__ void stage_combine(const Inst &d, const int stage, const int e, const bool live,
-                                              const int i, const int lane, const double w[4], double r0,
-                                              double r1, double r2, double r3) {
+__global__ void __launch_bounds__(256) face_kernel(const Inst d, const int stage) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= (d.nE + d.nB) * (N + 1)) return;
+  face_node<N>(d, stage, tid);
+}
+
+// SSPRK3 stage combine of one node's right-hand side (r0..r3), and in the last stage the
+// calc_dt maximum.  Every thread of the block calls it: `active` is false for warps beyond the
+// Np node-warps of a wider block (they only take part in the barrier), `live` is false for
+// lanes past the last cell (they take part in the warp reductions).
+template <int N>
+__device__ __forceinline__ void stage_combine(const Inst &d, const int stage, const int e, const bool active,
+                                              const bool live, const int i, const int lane, const double w[4],
+                                              double r0, double r1, double r2, double r3) {
   constexpr int Np = np_of(N);
   const Phys &P = d.P;
-  const size_t off = ((size_t)(live ? e : 0) * Np + i) * 4;
+  const size_t off = ((size_t)(live ? e : 0) * Np + (active ? i : 0)) * 4;
   double *wp = d.W + off;
   if (stage == 3) {
     if (live) {
@@ -233,7 +240,7 @@ __device__ __forceinline__ void stage_combine(const Inst &d, const int stage, co
     // estimate is within ~1e-6 of the FP64 value, so the block's true maximum is always a
     // candidate and the result equals the all-FP64 maximum.
     __shared__ float s_wmax[32];
-    const int fa = c_dtf[N][2 * i], fb = c_dtf[N][2 * i + 1];
+    const int fa = active ? c_dtf[N][2 * i] : -1, fb = active ? c_dtf[N][2 * i + 1] : -1;
     const double *ge = d.geo + (size_t)(live ? e : 0) * 16 + 6;
     float est = 0.0f;
     double fs = 0.0;
@@ -246,28 +253,35 @@ __device__ __forceinline__ void stage_combine(const Inst &d, const int stage, co
       est = ((N + 1) * (N + 1) * 0.5f) * (sqrtf(v2) + cs) * (float)fs;
       if (!(est == est) || est > 3.0e38f) est = 3.0e38f;  // non-finite: always a candidate
     }
-    float wm = est;
-    for (int o = 16; o > 0; o >>= 1) wm = fmaxf(wm, __shfl_xor_sync(0xffffffffu, wm, o));
-    if (lane == 0) s_wmax[i] = wm;
+    if (active) {
+      float wm = est;
+      for (int o = 16; o > 0; o >>= 1) wm = fmaxf(wm, __shfl_xor_sync(0xffffffffu, wm, o));
+      if (lane == 0) s_wmax[i] = wm;
+    }
     __syncthreads();
-    float bm = 0.0f;
-    for (int k = 0; k < Np; k++) bm = fmaxf(bm, s_wmax[k]);
-    unsigned long long best = 0ull;
-    if (live && fa >= 0 && est >= bm * 0.9999f) {
-      const double ir = rcp(n0);
-      const double u = n1 * ir, v = n2 * ir;
-      const double v2 = fma(u, u, v * v);
-      const double p = P.gm1 * fma(-0.5 * n0, v2, n3);
-      const double cs = sqrt(fabs(P.gam * p * ir));
-      const double spd = ((N + 1) * (N + 1) * 0.5) * (sqrt(v2) + cs);
-      best = (unsigned long long)__double_as_longlong(spd * fs);
+    if (active) {
+      float bm = 0.0f;
+      for (int k = 0; k < Np; k++) bm = fmaxf(bm, s_wmax[k]);
+      unsigned long long best = 0ull;
+      if (live && fa >= 0 && est >= bm * 0.9999f) {
+        const double ir = rcp(n0);
+        const double u = n1 * ir, v = n2 * ir;
+        const double v2 = fma(u, u, v * v);
+        const double p = P.gm1 * fma(-0.5 * n0, v2, n3);
+        const double cs = sqrt(fabs(P.gam * p * ir));
+        const double spd = ((N + 1) * (N + 1) * 0.5) * (sqrt(v2) + cs);
+        best = (unsigned long long)__double_as_longlong(spd * fs);
+      }
+      // warp max on the bit patterns of non-negative doubles (all 32 lanes take part)
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long x = __shfl_xor_sync(0xffffffffu, best, o);
+        best = x > best ? x : best;
+      }
+      if (lane == 0 && best) atomicMax(&d.st->dt1_bits, best);
     }
-    // warp max on the bit patterns of non-negative doubles (all 32 lanes take part)
-    for (int o = 16; o > 0; o >>= 1) {
-      const unsigned long long x = __shfl_xor_sync(0xffffffffu, best, o);
-      best = x > best ? x : best;
-    }
-    if (lane == 0 && best) atomicMax(&d.st->dt1_bits, best);
+    // the block may run another tile next (batched kernel): s_wmax is rewritten only after
+    // every warp has read it
+    __syncthreads();
   }
 }
 
@@ -344,7 +358,7 @@ __global__ void __launch_bounds__(32 * np_of(N)) elem_kernel(const Inst d, const
     r2 = fma(c, x23.x, r2);
     r3 = fma(c, x23.y, r3);
   }
-  stage_combine<N>(d, stage, e, live, i, lane, w, r0, r1, r2, r3);
+  stage_combine<N>(d, stage, e, true, live, i, lane, w, r0, r1, r2, r3);
 }
 
 // The element kernel in even/odd form.  The reflection sigma: (r,s) -> (s,r) of the reference
@@ -354,18 +368,19 @@ __global__ void __launch_bounds__(32 * np_of(N)) elem_kernel(const Inst d, const
 // P A = A Pi.  Splitting the staged inputs into sums and differences over the Pi-pairs
 // ("butterfly") makes A block-diagonal: even rows on the sums give y_i + y_P(i), odd rows on the
 // differences give y_i - y_P(i).  The contraction shrinks to 0.55-0.62 of the dense one.
+// One tile of 32 cells starting at e0, thread (lane, node i) of a block with at least Np
+// node-warps (warps with i >= Np only take part in the barriers).
 template <int N>
-__global__ void __launch_bounds__(32 * np_of(N)) elem_kernel_sym(const Inst d, const int stage) {
+__device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, const int e0, const int lane,
+                                              const int i, double2 *X) {
   constexpr int Np = np_of(N), Nfp = N + 1, NK = nk_of(N);
   constexpr int NUe = Sym<N>::NUe, NUo = Sym<N>::NUo, NRe = Sym<N>::NRe;
   constexpr int NPin = NUo;  // input pairs
-  extern __shared__ double2 X[];  // [NK][32] x 4 doubles, then Y [Np][32] x 4 doubles
   double2 *Y = X + NK * 32 * 2;
-  const int lane = threadIdx.x, i = threadIdx.y;
   const int nthr = 32 * Np, tid = i * 32 + lane;
-  const int e0 = blockIdx.x * 32;
+  const bool active = i < Np;
   const int e = e0 + lane;
-  const bool live = e < d.K;
+  const bool live = active && e < d.K;
   const Phys &P = d.P;
 
   double w[4] = {0.0, 0.0, 0.0, 0.0};
@@ -395,14 +410,16 @@ __global__ void __launch_bounds__(32 * np_of(N)) elem_kernel_sym(const Inst d, c
       fs2 = fma(w[2], V, sy * p);
       fs3 = V * ep;
     }
-    const int pr = c_pos[N][i], ps = c_pos[N][Np + i];
-    X[(pr * 32 + lane) * 2] = make_double2(fr0, fr1);
-    X[(pr * 32 + lane) * 2 + 1] = make_double2(fr2, fr3);
-    X[(ps * 32 + lane) * 2] = make_double2(fs0, fs1);
-    X[(ps * 32 + lane) * 2 + 1] = make_double2(fs2, fs3);
+    if (active) {
+      const int pr = c_pos[N][i], ps = c_pos[N][Np + i];
+      X[(pr * 32 + lane) * 2] = make_double2(fr0, fr1);
+      X[(pr * 32 + lane) * 2 + 1] = make_double2(fr2, fr3);
+      X[(ps * 32 + lane) * 2] = make_double2(fs0, fs1);
+      X[(ps * 32 + lane) * 2 + 1] = make_double2(fs2, fs3);
+    }
   }
   // face fluxes: j = tid + m*nthr, so the face point f = j / 32 is uniform in a warp
-  for (int j = tid; j < 3 * Nfp * 32; j += nthr) {
+  for (int j = active ? tid : 3 * Nfp * 32; j < 3 * Nfp * 32; j += nthr) {
     const int f = j >> 5, el = j & 31;
     double2 a = make_double2(0.0, 0.0), b = make_double2(0.0, 0.0);
     if (e0 + el < d.K) {
@@ -416,7 +433,7 @@ __global__ void __launch_bounds__(32 * np_of(N)) elem_kernel_sym(const Inst d, c
   }
   __syncthreads();
   // butterfly over the input pairs: slot p <- x_a + x_b, slot NUe + p <- x_a - x_b
-  for (int j = tid; j < NPin * 32; j += nthr) {
+  for (int j = active ? tid : NPin * 32; j < NPin * 32; j += nthr) {
     const int p = j >> 5, el = j & 31;
     double2 *xa = X + (p * 32 + el) * 2, *xb = X + ((NUe + p) * 32 + el) * 2;
     const double2 a0 = xa[0], a1 = xa[1], b0 = xb[0], b1 = xb[1];
@@ -427,7 +444,8 @@ __global__ void __launch_bounds__(32 * np_of(N)) elem_kernel_sym(const Inst d, c
   }
   __syncthreads();
   double r0 = 0.0, r1 = 0.0, r2 = 0.0, r3 = 0.0;
-  if (i < NRe) {
+  if (!active) {
+  } else if (i < NRe) {
 #pragma unroll
     for (int k = 0; k < NUe; k++) {
       const double c = opS<N>(i * NUe + k);
@@ -448,10 +466,12 @@ __global__ void __launch_bounds__(32 * np_of(N)) elem_kernel_sym(const Inst d, c
       r3 = fma(c, x23.y, r3);
     }
   }
-  Y[(i * 32 + lane) * 2] = make_double2(r0, r1);
-  Y[(i * 32 + lane) * 2 + 1] = make_double2(r2, r3);
+  if (active) {
+    Y[(i * 32 + lane) * 2] = make_double2(r0, r1);
+    Y[(i * 32 + lane) * 2 + 1] = make_double2(r2, r3);
+  }
   __syncthreads();
-  {
+  if (active) {
     const int re = c_out[N][3 * i], ro = c_out[N][3 * i + 1], sg = c_out[N][3 * i + 2];
     const double2 e01 = Y[(re * 32 + lane) * 2], e23 = Y[(re * 32 + lane) * 2 + 1];
     r0 = e01.x; r1 = e01.y; r2 = e23.x; r3 = e23.y;
@@ -464,7 +484,15 @@ __global__ void __launch_bounds__(32 * np_of(N)) elem_kernel_sym(const Inst d, c
       }
     }
   }
-  stage_combine<N>(d, stage, e, live, i, lane, w, r0, r1, r2, r3);
+  stage_combine<N>(d, stage, e, active, live, i, lane, w, r0, r1, r2, r3);
+  // X and Y are rewritten by the next tile only after every warp is past this point
+  __syncthreads();
+}
+
+template <int N>
+__global__ void __launch_bounds__(32 * np_of(N)) elem_kernel_sym(const Inst d, const int stage) {
+  extern __shared__ double2 Xs[];  // [NK][32] x 4 doubles, then [Np][32] x 4 doubles
+  elem_tile_sym<N>(d, stage, blockIdx.x * 32, threadIdx.x, threadIdx.y, Xs);
 }
 
 // ---------------------------------------------------------------- per-step finalize
@@ -1120,4 +1148,121 @@ extern "C" int dg_rhs_noalloc(const dg_config_t *cfg, int n_cells, int n_edges, 
   }
   return 0;
 }
+
+#include "dg_batch.cuh"
+
+// ---------------------------------------------------------------- batched C ABI
+#include "dg_handles.h"
+
+struct dg_batch_t {
+  dg::Batch b;
+};
+
+namespace {
+thread_local std::string g_batch_err;
+int batch_fail(int code, const std::string &m) {
+  g_batch_err = m;
+  return code;
+}
+}  // namespace
+
+extern "C" const char *dg_batch_last_error(void) { return g_batch_err.c_str(); }
+
+extern "C" int dg_batch_create(int n, const dg_config_t *cfgs, const dg_mesh_t *const *meshes, dg_batch_t **out) {
+  if (n <= 0 || !cfgs || !meshes || !out) return batch_fail(DG_ERR_ARG, "bad arguments");
+  std::vector<dg::Config> cs(n);
+  std::vector<const dg::Mesh *> ms(n);
+  for (int k = 0; k < n; k++) {
+    const dg_config_t &c = cfgs[k];
+    if (c.N < 1 || c.N > 6 || !(c.cfl > 0.0) || !(c.gam > 1.0) || !(c.rho_inf > 0.0) || !(c.p_inf > 0.0) ||
+        (c.app != 0 && c.app != 1) || !meshes[k])
+      return batch_fail(DG_ERR_ARG, "instance " + std::to_string(k) + ": bad configuration");
+    cs[k].N = c.N; cs[k].app = c.app; cs[k].dt_mode = c.dt_mode; cs[k].cfl = c.cfl; cs[k].gam = c.gam;
+    cs[k].mach = c.mach; cs[k].alpha_deg = c.alpha_deg; cs[k].p_inf = c.p_inf; cs[k].rho_inf = c.rho_inf;
+    cs[k].vortex_x0 = c.vortex_x0; cs[k].vortex_y0 = c.vortex_y0; cs[k].vortex_beta = c.vortex_beta;
+    ms[k] = &meshes[k]->m;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return batch_fail(DG_ERR_CUDA, "no CUDA device");
+  auto *h = new (std::nothrow) dg_batch_t();
+  if (!h) return batch_fail(DG_ERR_ARG, "out of host memory");
+  std::string err;
+  if (int rc = h->b.create(cs, ms, err)) {
+    delete h;
+    return batch_fail(rc <= -100 ? DG_ERR_CUDA : DG_ERR_ARG, err);
+  }
+  *out = h;
+  return 0;
+}
+
+extern "C" int dg_batch_init(dg_batch_t *h) {
+  if (!h) return batch_fail(DG_ERR_ARG, "null batch");
+  std::string err;
+  if (int rc = h->b.init(err)) return batch_fail(rc <= -100 ? DG_ERR_CUDA : DG_ERR_ARG, err);
+  return 0;
+}
+
+extern "C" int dg_batch_autotune(dg_batch_t *h, int steps, double *best_ms_per_step) {
+  if (!h || steps <= 0) return batch_fail(DG_ERR_ARG, "bad arguments");
+  std::string err;
+  if (int rc = h->b.autotune(steps, err)) return batch_fail(rc <= -100 ? DG_ERR_CUDA : DG_ERR_ARG, err);
+  if (best_ms_per_step) *best_ms_per_step = h->b.shape.ms_per_step;
+  return 0;
+}
+
+extern "C" int dg_batch_run(dg_batch_t *h, int nsteps) {
+  if (!h || nsteps < 0) return batch_fail(DG_ERR_ARG, "bad arguments");
+  std::string err;
+  if (int rc = h->b.run(nsteps, err)) return batch_fail(rc <= -100 ? DG_ERR_CUDA : DG_ERR_ARG, err);
+  return 0;
+}
+
+extern "C" int dg_batch_sync(dg_batch_t *h) {
+  if (!h) return batch_fail(DG_ERR_ARG, "null batch");
+  std::string err;
+  const int rc = h->b.sync(err);
+  if (rc == -200) return batch_fail(DG_ERR_NONPHYSICAL, err);
+  if (rc) return batch_fail(DG_ERR_CUDA, err);
+  return 0;
+}
+
+extern "C" int dg_batch_get(dg_batch_t *h, int k, const char *name, double *host) {
+  if (!h || !name || !host || k < 0 || k >= (int)h->b.solvers.size()) return batch_fail(DG_ERR_ARG, "bad arguments");
+  dg::Solver *s = h->b.solvers[k];
+  const std::string n(name);
+  const double *p = n == "q" ? s->d.q : (n == "workingQ" ? s->d.W : nullptr);
+  if (!p) return batch_fail(DG_ERR_ARG, "unknown dat " + n);
+  cudaError_t ce = cudaStreamSynchronize(h->b.stream);
+  if (ce == cudaSuccess) ce = cudaMemcpy(host, p, s->q_count() * 8, cudaMemcpyDeviceToHost);
+  if (ce != cudaSuccess) return batch_fail(DG_ERR_CUDA, cudaGetErrorString(ce));
+  return 0;
+}
+
+extern "C" int dg_batch_time(dg_batch_t *h, int k, double *t, double *dt, unsigned long long *step) {
+  if (!h || k < 0 || k >= (int)h->b.solvers.size()) return batch_fail(DG_ERR_ARG, "bad arguments");
+  dg::StepState st;
+  std::string err;
+  if (cudaStreamSynchronize(h->b.stream) != cudaSuccess || h->b.solvers[k]->state(st, err))
+    return batch_fail(DG_ERR_CUDA, err);
+  if (t) *t = st.t;
+  if (dt) *dt = st.dt;
+  if (step) *step = st.step;
+  return 0;
+}
+
+extern "C" int dg_batch_shape(dg_batch_t *h, int *variant, int *block, int *face_tile, int *grid) {
+  if (!h) return batch_fail(DG_ERR_ARG, "null batch");
+  std::string err;
+  if (h->b.ensure_shape(err)) return batch_fail(DG_ERR_ARG, err);
+  const auto vs = dg::batch_variants();
+  if (variant) *variant = h->b.shape.variant;
+  if (block) *block = vs[h->b.shape.variant].bs;
+  if (face_tile) *face_tile = h->b.shape.face_tile;
+  if (grid) *grid = h->b.shape.grid;
+  return 0;
+}
+
+extern "C" int dg_batch_uses_graph(dg_batch_t *h) { return h && h->b.graph_exec ? 1 : 0; }
+extern "C" void *dg_batch_stream(dg_batch_t *h) { return h ? (void *)h->b.stream : nullptr; }
+extern "C" void dg_batch_free(dg_batch_t *h) { delete h; }
 

@@ -161,6 +161,49 @@ def cpu_oracle_rate(steps, nthreads, warmup=1):
     return 3 * 4 * K * np_of(N_ORDER) * steps / dt, dt
 
 
+def batched_measure(pkg, steps, n_inst=64, seed=20261203):
+    """The batched sweep: 64 O-grid airfoil instances, alpha ~ U[-4,8], M ~ U[0.3,0.6] (seed
+    20261203), grids 128x32 .. 384x96 (K 8192 .. 73728), N=3/4 alternating, CFL 0.5; one
+    persistent kernel per RK stage (autotuned shape) vs the same instances on the plain path
+    (each its own solver, all enqueued on their own streams, then synchronised)."""
+    sc = pkg.sweep_config(n_inst, seed)
+    meshes = [pkg.Mesh.naca_ogrid(c["n_theta"], c["n_r"]) for c in sc]
+    cfgs = [pkg.config(N=c["N"], cfl=CFL, mach=c["mach"], alpha_deg=c["alpha_deg"]) for c in sc]
+    cells = sum(m.size("cells") for m in meshes)
+    dof = sum(m.size("cells") * np_of(c.N) * 4 for m, c in zip(meshes, cfgs))
+    b = pkg.Batch(meshes, cfgs).init()
+    tuned = b.autotune(2)
+    b.run(3)
+    b.sync()
+    evs = [(pkg.Event(), pkg.Event()) for _ in range(steps)]
+    for i in range(steps):  # inputs (~3.7 GB) far exceed L2: no flush needed
+        evs[i][0].record(b.stream)
+        b.run(1)
+        evs[i][1].record(b.stream)
+    b.sync()
+    bms = sum(a.elapsed_ms(c) for a, c in evs) / steps
+    solvers = [pkg.Solver(m, c).init() for m, c in zip(meshes, cfgs)]
+    for s in solvers:
+        s.run(2)
+    for s in solvers:
+        s.sync()
+    psteps = max(3, steps // 4)
+    t0 = time.perf_counter()
+    for _ in range(psteps):
+        for s in solvers:
+            s.run(1)
+        for s in solvers:
+            s.sync()
+    pms = (time.perf_counter() - t0) / psteps * 1e3
+    del solvers
+    return {"value": 3 * dof / (bms * 1e-3), "unit": "DOF-stage/s", "ms_per_step": bms, "steps": steps,
+            "instances": n_inst, "cells": cells, "dof_stage_per_step": 3 * dof, "shape": b.shape(),
+            "autotune_ms_per_step": tuned,
+            "plain_same_instances": {"value": 3 * dof / (pms * 1e-3), "ms_per_step": pms,
+                                     "how": "64 plain solvers, each on its own stream, host-timed"},
+            "speedup_vs_plain": pms / bms}
+
+
 def run_reference(args):
     """The reference arm: the reference's user kernels (restated; the reference's own build is
     N=4-only and cannot run this N=3 workload) on all host cores."""
@@ -198,11 +241,13 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=40, help="CPU-baseline sample size (steps)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batched-steps", type=int, default=20)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -322,6 +367,8 @@ def main():
         rate, secs = cpu_oracle_rate(args.cpu_steps, nthreads)
         line["cpu_baseline"] = {"value": rate, "unit": "DOF-stage/s", "cores": nthreads, "kind": "port",
                                 "sample": "%d SSPRK3 steps of the full workload (%.1f s)" % (args.cpu_steps, secs)}
+    if not args.no_batched:
+        line["batched"] = batched_measure(pkg, args.batched_steps)
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:

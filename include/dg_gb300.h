@@ -106,6 +106,32 @@ void *dg_solver_stream(dg_solver_t *s);
 int dg_solver_step_timed(dg_solver_t *s, float *ms7);
 void dg_solver_free(dg_solver_t *s);
 
+/* ------------------------------------------------------------------ batched instances
+ * Many instances (airfoil or vortex, any size, order 1..6, Mach, alpha) advanced together:
+ * each RK stage of the whole batch is one persistent kernel (cooperative launch: face phase,
+ * grid barrier, element phase over all instances' tiles), a step is three of them plus one
+ * finalize, captured in a CUDA graph.  Each instance computes exactly what dg_solver would.
+ * A grid barrier wait is bounded (about 2 s); if one gives up, dg_batch_sync reports it. */
+typedef struct dg_batch_t dg_batch_t;
+int dg_batch_create(int n, const dg_config_t *cfgs, const dg_mesh_t *const *meshes, dg_batch_t **out);
+int dg_batch_init(dg_batch_t *b);
+/* Time every launch shape (kernel variant x face-tile size) over `steps` steps, keep the
+ * fastest; the instances' state is restored afterwards. */
+int dg_batch_autotune(dg_batch_t *b, int steps, double *best_ms_per_step);
+int dg_batch_run(dg_batch_t *b, int nsteps);
+int dg_batch_sync(dg_batch_t *b);
+int dg_batch_get(dg_batch_t *b, int instance, const char *name, double *host);
+int dg_batch_time(dg_batch_t *b, int instance, double *t, double *dt, unsigned long long *step);
+int dg_batch_shape(dg_batch_t *b, int *variant, int *block, int *face_tile, int *grid);
+int dg_batch_uses_graph(dg_batch_t *b);
+void *dg_batch_stream(dg_batch_t *b);
+void dg_batch_free(dg_batch_t *b);
+const char *dg_batch_last_error(void);
+/* The batched sweep's instances: alpha ~ U[-4,8] deg, Mach ~ U[0.3,0.6] from
+ * std::mt19937_64(seed); O-grids 128x32 .. 384x96 linearly; order 3 even / 4 odd. */
+int dg_sweep_config(int n, unsigned long long seed, int *n_theta, int *n_r, int *order, double *alpha_deg,
+                    double *mach);
+
 /* ------------------------------------------------------------------ allocation-free RHS
  * No counterpart in the reference.  For callers that cannot call cudaMalloc — the device
  * memory belongs to another runtime's pool or budget, or the call may happen while another

@@ -1,0 +1,67 @@
+"""The batched persistent-kernel path (dg_batch_*): every instance must compute exactly what its
+own plain solver computes (same device functions, same operation order, one writer per face
+slot, order-independent dt maximum) — bitwise, before and after autotuning, for mixed orders
+and mixed airfoil / vortex instances."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def instances(pkg):
+    specs = [
+        (pkg.Mesh.naca_ogrid(48, 12), pkg.config(N=3, cfl=0.5, mach=0.45, alpha_deg=2.0)),
+        (pkg.Mesh.naca_ogrid(64, 16, farfield="reference"), pkg.config(N=4, cfl=0.5, mach=0.35, alpha_deg=-3.0)),
+        (pkg.Mesh.vortex_square(12), pkg.config(N=3, app=pkg.APP_VORTEX, dt_mode=pkg.DT_FROZEN, cfl=0.5,
+                                                vortex_x0=0.0)),
+        (pkg.Mesh.naca_ogrid(32, 8), pkg.config(N=2, cfl=0.5)),
+        (pkg.Mesh.naca_ogrid(40, 10), pkg.config(N=4, cfl=0.4, mach=0.55)),
+    ]
+    return [m for m, _ in specs], [c for _, c in specs]
+
+
+def plain(pkg, meshes, cfgs, steps):
+    out = []
+    for m, c in zip(meshes, cfgs):
+        s = pkg.Solver(m, c).init()
+        s.run(steps)
+        s.sync()
+        out.append((s.get("q"), s.time()))
+    return out
+
+
+def test_batch_equals_plain_solvers(pkg):
+    meshes, cfgs = instances(pkg)
+    ref = plain(pkg, meshes, cfgs, 25)
+    b = pkg.Batch(meshes, cfgs).init()
+    b.run(25)
+    b.sync()
+    assert b.shape()["graph"]  # the step runs as one graph launch
+    for k in range(len(cfgs)):
+        assert np.array_equal(b.get(k, "q"), ref[k][0]), k
+        assert b.time(k) == ref[k][1], k
+
+
+def test_batch_autotuned_equals_plain(pkg):
+    meshes, cfgs = instances(pkg)
+    ref = plain(pkg, meshes, cfgs, 12)
+    b = pkg.Batch(meshes, cfgs).init()
+    ms = b.autotune(steps=2)
+    assert ms > 0
+    sh = b.shape()
+    assert sh["block"] >= 32 * 15 and sh["grid"] > 0
+    b.run(12)
+    b.sync()
+    for k in range(len(cfgs)):
+        assert np.array_equal(b.get(k, "q"), ref[k][0]), k
+
+
+def test_batch_reports_nonphysical(pkg):
+    meshes, cfgs = instances(pkg)
+    b = pkg.Batch(meshes[:2], cfgs[:2]).init()
+    b.run(1)
+    b.sync()
+    bad = pkg.Batch([pkg.Mesh.naca_ogrid(32, 8)], [pkg.config(N=3, cfl=50.0)]).init()
+    bad.run(40)
+    with pytest.raises(pkg.DGError):
+        bad.sync()
