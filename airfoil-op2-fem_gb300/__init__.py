@@ -117,6 +117,15 @@ def lib():
         "dg_batch_free": (None, [vp]),
         "dg_batch_last_error": (cp, []),
         "dg_sweep_config": (C.c_int, [C.c_int, C.c_ulonglong, ip, ip, ip, dp, dp]),
+        "dg_adjoint_create": (C.c_int, [C.POINTER(Config), vp, C.c_int, C.c_int, C.c_int, C.POINTER(vp)]),
+        "dg_adjoint_forward": (C.c_int, [vp, dp]),
+        "dg_adjoint_backward": (C.c_int, [vp, C.c_double, dp, dp]),
+        "dg_adjoint_evaluate": (C.c_int, [vp, C.c_double, dp, dp]),
+        "dg_adjoint_dt_sequence": (C.c_int, [vp, dp, C.c_int]),
+        "dg_adjoint_rhs_vjp": (C.c_int, [vp, dp, dp, dp, dp]),
+        "dg_adjoint_stream": (vp, [vp]),
+        "dg_adjoint_free": (None, [vp]),
+        "dg_adjoint_last_error": (cp, []),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -371,6 +380,61 @@ class Batch:
     @property
     def stream(self):
         return lib().dg_batch_stream(self.h)
+
+
+class LiftObjective:
+    """Lift-coefficient objective with its discrete adjoint (dg_adjoint_t), used like
+    torch.autograd.Function: J = forward(); grad_alpha, grad_q0 = backward(grad_J)."""
+
+    def __init__(self, mesh, cfg, nsteps, navg, checkpoint_every=50):
+        self.mesh, self.cfg, self.nsteps = mesh, cfg, nsteps
+        self.K = mesh.size("cells")
+        self.nq = self.K * (cfg.N + 1) * (cfg.N + 2) // 2 * 4
+        h = C.c_void_p()
+        self._check(lib().dg_adjoint_create(C.byref(cfg), mesh.h, nsteps, navg, checkpoint_every, C.byref(h)))
+        self.h = h
+
+    @staticmethod
+    def _check(rc):
+        if rc != 0:
+            raise DGError(rc, lib().dg_adjoint_last_error().decode())
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.dg_adjoint_free(self.h)
+            self.h = None
+
+    def forward(self):
+        J = C.c_double()
+        self._check(lib().dg_adjoint_forward(self.h, C.byref(J)))
+        return J.value
+
+    def backward(self, grad_J=1.0, want_q0=True):
+        ga = C.c_double()
+        gq = np.empty(self.nq) if want_q0 else None
+        self._check(lib().dg_adjoint_backward(self.h, grad_J, C.byref(ga), _dp(gq) if want_q0 else None))
+        return ga.value, gq
+
+    def evaluate(self, alpha_deg, q0=None):
+        J = C.c_double()
+        q = None if q0 is None else _f64(q0).ravel()
+        self._check(lib().dg_adjoint_evaluate(self.h, alpha_deg, _dp(q) if q is not None else None, C.byref(J)))
+        return J.value
+
+    def dt_sequence(self):
+        out = np.empty(self.nsteps)
+        self._check(lib().dg_adjoint_dt_sequence(self.h, _dp(out), self.nsteps))
+        return out
+
+    def rhs_vjp(self, W, v):
+        W, v = _f64(W).ravel(), _f64(v).ravel()
+        out, ap = np.empty(self.nq), C.c_double()
+        self._check(lib().dg_adjoint_rhs_vjp(self.h, _dp(W), _dp(v), _dp(out), C.byref(ap)))
+        return out, ap.value
+
+    @property
+    def stream(self):
+        return lib().dg_adjoint_stream(self.h)
 
 
 def sweep_config(n=64, seed=20261203):

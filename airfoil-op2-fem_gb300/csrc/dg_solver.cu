@@ -19,7 +19,7 @@
 // Data layout in HBM (K cells, order N, Np=(N+1)(N+2)/2, Nfp=N+1):
 //   q, W   [K][Np][4] doubles (the reference's AoS, src/airfoil.cpp:171)
 //   flux   [K][3][Nfp][4]
-//   geo    [K][16]: rx, ry, sx, sy, then (nx, ny, fscale) of faces 0..2, 3 pad
+//   geo    [K][16]: rx, ry, sx, sy, then (nx, ny, fscale) of faces 0..2, J, 2 pad
 //   edges  int4 {cL, cR, fL | fR << 2 | reverse << 4, 0};  bedges int4 {cell, face, type, 0}
 //   bxy    [nB][Nfp][2] boundary face-node coordinates (vortex boundary)
 #include <cuda_runtime.h>
@@ -38,14 +38,14 @@
 #include "dg_solver.h"
 #include "../../include/dg_gb300.h"
 
-#define DG_DISPATCH(N_, CALL)            \
-  switch (N_) {                          \
-    case 1: { constexpr int NN = 1; CALL; } break; \
-    case 2: { constexpr int NN = 2; CALL; } break; \
-    case 3: { constexpr int NN = 3; CALL; } break; \
-    case 4: { constexpr int NN = 4; CALL; } break; \
-    case 5: { constexpr int NN = 5; CALL; } break; \
-    default: { constexpr int NN = 6; CALL; } break; \
+#define DG_DISPATCH(N_, ...)                                 \
+  switch (N_) {                                              \
+    case 1: { constexpr int NN = 1; __VA_ARGS__; } break;   \
+    case 2: { constexpr int NN = 2; __VA_ARGS__; } break;   \
+    case 3: { constexpr int NN = 3; __VA_ARGS__; } break;   \
+    case 4: { constexpr int NN = 4; __VA_ARGS__; } break;   \
+    case 5: { constexpr int NN = 5; __VA_ARGS__; } break;   \
+    default: { constexpr int NN = 6; __VA_ARGS__; } break;  \
   }
 
 namespace dg {
@@ -58,8 +58,10 @@ __constant__ double c_A1[np_of(1) * nk_of(1)];
 __constant__ double c_A2[np_of(2) * nk_of(2)];
 __constant__ double c_A3[np_of(3) * nk_of(3)];
 __constant__ double c_A4[np_of(4) * nk_of(4)];
-__constant__ double c_A5[np_of(5) * nk_of(5)];
-__constant__ double c_A6[np_of(6) * nk_of(6)];
+// Orders 5 and 6 live in global memory (read-only path; warp-uniform reads): constant memory
+// (64 KB) holds the other tables.
+__device__ double c_A5[np_of(5) * nk_of(5)];
+__device__ double c_A6[np_of(6) * nk_of(6)];
 // Even/odd (reflection r <-> s) form of the same operator, per order: even rows (NRe x NUe)
 // then odd rows (NRo x NUo); staging slot of each input column; per node its even row, odd
 // row (-1 if on the symmetry axis) and sign.  See sym_tables().
@@ -92,8 +94,8 @@ __device__ __forceinline__ double opA(int idx) {
   else if constexpr (N == 2) return c_A2[idx];
   else if constexpr (N == 3) return c_A3[idx];
   else if constexpr (N == 4) return c_A4[idx];
-  else if constexpr (N == 5) return c_A5[idx];
-  else return c_A6[idx];
+  else if constexpr (N == 5) return __ldg(&c_A5[idx]);
+  else return __ldg(&c_A6[idx]);
 }
 
 template <int N>
@@ -536,7 +538,8 @@ __global__ void geometry_kernel(int K, const double *coords, const int *cells, d
     g[5 + 3 * f] = __ddiv_rn(fny[f], sJ);
     g[6 + 3 * f] = __ddiv_rn(sJ, J);
   }
-  g[13] = g[14] = g[15] = 0.0;
+  g[13] = J;  // cell Jacobian: face arc-length element sJ = fscale * J
+  g[14] = g[15] = 0.0;
 }
 
 // Node position with the operation order of src/init_grid.h:19-54 (cblas dcopy/daxpy/dscal).
@@ -1150,6 +1153,7 @@ extern "C" int dg_rhs_noalloc(const dg_config_t *cfg, int n_cells, int n_edges, 
 }
 
 #include "dg_batch.cuh"
+#include "dg_adjoint.cuh"
 
 // ---------------------------------------------------------------- batched C ABI
 #include "dg_handles.h"

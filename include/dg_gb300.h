@@ -132,6 +132,30 @@ const char *dg_batch_last_error(void);
 int dg_sweep_config(int n, unsigned long long seed, int *n_theta, int *n_r, int *order, double *alpha_deg,
                     double *mach);
 
+/* ------------------------------------------------------------------ adjoint (lift gradient)
+ * J = mean over the last navg of nsteps SSPRK3 steps of the lift coefficient
+ *   C_l = sum over wall face nodes of w_k sJ p (n . (-sin a, cos a)) / (1/2 rho |V|^2 c), c = 1
+ * (airfoil boundary types 0, 1, 2).  dg_adjoint_forward runs the solver from its initial state
+ * recording the dt sequence and checkpointing q every checkpoint_every steps;
+ * dg_adjoint_backward runs the discrete adjoint (hand-written reverse kernels of the Roe flux,
+ * boundary states, volume and lift operators; SSPRK3 reversed segment by segment with
+ * recomputation from the checkpoints) and returns grad_J * dJ/dalpha (alpha in degrees) and
+ * grad_J * dJ/dq0 ([K][Np][4], may be NULL), with the dt sequence frozen.
+ * dg_adjoint_evaluate gives J for another alpha / initial state with that frozen sequence (the
+ * function backward differentiates), for finite-difference checks. */
+typedef struct dg_adjoint_t dg_adjoint_t;
+int dg_adjoint_create(const dg_config_t *cfg, const dg_mesh_t *mesh, int nsteps, int navg, int checkpoint_every,
+                      dg_adjoint_t **out);
+int dg_adjoint_forward(dg_adjoint_t *a, double *J);
+int dg_adjoint_backward(dg_adjoint_t *a, double grad_J, double *grad_alpha, double *grad_q0);
+int dg_adjoint_evaluate(dg_adjoint_t *a, double alpha_deg, const double *q0, double *J);
+int dg_adjoint_dt_sequence(dg_adjoint_t *a, double *out, int n);
+/* (dL/dW at W)^T v and v . dL/dalpha of one right-hand side (host arrays [K][Np][4]). */
+int dg_adjoint_rhs_vjp(dg_adjoint_t *a, const double *W, const double *v, double *out, double *alpha_part);
+void *dg_adjoint_stream(dg_adjoint_t *a);
+void dg_adjoint_free(dg_adjoint_t *a);
+const char *dg_adjoint_last_error(void);
+
 /* ------------------------------------------------------------------ allocation-free RHS
  * No counterpart in the reference.  For callers that cannot call cudaMalloc — the device
  * memory belongs to another runtime's pool or budget, or the call may happen while another
