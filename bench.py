@@ -204,6 +204,30 @@ def batched_measure(pkg, steps, n_inst=64, seed=20261203):
             "speedup_vs_plain": pms / bms}
 
 
+def adjoint_measure(pkg, nsteps=2000, navg=100, C=50):
+    """The adjoint case: NACA 0012 O-grid 256x64 (K=32768), N=3, M=0.5, alpha=2 deg, inflow /
+    outflow farfield typing (the adjoint covers boundary types 0-2), J = mean C_l over the last
+    100 of 2000 steps, checkpoints every 50 steps.  Reports forward and backward device times, the
+    adjoint/forward cost ratio and a central-difference check of dJ/dalpha (h = 1e-6)."""
+    mesh = pkg.Mesh.naca_ogrid(N_THETA, N_R, farfield="reference")
+    cfg = pkg.config(N=N_ORDER, cfl=CFL, mach=0.5, alpha_deg=2.0)
+    obj = pkg.LiftObjective(mesh, cfg, nsteps, navg, C)
+    a, b, c = pkg.Event(), pkg.Event(), pkg.Event()
+    a.record(obj.stream)
+    J = obj.forward()
+    b.record(obj.stream)
+    ga, _ = obj.backward(want_q0=False)
+    c.record(obj.stream)
+    fwd_ms, bwd_ms = a.elapsed_ms(b), b.elapsed_ms(c)
+    h = 1e-6
+    fd = (obj.evaluate(2.0 + h) - obj.evaluate(2.0 - h)) / (2 * h)
+    return {"J_mean_cl": J, "dJ_dalpha_deg": ga, "fd_dJ_dalpha_deg": fd,
+            "fd_rel_diff": abs(ga - fd) / max(abs(fd), 1e-300), "forward_ms": fwd_ms, "backward_ms": bwd_ms,
+            "adjoint_over_forward": bwd_ms / fwd_ms, "steps": nsteps, "avg_last": navg,
+            "checkpoint_every": C, "cells": mesh.size("cells"), "order": N_ORDER,
+            "note": "backward = segment recomputation from checkpoints + reverse sweep"}
+
+
 def run_reference(args):
     """The reference arm: the reference's user kernels (restated; the reference's own build is
     N=4-only and cannot run this N=3 workload) on all host cores."""
@@ -248,6 +272,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batched-steps", type=int, default=20)
+    ap.add_argument("--no-adjoint", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -369,6 +394,8 @@ def main():
                                 "sample": "%d SSPRK3 steps of the full workload (%.1f s)" % (args.cpu_steps, secs)}
     if not args.no_batched:
         line["batched"] = batched_measure(pkg, args.batched_steps)
+    if not args.no_adjoint:
+        line["adjoint"] = adjoint_measure(pkg)
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:
