@@ -339,6 +339,14 @@ def main():
         hbm_src = "measured (MEASURED_PEAKS.json)"
     except (OSError, KeyError, ValueError):
         hbm_peak, hbm_src = 6800.0, "fallback"
+    traffic = None
+    try:  # ncu-measured DRAM bytes per element-kernel launch (stage average), committed profile
+        with open(os.path.join(ROOT, "profiles", "elem_kernel_sym_face_kernel_naca_ogrid_K32768_N3.md")) as f:
+            for ln in f:
+                if ln.startswith("traffic_bytes_per_launch_elem_kernel:"):
+                    traffic = float(ln.split(":")[1])
+    except OSError:
+        traffic = None
     stage_bytes = algo_bytes(N_ORDER) * K
     hbm_gbs = stage_bytes / ((face_ms + elem_ms) * 1e-3) * 1e-9
 
@@ -372,7 +380,8 @@ def main():
         "roofline": {"bound": "fp64", "kernel": dominant, "achieved": elem_tf if dominant == "elem_kernel" else face_tf,
                      "peak": peak_tf, "unit": "TFLOP/s",
                      "frac": (elem_tf if dominant == "elem_kernel" else face_tf) / peak_tf,
-                     "traffic": None,
+                     "traffic": traffic if dominant == "elem_kernel" else None,
+                     "traffic_source": "ncu dram__bytes_read+write per launch, stage average (profiles/)",
                      "peak_source": "DFMA throughput measured live on this GPU (MEASURED_PEAKS.json has no FP64 figure)",
                      "flops_per_unit": elem_flops(N_ORDER) if dominant == "elem_kernel" else face_flops(N_ORDER),
                      "unit_def": "cell-stage" if dominant == "elem_kernel" else "face node",
