@@ -93,6 +93,22 @@ def lib():
         "dg_solver_stream": (vp, [vp]),
         "dg_solver_step_timed": (C.c_int, [vp, C.POINTER(C.c_float)]),
         "dg_solver_free": (None, [vp]),
+        "dg_solver_vertex_fields": (C.c_int, [vp, vp, dp, dp, dp, dp]),
+        "dg_solver_write_vtk": (C.c_int, [vp, vp, cp]),
+        "dg_mesh_write_vtk": (C.c_int, [vp, cp, dp, dp, dp, dp]),
+        "dg_advec_create": (C.c_int, [vp, C.c_int, C.c_double, C.c_double, C.c_double, C.POINTER(vp)]),
+        "dg_advec_init": (C.c_int, [vp]),
+        "dg_advec_run": (C.c_int, [vp, C.c_int]),
+        "dg_advec_sync": (C.c_int, [vp]),
+        "dg_advec_get": (C.c_int, [vp, cp, dp]),
+        "dg_advec_set": (C.c_int, [vp, cp, dp]),
+        "dg_advec_rhs": (C.c_int, [vp, dp, dp]),
+        "dg_advec_time": (C.c_int, [vp, dp, C.POINTER(C.c_ulonglong)]),
+        "dg_advec_step_timed": (C.c_int, [vp, C.POINTER(C.c_float)]),
+        "dg_advec_vertex_values": (C.c_int, [vp, vp, dp]),
+        "dg_advec_write_vtk": (C.c_int, [vp, vp, cp]),
+        "dg_advec_stream": (vp, [vp]),
+        "dg_advec_free": (None, [vp]),
         "dg_host_alloc": (vp, [C.c_size_t]),
         "dg_host_free": (None, [vp]),
         "dg_event_create": (vp, []),
@@ -229,6 +245,14 @@ class Mesh:
         t = _i32(types)
         _check(lib().dg_mesh_set_bedge_type(self.h, _ip(t)))
 
+    def write_vtk(self, path, rho, u, v, p):
+        """Legacy-VTK file of per-vertex fields (host arrays of n_nodes)."""
+        a = [np.ascontiguousarray(x, dtype=np.float64) for x in (rho, u, v, p)]
+        n = self.size("nodes")
+        if any(x.size != n for x in a):
+            raise ValueError("fields must have one value per mesh vertex")
+        _check(lib().dg_mesh_write_vtk(self.h, str(path).encode(), *[_dp(x) for x in a]))
+
 
 def operators(N):
     """Nodal operators of order N (dict like the reference's constants headers)."""
@@ -320,6 +344,17 @@ class Solver:
     @property
     def stream(self):
         return lib().dg_solver_stream(self.h)
+
+    def vertex_fields(self):
+        """rho, u, v, p per mesh vertex (src/save_solution.cpp's sampling)."""
+        n = self.mesh.size("nodes")
+        out = [np.empty(n) for _ in range(4)]
+        _check(lib().dg_solver_vertex_fields(self.h, self.mesh.h, *[_dp(a) for a in out]))
+        return out
+
+    def write_vtk(self, path):
+        """The current solution as a legacy-VTK file (vertex_fields' values)."""
+        _check(lib().dg_solver_write_vtk(self.h, self.mesh.h, str(path).encode()))
 
 
 class Batch:
@@ -444,6 +479,74 @@ def sweep_config(n=64, seed=20261203):
     _check(lib().dg_sweep_config(n, seed, _ip(nt), _ip(nr), _ip(od), _dp(al), _dp(ma)))
     return [dict(n_theta=int(nt[i]), n_r=int(nr[i]), N=int(od[i]), alpha_deg=float(al[i]), mach=float(ma[i]))
             for i in range(n)]
+
+
+class Advection:
+    """The scalar advection app (advec/src/advec.cpp) on the GPU: q has one value per node,
+    classical RK4 with a fixed dt, velocity (vel_x, vel_y) (the app's -vx/-vy)."""
+
+    def __init__(self, mesh, N=4, vel_x=1.0, vel_y=1.0, dt=1e-3):
+        self.mesh, self.N, self.dt = mesh, N, dt
+        self.h = C.c_void_p()
+        _check(lib().dg_advec_create(mesh.h, N, vel_x, vel_y, dt, C.byref(self.h)))
+        self.n = mesh.size("cells") * (N + 1) * (N + 2) // 2
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().dg_advec_free(self.h)
+            self.h = None
+
+    def init(self):
+        _check(lib().dg_advec_init(self.h))
+        return self
+
+    def run(self, nsteps):
+        _check(lib().dg_advec_run(self.h, nsteps))
+
+    def sync(self):
+        _check(lib().dg_advec_sync(self.h))
+
+    def get(self, name="q"):
+        n = self.mesh.size("cells") * 16 if name == "geo" else self.n
+        out = np.empty(n)
+        _check(lib().dg_advec_get(self.h, name.encode(), _dp(out)))
+        return out
+
+    def set(self, name, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64).ravel()
+        if a.size != self.n:
+            raise ValueError("expected %d values" % self.n)
+        _check(lib().dg_advec_set(self.h, name.encode(), _dp(a)))
+
+    def rhs(self, W):
+        a = np.ascontiguousarray(W, dtype=np.float64).ravel()
+        if a.size != self.n:
+            raise ValueError("expected %d values" % self.n)
+        out = np.empty(self.n)
+        _check(lib().dg_advec_rhs(self.h, _dp(a), _dp(out)))
+        return out
+
+    def time(self):
+        t, k = C.c_double(), C.c_ulonglong()
+        _check(lib().dg_advec_time(self.h, C.byref(t), C.byref(k)))
+        return t.value, k.value
+
+    def step_timed(self):
+        ms = (C.c_float * 8)()
+        _check(lib().dg_advec_step_timed(self.h, ms))
+        return list(ms)
+
+    def vertex_values(self):
+        out = np.empty(self.mesh.size("nodes"))
+        _check(lib().dg_advec_vertex_values(self.h, self.mesh.h, _dp(out)))
+        return out
+
+    def write_vtk(self, path):
+        _check(lib().dg_advec_write_vtk(self.h, self.mesh.h, str(path).encode()))
+
+    @property
+    def stream(self):
+        return lib().dg_advec_stream(self.h)
 
 
 class PinnedArray:

@@ -4,6 +4,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <vector>
 #include <string>
 
 #include "../../include/dg_gb300.h"
@@ -334,6 +335,158 @@ int dg_solver_step_timed(dg_solver_t *h, float *ms7) {
   CKC(cudaEventSynchronize(h->ev[7]));
   for (int k = 0; k < 7; k++) CKC(cudaEventElapsedTime(&ms7[k], h->ev[k], h->ev[k + 1]));
   return 0;
+}
+
+// ---------------------------------------------------------------- scalar advection app
+int dg_advec_create(const dg_mesh_t *mesh, int order, double vel_x, double vel_y, double dt, dg_advec_t **out) {
+  if (!mesh || !out) return fail(DG_ERR_ARG, "bad arguments");
+  *out = nullptr;
+  int ndev = 0;
+  if (order < 1 || order > 6) return fail(DG_ERR_ARG, "order N must be in 1..6");
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(DG_ERR_CUDA, "no CUDA device");
+  auto *h = new (std::nothrow) dg_advec_t();
+  if (!h) return fail(DG_ERR_ARG, "out of host memory");
+  std::string err;
+  if (int rc = h->a.create(mesh->m, order, vel_x, vel_y, dt, err)) {
+    delete h;
+    return fail(rc <= -100 ? DG_ERR_CUDA : DG_ERR_ARG, err);
+  }
+  *out = h;
+  return 0;
+}
+
+int dg_advec_init(dg_advec_t *h) {
+  if (!h) return fail(DG_ERR_ARG, "bad arguments");
+  std::string err;
+  if (h->a.init(err)) return fail(DG_ERR_CUDA, err);
+  return 0;
+}
+
+int dg_advec_run(dg_advec_t *h, int nsteps) {
+  if (!h || nsteps < 0) return fail(DG_ERR_ARG, "bad arguments");
+  std::string err;
+  if (h->a.step(nsteps, true, err)) return fail(DG_ERR_CUDA, err);
+  return 0;
+}
+
+int dg_advec_sync(dg_advec_t *h) {
+  if (!h) return fail(DG_ERR_ARG, "bad arguments");
+  CKC(cudaStreamSynchronize(h->a.stream));
+  return 0;
+}
+
+static double *advec_dat(dg_advec_t *h, const std::string &n, size_t &cnt) {
+  cnt = h->a.q_count();
+  if (n == "q") return h->a.d.q;
+  if (n == "workingQ") return h->a.d.W;
+  if (n == "geo") { cnt = (size_t)h->a.K * 16; return const_cast<double *>(h->a.d.geo); }
+  return nullptr;
+}
+
+int dg_advec_get(dg_advec_t *h, const char *name, double *host) {
+  if (!h || !name || !host) return fail(DG_ERR_ARG, "bad arguments");
+  size_t n;
+  double *p = advec_dat(h, name, n);
+  if (!p) return fail(DG_ERR_ARG, std::string("unknown dat ") + name);
+  CKC(cudaMemcpyAsync(host, p, n * 8, cudaMemcpyDeviceToHost, h->a.stream));
+  CKC(cudaStreamSynchronize(h->a.stream));
+  return 0;
+}
+
+int dg_advec_set(dg_advec_t *h, const char *name, const double *host) {
+  if (!h || !name || !host) return fail(DG_ERR_ARG, "bad arguments");
+  std::string n(name);
+  if (n != "q" && n != "workingQ") return fail(DG_ERR_ARG, "only q and workingQ can be set");
+  size_t cnt;
+  double *p = advec_dat(h, n, cnt);
+  CKC(cudaMemcpyAsync(p, host, cnt * 8, cudaMemcpyHostToDevice, h->a.stream));
+  CKC(cudaStreamSynchronize(h->a.stream));
+  return 0;
+}
+
+int dg_advec_rhs(dg_advec_t *h, const double *host_W, double *host_rhs) {
+  if (!h || !host_W || !host_rhs) return fail(DG_ERR_ARG, "bad arguments");
+  const size_t n = h->a.q_count();
+  if (!h->rhs_buf && cudaMalloc(&h->rhs_buf, n * 8) != cudaSuccess) return fail(DG_ERR_CUDA, "cudaMalloc failed");
+  CKC(cudaMemcpyAsync(h->a.d.W, host_W, n * 8, cudaMemcpyHostToDevice, h->a.stream));
+  std::string err;
+  if (h->a.rhs(h->rhs_buf, err)) return fail(DG_ERR_CUDA, err);
+  CKC(cudaMemcpyAsync(host_rhs, h->rhs_buf, n * 8, cudaMemcpyDeviceToHost, h->a.stream));
+  CKC(cudaStreamSynchronize(h->a.stream));
+  return 0;
+}
+
+int dg_advec_time(dg_advec_t *h, double *t, unsigned long long *steps) {
+  if (!h || !t) return fail(DG_ERR_ARG, "bad arguments");
+  *t = h->a.t;
+  if (steps) *steps = h->a.steps;
+  return 0;
+}
+
+int dg_advec_step_timed(dg_advec_t *h, float *ms) {
+  if (!h || !ms) return fail(DG_ERR_ARG, "bad arguments");
+  if (!h->ev[0])
+    for (auto &e : h->ev) CKC(cudaEventCreate(&e));
+  CKC(cudaEventRecord(h->ev[0], h->a.stream));
+  h->a.enqueue_step_events(h->a.stream, h->ev);
+  CKC(cudaGetLastError());
+  CKC(cudaEventSynchronize(h->ev[8]));
+  for (int k = 0; k < 8; k++) CKC(cudaEventElapsedTime(&ms[k], h->ev[k], h->ev[k + 1]));
+  h->a.t += h->a.d.dt;
+  h->a.steps++;
+  return 0;
+}
+
+int dg_advec_vertex_values(dg_advec_t *h, const dg_mesh_t *m, double *out) {
+  if (!h || !m || !out) return fail(DG_ERR_ARG, "bad arguments");
+  if (m->m.n_cells() != h->a.K) return fail(DG_ERR_ARG, "mesh does not match the instance");
+  std::string err;
+  if (h->a.vertex_values(m->m.n_nodes(), out, err)) return fail(DG_ERR_CUDA, err);
+  return 0;
+}
+
+int dg_advec_write_vtk(dg_advec_t *h, const dg_mesh_t *m, const char *path) {
+  if (!h || !m || !path) return fail(DG_ERR_ARG, "bad arguments");
+  std::vector<double> v(m->m.n_nodes());
+  if (int rc = dg_advec_vertex_values(h, m, v.data())) return rc;
+  std::string err;
+  if (dg::write_vtk_scalar(path, m->m, "q", v.data(), err)) return fail(DG_ERR_ARG, err);
+  return 0;
+}
+
+void *dg_advec_stream(dg_advec_t *h) { return h ? (void *)h->a.stream : nullptr; }
+
+void dg_advec_free(dg_advec_t *h) {
+  if (!h) return;
+  if (h->rhs_buf) cudaFree(h->rhs_buf);
+  for (auto &e : h->ev)
+    if (e) cudaEventDestroy(e);
+  delete h;
+}
+
+int dg_mesh_write_vtk(const dg_mesh_t *m, const char *path, const double *rho, const double *u, const double *v,
+                      const double *p) {
+  if (!m || !path || !rho || !u || !v || !p) return fail(DG_ERR_ARG, "bad arguments");
+  std::string err;
+  if (dg::write_vtk(path, m->m, rho, u, v, p, err)) return fail(DG_ERR_ARG, err);
+  return 0;
+}
+
+int dg_solver_vertex_fields(dg_solver_t *h, const dg_mesh_t *m, double *rho, double *u, double *v, double *p) {
+  if (!h || !m || !rho || !u || !v || !p) return fail(DG_ERR_ARG, "bad arguments");
+  if (m->m.n_cells() != h->s.K) return fail(DG_ERR_ARG, "mesh does not match the solver");
+  std::string err;
+  if (h->s.vertex_fields(m->m.n_nodes(), rho, u, v, p, err)) return fail(DG_ERR_CUDA, err);
+  return 0;
+}
+
+int dg_solver_write_vtk(dg_solver_t *h, const dg_mesh_t *m, const char *path) {
+  if (!h || !m || !path) return fail(DG_ERR_ARG, "bad arguments");
+  const int nn = m->m.n_nodes();
+  std::vector<double> f((size_t)4 * nn);
+  if (int rc = dg_solver_vertex_fields(h, m, f.data(), f.data() + nn, f.data() + 2 * (size_t)nn, f.data() + 3 * (size_t)nn))
+    return rc;
+  return dg_mesh_write_vtk(m, path, f.data(), f.data() + nn, f.data() + 2 * (size_t)nn, f.data() + 3 * (size_t)nn);
 }
 
 void dg_solver_free(dg_solver_t *h) {

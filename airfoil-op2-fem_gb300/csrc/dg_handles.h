@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "dg_advec.h"
 #include "dg_mesh.h"
 #include "dg_solver.h"
 
@@ -14,4 +15,9 @@ struct dg_solver_t {
   int dt_hist_len = 0;
   double *rhs_buf = nullptr;
   cudaEvent_t ev[8] = {};
+};
+struct dg_advec_t {
+  dg::Advection a;
+  double *rhs_buf = nullptr;
+  cudaEvent_t ev[9] = {};
 };

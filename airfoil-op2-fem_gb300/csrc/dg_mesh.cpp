@@ -5,6 +5,7 @@
 #include <cmath>
 #include <fstream>
 #include <random>
+#include <cstdio>
 #include <sstream>
 
 namespace dg {
@@ -203,6 +204,54 @@ void sweep_config(int n, uint64_t seed, int *n_theta, int *n_r, int *order, doub
     n_r[i] = (int)std::lround(32.0 + 64.0 * i / (n - 1));
     order[i] = (i % 2) ? 4 : 3;
   }
+}
+
+// Legacy-VTK header and grid; the caller appends POINT_DATA.
+static FILE *vtk_open_grid(const std::string &path, const Mesh &m, std::string &err) {
+  FILE *f = std::fopen(path.c_str(), "w");
+  if (!f) { err = "cannot open " + path; return nullptr; }
+  const int nn = m.n_nodes(), nc = m.n_cells();
+  std::fprintf(f, "# vtk DataFile Version 2.0\nDG solution\nASCII\nDATASET UNSTRUCTURED_GRID\n");
+  std::fprintf(f, "POINTS %d double\n", nn);
+  for (int i = 0; i < nn; i++) std::fprintf(f, "%.17g %.17g 0\n", m.coords[2 * i], m.coords[2 * i + 1]);
+  std::fprintf(f, "CELLS %d %d\n", nc, 4 * nc);
+  for (int c = 0; c < nc; c++)
+    std::fprintf(f, "3 %d %d %d\n", m.cell2nodes[3 * c], m.cell2nodes[3 * c + 1], m.cell2nodes[3 * c + 2]);
+  std::fprintf(f, "CELL_TYPES %d\n", nc);
+  for (int c = 0; c < nc; c++) std::fprintf(f, "5\n");
+  std::fprintf(f, "POINT_DATA %d\n", nn);
+  return f;
+}
+
+static void vtk_scalars(FILE *f, const char *name, const double *v, int n) {
+  std::fprintf(f, "SCALARS %s double 1\nLOOKUP_TABLE default\n", name);
+  for (int i = 0; i < n; i++) std::fprintf(f, "%.17g\n", v[i]);
+}
+
+static int vtk_close(FILE *f, const std::string &path, std::string &err) {
+  const bool ok = std::ferror(f) == 0;
+  if (std::fclose(f) != 0 || !ok) { err = "write error on " + path; return -2; }
+  return 0;
+}
+
+int write_vtk(const std::string &path, const Mesh &m, const double *rho, const double *u, const double *v,
+              const double *p, std::string &err) {
+  FILE *f = vtk_open_grid(path, m, err);
+  if (!f) return -1;
+  const int nn = m.n_nodes();
+  vtk_scalars(f, "rho", rho, nn);
+  vtk_scalars(f, "p", p, nn);
+  std::fprintf(f, "VECTORS velocity double\n");
+  for (int i = 0; i < nn; i++) std::fprintf(f, "%.17g %.17g 0\n", u[i], v[i]);
+  return vtk_close(f, path, err);
+}
+
+int write_vtk_scalar(const std::string &path, const Mesh &m, const char *name, const double *values,
+                     std::string &err) {
+  FILE *f = vtk_open_grid(path, m, err);
+  if (!f) return -1;
+  vtk_scalars(f, name, values, m.n_nodes());
+  return vtk_close(f, path, err);
 }
 
 int validate(const Mesh &m, std::string &err) {

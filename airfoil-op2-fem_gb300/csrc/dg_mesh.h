@@ -49,6 +49,14 @@ int vortex_square(int n, double lo, double hi, uint64_t seed, Mesh &m, std::stri
 // linearly from 128 x 32 to 384 x 96, order 3 for even and 4 for odd instances.
 void sweep_config(int n, uint64_t seed, int *n_theta, int *n_r, int *order, double *alpha_deg, double *mach);
 
+// Legacy-VTK (ASCII) unstructured grid with per-vertex scalars rho, p and vector velocity: the
+// fields src/save_solution.cpp:48-98 writes to CGNS.
+int write_vtk(const std::string &path, const Mesh &m, const double *rho, const double *u, const double *v,
+              const double *p, std::string &err);
+// The same grid with one per-vertex scalar (the advection app's q, advec/src/save_solution.cpp).
+int write_vtk_scalar(const std::string &path, const Mesh &m, const char *name, const double *values,
+                     std::string &err);
+
 // Checks ranges and that every (cell, face) slot is covered by exactly one edge or boundary
 // edge.  The hot path depends on this single-writer property.
 int validate(const Mesh &m, std::string &err);

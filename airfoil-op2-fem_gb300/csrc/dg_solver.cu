@@ -643,6 +643,37 @@ __global__ void l2_error_kernel(const Inst d, const double *coords, const int *c
   for (int k = 0; k < 4; k++) part[4 * (size_t)c + k] = acc[k];
 }
 
+// ---------------------------------------------------------------- solution output
+// src/save_solution.cpp:13-46: per mesh vertex, rho, u, v, p from the cell's vertex node (local
+// nodes 0, N, Np-1 for vertices 0, 1, 2); cells are visited in ascending order there, so the last
+// cell containing a vertex wins.  Here pass 1 finds that cell (atomicMax of the cell index per
+// vertex), pass 2 lets it write: the same values, independent of thread order.
+__global__ void vertex_owner_kernel(int K, const int *cells, int *owner) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= K) return;
+  for (int v = 0; v < 3; v++) atomicMax(&owner[cells[3 * c + v]], c);
+}
+
+template <int N>
+__global__ void vertex_fields_kernel(int K, const int *cells, const int *owner, const double *q, double gam,
+                                     double *rho, double *u, double *v, double *p) {
+  constexpr int Np = np_of(N);
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= K) return;
+  const int local[3] = {0, N, Np - 1};
+  for (int k = 0; k < 3; k++) {
+    const int node = cells[3 * c + k];
+    if (owner[node] != c) continue;
+    const double *qq = q + ((size_t)c * Np + local[k]) * 4;
+    const double r = qq[0], uu = qq[1] / r, vv = qq[2] / r;  // IEEE division, as on the host
+    rho[node] = r;
+    u[node] = uu;
+    v[node] = vv;
+    // unfused products in the reference's order, so the fields are bit-identical to it
+    p[node] = __dmul_rn(gam - 1, __dsub_rn(qq[3], __dmul_rn(0.5, __dadd_rn(__dmul_rn(qq[1], uu), __dmul_rn(qq[2], vv)))));
+  }
+}
+
 // ---------------------------------------------------------------- launch helpers
 template <int N>
 static void launch_face(const Inst &d, int stage, cudaStream_t s) {
@@ -831,6 +862,22 @@ void *Solver::dalloc(size_t bytes) {
   return p;
 }
 
+// Device edge records: {cL, cR, fL | fR << 2 | reverse << 4, 0} and {cell, face, type, 0}.
+static void edge_records(const Mesh &m, std::vector<int4> &edges, std::vector<int4> &bedges) {
+  edges.resize(m.n_edges());
+  bedges.resize(m.n_bedges());
+  for (int i = 0; i < m.n_edges(); i++) {
+    const int cL = m.edge2cells[2 * i], cR = m.edge2cells[2 * i + 1];
+    const int fL = m.edgeNum[2 * i], fR = m.edgeNum[2 * i + 1];
+    // src/get_neighbour_q.h:10-34: vertex fL of L against vertex fR of R, exact comparison
+    const int vL = m.cell2nodes[3 * cL + fL], vR = m.cell2nodes[3 * cR + fR];
+    const bool rev = !(m.coords[2 * vL] == m.coords[2 * vR] && m.coords[2 * vL + 1] == m.coords[2 * vR + 1]);
+    edges[i] = make_int4(cL, cR, fL | (fR << 2) | ((rev ? 1 : 0) << 4), 0);
+  }
+  for (int i = 0; i < m.n_bedges(); i++)
+    bedges[i] = make_int4(m.bedge2cell[i], m.bedgeNum[i], m.bedge_type.empty() ? 2 : m.bedge_type[i], 0);
+}
+
 int Solver::create(const Config &c, const Mesh &m, std::string &err) {
   cfg = c;
   if (int rc = validate(m, err)) return rc;
@@ -870,17 +917,8 @@ int Solver::create(const Config &c, const Mesh &m, std::string &err) {
   d.P.vy0 = c.vortex_y0;
   d.P.vbeta = c.vortex_beta;
 
-  std::vector<int4> edges(d.nE), bedges(d.nB);
-  for (int i = 0; i < d.nE; i++) {
-    const int cL = m.edge2cells[2 * i], cR = m.edge2cells[2 * i + 1];
-    const int fL = m.edgeNum[2 * i], fR = m.edgeNum[2 * i + 1];
-    // src/get_neighbour_q.h:10-34: vertex fL of L against vertex fR of R, exact comparison
-    const int vL = m.cell2nodes[3 * cL + fL], vR = m.cell2nodes[3 * cR + fR];
-    const bool rev = !(m.coords[2 * vL] == m.coords[2 * vR] && m.coords[2 * vL + 1] == m.coords[2 * vR + 1]);
-    edges[i] = make_int4(cL, cR, fL | (fR << 2) | ((rev ? 1 : 0) << 4), 0);
-  }
-  for (int i = 0; i < d.nB; i++)
-    bedges[i] = make_int4(m.bedge2cell[i], m.bedgeNum[i], m.bedge_type.empty() ? 2 : m.bedge_type[i], 0);
+  std::vector<int4> edges, bedges;
+  edge_records(m, edges, bedges);
 
   const size_t nq = (size_t)K * Np * 4;
   d.q = (double *)dalloc(nq * 8);
@@ -999,6 +1037,25 @@ int Solver::l2_error(double err4[4], std::string &err) {
   for (int k = 0; k < 4; k++) err4[k] = 0.0;
   for (int c = 0; c < K; c++)
     for (int k = 0; k < 4; k++) err4[k] += h[4 * (size_t)c + k];
+  return 0;
+}
+
+int Solver::vertex_fields(int n_nodes, double *rho, double *u, double *v, double *p, std::string &err) {
+  int *owner = nullptr;
+  double *buf = nullptr;
+  CK(cudaMallocAsync((void **)&owner, (size_t)n_nodes * 4, stream));
+  CK(cudaMallocAsync((void **)&buf, (size_t)n_nodes * 4 * 8, stream));
+  CK(cudaMemsetAsync(owner, 0xff, (size_t)n_nodes * 4, stream));  // -1: vertex of no cell
+  CK(cudaMemsetAsync(buf, 0, (size_t)n_nodes * 4 * 8, stream));
+  vertex_owner_kernel<<<(K + 127) / 128, 128, 0, stream>>>(K, cells_d, owner);
+  DG_DISPATCH(cfg.N, (vertex_fields_kernel<NN><<<(K + 127) / 128, 128, 0, stream>>>(
+                         K, cells_d, owner, d.q, cfg.gam, buf, buf + n_nodes, buf + 2 * n_nodes, buf + 3 * n_nodes)));
+  double *outs[4] = {rho, u, v, p};
+  for (int k = 0; k < 4; k++)
+    CK(cudaMemcpyAsync(outs[k], buf + (size_t)k * n_nodes, (size_t)n_nodes * 8, cudaMemcpyDeviceToHost, stream));
+  CK(cudaFreeAsync(owner, stream));
+  CK(cudaFreeAsync(buf, stream));
+  CK(cudaStreamSynchronize(stream));
   return 0;
 }
 
@@ -1154,6 +1211,7 @@ extern "C" int dg_rhs_noalloc(const dg_config_t *cfg, int n_cells, int n_edges, 
 
 #include "dg_batch.cuh"
 #include "dg_adjoint.cuh"
+#include "dg_advec.cuh"
 
 // ---------------------------------------------------------------- batched C ABI
 #include "dg_handles.h"

@@ -74,6 +74,8 @@ struct Solver {
   int rhs(double *out_dev, std::string &err);
   int l2_error(double err4[4], std::string &err);
   int state(StepState &s, std::string &err);
+  // rho, u, v, p per mesh vertex as src/save_solution.cpp:13-46 samples them.
+  int vertex_fields(int n_nodes, double *rho, double *u, double *v, double *p, std::string &err);
   size_t q_count() const { return (size_t)K * (cfg.N + 1) * (cfg.N + 2) / 2 * 4; }
 };
 

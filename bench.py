@@ -228,6 +228,51 @@ def adjoint_measure(pkg, nsteps=2000, navg=100, C=50):
             "note": "backward = segment recomputation from checkpoints + reverse sweep"}
 
 
+def advection_measure(pkg, steps=200, n=512, order=4, cpu_steps=40):
+    """The scalar advection app (advec/src/advec.cpp) at scale: [0,10]^2 cut into 2 n^2 = 524288
+    triangles, order 4, velocity (1, 1), dt = 1e-3, classical RK4 (four stages a step).  Device
+    steps are CUDA-graph launches timed with events (q, W and the RK accumulator, 3 x 63 MB, exceed
+    L2); per-kernel times from separately launched steps; the CPU oracle on the same mesh (all
+    cores, a few steps) beside it."""
+    mesh = pkg.Mesh.vortex_square(n, 0.0, 10.0)
+    K = mesh.size("cells")
+    Np = np_of(order)
+    a = pkg.Advection(mesh, N=order, vel_x=1.0, vel_y=1.0, dt=1e-3).init()
+    a.run(3)
+    a.sync()
+    evs = [(pkg.Event(), pkg.Event()) for _ in range(steps)]
+    for i in range(steps):
+        evs[i][0].record(a.stream)
+        a.run(1)
+        evs[i][1].record(a.stream)
+    a.sync()
+    ms = sum(x.elapsed_ms(y) for x, y in evs) / steps
+    per = [a.step_timed() for _ in range(20)]
+    face_ms = sum(sum(p[0::2]) for p in per) / len(per)
+    elem_ms = sum(sum(p[1::2]) for p in per) / len(per)
+    Nfp = order + 1
+    # element kernel, per cell and stage: the contraction 2 (2 Np^2 + 3 Nfp Np), the metric
+    # combine 2 Np + 6 and the RK4 combine 3 Np
+    flops = K * (2 * (2 * Np * Np + 3 * Nfp * Np) + 5 * Np + 6)
+    import __graft_entry__ as g
+    orc, om, oo = g.load_oracle()
+    if not os.path.exists(orc.PORT_LIB):
+        orc.build(ref=False)
+    o = orc.Advection(om.vortex_square(n, 0.0, 10.0), oo.operators(order), 1.0, 1.0)
+    o.init(1e-3)
+    nthreads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    o.run(cpu_steps, nthreads=nthreads)
+    cpu_s = time.perf_counter() - t0
+    dof_stage = 4 * K * Np
+    return {"value": dof_stage / (ms * 1e-3), "unit": "DOF-stage/s", "ms_per_step": ms, "steps": steps,
+            "cells": K, "order": order, "kernels_per_step": 8,
+            "face_kernel_ms_per_stage": face_ms / 4, "elem_kernel_ms_per_stage": elem_ms / 4,
+            "elem_kernel_fp64_tflops": flops / (elem_ms / 4 * 1e-3) / 1e12,
+            "cpu_oracle": {"value": cpu_steps * dof_stage / cpu_s, "unit": "DOF-stage/s", "cores": nthreads,
+                           "sample": "%d RK4 steps of the same mesh (%.1f s)" % (cpu_steps, cpu_s)}}
+
+
 def run_reference(args):
     """The reference arm: the reference's user kernels (restated; the reference's own build is
     N=4-only and cannot run this N=3 workload) on all host cores."""
@@ -268,11 +313,13 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--cpu-steps", type=int, default=40, help="CPU-baseline sample size (steps)")
+    ap.add_argument("--cpu-steps", type=int, default=1500,
+                    help="CPU-baseline sample size (steps; ~10 s on 16 Grace cores)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batched-steps", type=int, default=20)
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-advection", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -405,6 +452,8 @@ def main():
         line["batched"] = batched_measure(pkg, args.batched_steps)
     if not args.no_adjoint:
         line["adjoint"] = adjoint_measure(pkg)
+    if not args.no_advection:
+        line["advection"] = advection_measure(pkg)
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:

@@ -104,6 +104,38 @@ void *dg_solver_stream(dg_solver_t *s);
 /* Launch one step as separate kernels with an event between each, wait, and write the seven
  * kernel durations (face, elem x 3 stages, finalize) in milliseconds. */
 int dg_solver_step_timed(dg_solver_t *s, float *ms7);
+/* Per mesh vertex rho, u, v, p (host arrays of n_nodes) sampled as src/save_solution.cpp:13-46
+ * does (the vertex nodes of the last cell containing the vertex), and the same fields written as
+ * a legacy-VTK file (the reference writes them to CGNS, :48-98). */
+int dg_solver_vertex_fields(dg_solver_t *s, const dg_mesh_t *mesh, double *rho, double *u, double *v, double *p);
+int dg_solver_write_vtk(dg_solver_t *s, const dg_mesh_t *mesh, const char *path);
+/* ------------------------------------------------------------------ scalar advection app
+ * advec/src/advec.cpp: one scalar per node (q [n_cells][Np] doubles), flux (vx q, vy q) with the
+ * Lax-Friedrichs face flux of advec/src/advec_rhs.h:36-63, the constant ghost value 4.5e-5 on
+ * every boundary face (advec/src/get_bedge_q.h), the Gaussian pulse of advec/src/set_ic.h and
+ * classical RK4 with a fixed dt (advec.cpp:230-296; -vx/-vy/-iter there are vel_x, vel_y and the
+ * step count here).  Same operators, geometry and edge records as the Euler solver; order 1..6. */
+typedef struct dg_advec_t dg_advec_t;
+int dg_advec_create(const dg_mesh_t *mesh, int order, double vel_x, double vel_y, double dt, dg_advec_t **out);
+int dg_advec_init(dg_advec_t *a);                 /* set_ic, t = 0 */
+int dg_advec_run(dg_advec_t *a, int nsteps);      /* enqueue nsteps RK4 steps (a CUDA graph) */
+int dg_advec_sync(dg_advec_t *a);
+int dg_advec_get(dg_advec_t *a, const char *name, double *host);        /* q, workingQ, geo */
+int dg_advec_set(dg_advec_t *a, const char *name, const double *host);  /* q, workingQ */
+/* One right-hand side of W (advec_rhs after the face loops); overwrites workingQ. */
+int dg_advec_rhs(dg_advec_t *a, const double *W, double *rhs);
+int dg_advec_time(dg_advec_t *a, double *t, unsigned long long *steps);
+/* One step as separate launches with per-kernel times (face, element) x 4 stages, in ms. */
+int dg_advec_step_timed(dg_advec_t *a, float *ms8);
+/* q per mesh vertex as advec/src/save_solution.cpp:13-52 samples it, and as a legacy-VTK file. */
+int dg_advec_vertex_values(dg_advec_t *a, const dg_mesh_t *mesh, double *out);
+int dg_advec_write_vtk(dg_advec_t *a, const dg_mesh_t *mesh, const char *path);
+void *dg_advec_stream(dg_advec_t *a);
+void dg_advec_free(dg_advec_t *a);
+
+/* The writer alone (host only): per-vertex fields given by the caller. */
+int dg_mesh_write_vtk(const dg_mesh_t *mesh, const char *path, const double *rho, const double *u,
+                      const double *v, const double *p);
 void dg_solver_free(dg_solver_t *s);
 
 /* ------------------------------------------------------------------ batched instances

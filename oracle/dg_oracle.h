@@ -83,6 +83,19 @@ int orc_l2_error(void *h, double *err4);
 /* Recompute dt = (1/dt1)*cfl from the current q and fscale (after geometry was replaced with orc_set). */
 int orc_refresh_dt(void *h);
 
+/* Scalar advection app (advec/src/advec.cpp): one value per node, q[c*Np + node].
+ * adv_init runs init_grid and set_ic and fixes dt; adv_rhs evaluates one stage's right-hand
+ * side of workingQ into rk<stage+1>; adv_run takes classical RK4 steps (advec.cpp:237-296).
+ * Dats by name: q, workingQ, rk1..rk4, exteriorQ and the geometry dats of orc_get. */
+void *adv_create(const orc_ops *ops, const orc_mesh *mesh, double vel_x, double vel_y);
+void adv_destroy(void *h);
+int adv_init(void *h, double dt);
+int adv_get(void *h, const char *name, double *out);
+int adv_set(void *h, const char *name, const double *in);
+int adv_rhs(void *h, int stage);
+int adv_run(void *h, int iters, int nthreads);
+double adv_time(void *h);
+
 #ifdef __cplusplus
 }
 #endif

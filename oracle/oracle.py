@@ -75,6 +75,16 @@ def load(kind: str = "port"):
         lib.orc_time.argtypes = [C.c_void_p]
         lib.orc_l2_error.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         lib.orc_refresh_dt.argtypes = [C.c_void_p]
+        lib.adv_create.restype = C.c_void_p
+        lib.adv_create.argtypes = [C.POINTER(_Ops), C.POINTER(_Mesh), C.c_double, C.c_double]
+        lib.adv_destroy.argtypes = [C.c_void_p]
+        lib.adv_init.argtypes = [C.c_void_p, C.c_double]
+        lib.adv_get.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_double)]
+        lib.adv_set.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_double)]
+        lib.adv_rhs.argtypes = [C.c_void_p, C.c_int]
+        lib.adv_run.argtypes = [C.c_void_p, C.c_int, C.c_int]
+        lib.adv_time.restype = C.c_double
+        lib.adv_time.argtypes = [C.c_void_p]
         _LIBS[path] = lib
     return _LIBS[path]
 
@@ -101,6 +111,30 @@ def _ip(a):
     return a.ctypes.data_as(C.POINTER(C.c_int))
 
 
+def _structs(mesh, ops):
+    """(_Ops, _Mesh, arrays to keep alive) from an operator dict and a mesh dict."""
+    keep = {}
+    N = int(ops["N"])
+
+    def f64(name):
+        a = np.ascontiguousarray(ops[name], dtype=np.float64).ravel()
+        keep[name] = a
+        return _dp(a)
+
+    fm = np.ascontiguousarray(ops["FMASK"], dtype=np.int32).ravel()
+    keep["FMASK"] = fm
+    o = _Ops(N, f64("r"), f64("s"), f64("Dr"), f64("Ds"), f64("Drw"), f64("Dsw"), f64("LIFT"), _ip(fm))
+    m = {k: np.ascontiguousarray(v) for k, v in mesh.items()}
+    if "bedge_type" not in m:
+        m["bedge_type"] = np.full(m["bedge2cell"].shape[0], 2, dtype=np.int32)
+    keep.update(m)
+    ms = _Mesh(int(m["coords"].shape[0]), int(m["cell2nodes"].shape[0]), int(m["edge2cells"].shape[0]),
+               int(m["bedge2cell"].shape[0]), _dp(m["coords"]), _ip(m["cell2nodes"]),
+               _ip(m["edge2cells"]), _ip(m["edgeNum"]), _ip(m["bedge2cell"]),
+               _ip(m["bedgeNum"]), _ip(m["bedge_type"]))
+    return o, ms, keep
+
+
 class Oracle:
     """One oracle instance over a mesh dict (oracle.mesh layout) and an operator dict
     (oracle.operators layout)."""
@@ -110,26 +144,9 @@ class Oracle:
         self.N = int(ops["N"])
         self.Np = (self.N + 1) * (self.N + 2) // 2
         self.Nfp = self.N + 1
-        keep = {}
-
-        def f64(name):
-            a = np.ascontiguousarray(ops[name], dtype=np.float64).ravel()
-            keep[name] = a
-            return _dp(a)
-
-        fm = np.ascontiguousarray(ops["FMASK"], dtype=np.int32).ravel()
-        keep["FMASK"] = fm
-        self._ops = _Ops(self.N, f64("r"), f64("s"), f64("Dr"), f64("Ds"), f64("Drw"), f64("Dsw"),
-                         f64("LIFT"), _ip(fm))
+        self._ops, self._mesh, self._keep = _structs(mesh, ops)
         self._phys = _Phys(**{k: float(phys[k]) for k, _ in _Phys._fields_})
-        m = {k: np.ascontiguousarray(v) for k, v in mesh.items()}
-        keep.update(m)
-        self.K = int(m["cell2nodes"].shape[0])
-        self._mesh = _Mesh(int(m["coords"].shape[0]), self.K, int(m["edge2cells"].shape[0]),
-                           int(m["bedge2cell"].shape[0]), _dp(m["coords"]), _ip(m["cell2nodes"]),
-                           _ip(m["edge2cells"]), _ip(m["edgeNum"]), _ip(m["bedge2cell"]),
-                           _ip(m["bedgeNum"]), _ip(m["bedge_type"]))
-        self._keep = keep
+        self.K = int(self._mesh.n_cells)
         self.h = self.lib.orc_create(C.byref(self._ops), C.byref(self._phys), C.byref(self._mesh), app)
         if not self.h:
             raise RuntimeError(self.lib.orc_last_error().decode())
@@ -189,6 +206,101 @@ class Oracle:
     def _check(self, rc):
         if rc != 0:
             raise RuntimeError(self.lib.orc_last_error().decode())
+
+
+class Advection:
+    """The scalar advection app (advec/src/advec.cpp) on the oracle: q has one value per node."""
+
+    def __init__(self, mesh, ops, vel_x=1.0, vel_y=1.0, kind="port"):
+        self.lib = load(kind)
+        self.N = int(ops["N"])
+        self.Np = (self.N + 1) * (self.N + 2) // 2
+        self.Nfp = self.N + 1
+        self._ops, self._mesh, self._keep = _structs(mesh, ops)
+        self.K = int(self._mesh.n_cells)
+        self.h = self.lib.adv_create(C.byref(self._ops), C.byref(self._mesh), vel_x, vel_y)
+        if not self.h:
+            raise RuntimeError(self.lib.orc_last_error().decode())
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            self.lib.adv_destroy(h)
+            self.h = None
+
+    def dim(self, name):
+        return {"nodeX": 3, "nodeY": 3, "nx": 3 * self.Nfp, "ny": 3 * self.Nfp, "fscale": 3 * self.Nfp,
+                "exteriorQ": 3 * self.Nfp}.get(name, self.Np)
+
+    def init(self, dt=1e-3):
+        self._check(self.lib.adv_init(self.h, dt))
+
+    def get(self, name):
+        out = np.empty(self.K * self.dim(name))
+        self._check(self.lib.adv_get(self.h, name.encode(), _dp(out)))
+        return out
+
+    def set(self, name, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64).ravel()
+        assert a.size == self.K * self.dim(name)
+        self._check(self.lib.adv_set(self.h, name.encode(), _dp(a)))
+
+    def rhs(self, stage=0):
+        self._check(self.lib.adv_rhs(self.h, stage))
+        return self.get("rk%d" % (stage + 1))
+
+    def run(self, iters, nthreads=0):
+        self._check(self.lib.adv_run(self.h, iters, nthreads))
+
+    @property
+    def t(self):
+        return self.lib.adv_time(self.h)
+
+    def _check(self, rc):
+        if rc != 0:
+            raise RuntimeError(self.lib.orc_last_error().decode())
+
+
+def vertex_fields(cells, q, N, gam=1.4, n_nodes=None):
+    """rho, u, v, p per mesh vertex, restating src/save_solution.cpp:13-46: cells visited in
+    ascending order, vertex k of a cell takes local node (0, N, Np-1)[k], a later cell
+    overwrites an earlier one."""
+    cells = np.asarray(cells, dtype=np.int64).reshape(-1, 3)
+    Np = (N + 1) * (N + 2) // 2
+    q = np.asarray(q, dtype=np.float64).reshape(len(cells), Np, 4)
+    n_nodes = int(cells.max()) + 1 if n_nodes is None else n_nodes
+    out = np.zeros((4, n_nodes))
+    local = (0, N, Np - 1)
+    node = cells.reshape(-1)                         # visiting order: cell-major, vertex 0..2
+    qv = q[np.repeat(np.arange(len(cells)), 3), np.tile(local, len(cells))]
+    last = len(node) - 1 - np.unique(node[::-1], return_index=True)[1]   # last visit per vertex
+    n, qq = node[last], qv[last]
+    r = qq[:, 0]
+    u = qq[:, 1] / r
+    v = qq[:, 2] / r
+    out[0, n], out[1, n], out[2, n] = r, u, v
+    out[3, n] = (gam - 1) * (qq[:, 3] - 0.5 * (qq[:, 1] * u + qq[:, 2] * v))
+    return out
+
+
+def read_vtk_point_data(path):
+    """The POINT_DATA arrays of a legacy-ASCII VTK file as {name: array}."""
+    tok = open(path).read().split()
+    i, out = tok.index("POINT_DATA"), {}
+    n = int(tok[i + 1])
+    i += 2
+    while i < len(tok):
+        if tok[i] == "SCALARS":
+            name, i = tok[i + 1], i + 6           # SCALARS name type 1 LOOKUP_TABLE default
+            out[name] = np.array(tok[i:i + n], dtype=np.float64)
+            i += n
+        elif tok[i] == "VECTORS":
+            name, i = tok[i + 1], i + 3
+            out[name] = np.array(tok[i:i + 3 * n], dtype=np.float64).reshape(n, 3)
+            i += 3 * n
+        else:
+            raise ValueError("unexpected token " + tok[i])
+    return out
 
 
 def rel_l2(a, b):

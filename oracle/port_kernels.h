@@ -24,6 +24,7 @@ struct Ctx {
   std::vector<int> FMASK;
   double gam, bc_mach, bc_alpha, bc_p, bc_r, bc_u, bc_v, bc_e;
   double vortex_x0, vortex_y0, vortex_beta;
+  double velX = 1.0, velY = 1.0;  // scalar advection velocity (advec/src/constants/constant_util.h:9-10)
 };
 extern Ctx g;
 

@@ -62,6 +62,16 @@ def golden_vortex():
     return load_golden("vortex_n4.npz")
 
 
+@pytest.fixture(scope="session")
+def golden_advec():
+    d, mesh = load_golden("advec_n4.npz")
+    for k in ("rhs_perturbed", "q100"):       # stored sparse: rebuild the dense vector
+        a = np.zeros(int(d[k + "_n"]))
+        a[d[k + "_idx"]] = d[k + "_val"]
+        d[k] = a
+    return d, mesh
+
+
 def reference_tables():
     """The reference's literal N=4 tables, read from its constants headers (only where the
     reference tree exists)."""

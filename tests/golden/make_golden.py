@@ -13,11 +13,18 @@ on the reference's own meshes:
   vortex_n4.npz    vortex/grid.vtk (K=618, N=4), isentropic vortex x0=5, beta=5,
                    dt = 0.1/dt1 frozen (vortex/src/vortex.cpp:209-306): q and the
                    L2 error sums after 100 steps.
+  advec_n4.npz     advec/grid.vtk (K=23252, N=4), scalar advection with velocity
+                   (1, 1) and dt = 0.001 (advec/src/advec.cpp:230): the RHS of a
+                   seeded perturbed state and q after 100 RK4 steps (the app's
+                   default -iter).  Both are stored sparse (entries of magnitude at least
+                   1e-16 of the largest, with the relative L2 of the rest, below 4e-16):
+                   the boundary ghost value seeds a tail of tiny values that would not
+                   compress.
 Each file also holds the mesh tables (coordinates, cells, edge and boundary-edge
 tables built with the conventions of tools/vtk2CGNS.cpp), so that tests can run
 where the reference tree is absent.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [naca] [vortex] [advec]   (default: all)
 """
 from __future__ import annotations
 
@@ -47,13 +54,7 @@ def mesh_arrays(m):
     return {"mesh_" + k: v for k, v in m.items()}
 
 
-def main():
-    if not os.path.isdir(REF):
-        raise SystemExit("reference tree not present")
-    orc.build(ref=True)
-    ops = oo.operators(4)  # ignored by the reference build except for N
-
-    # --- airfoil
+def make_naca(ops):
     coords, cells = om.read_vtk(os.path.join(REF, "naca0012.vtk"))
     m = om.build_tables(coords, cells)
     m["bedge_type"] = om.classify_box(m)
@@ -77,7 +78,8 @@ def main():
                         t1000=o2.t, **mesh_arrays(m))
     print("naca0012: K=%d dt0=%.17g t1000=%.17g" % (o.K, dt0, o2.t))
 
-    # --- vortex
+
+def make_vortex(ops):
     coords, cells = om.read_vtk(os.path.join(REF, "vortex", "grid.vtk"))
     mv = om.build_tables(coords, cells)
     mv["bedge_type"] = np.zeros(mv["bedge2cell"].shape[0], dtype=np.int32)
@@ -92,5 +94,40 @@ def main():
     print("vortex: K=%d dt=%.17g l2=%s" % (v.K, dtv, v.l2_error()))
 
 
+def sparse(name, a, rel=1e-16):
+    """{name_idx, name_val, name_n, name_dropped}: the entries with |a| >= rel * max|a|."""
+    keep = np.abs(a) >= rel * np.abs(a).max()
+    dropped = np.linalg.norm(a[~keep]) / np.linalg.norm(a)
+    return {name + "_idx": np.flatnonzero(keep).astype(np.int32), name + "_val": a[keep],
+            name + "_n": a.size, name + "_dropped": dropped}
+
+
+def make_advec(ops):
+    coords, cells = om.read_vtk(os.path.join(REF, "advec", "grid.vtk"))
+    m = om.build_tables(coords, cells)
+    a = orc.Advection(m, ops, 1.0, 1.0, kind="reference")
+    a.init(1e-3)
+    q0 = a.get("q")
+    a.set("workingQ", perturbed(q0, amp=0.5))
+    rhs_p = a.rhs(0)
+    a.set("workingQ", q0)
+    a.run(100, nthreads=8)
+    np.savez_compressed(os.path.join(HERE, "advec_n4.npz"), dt=1e-3, vel=np.array([1.0, 1.0]),
+                        perturb_seed=PERTURB_SEED, perturb_amp=0.5, t100=a.t,
+                        **sparse("rhs_perturbed", rhs_p), **sparse("q100", a.get("q")),
+                        **mesh_arrays(m))
+    print("advec: K=%d t100=%.17g" % (a.K, a.t))
+
+
+def main(which):
+    if not os.path.isdir(REF):
+        raise SystemExit("reference tree not present")
+    orc.build(ref=True)
+    ops = oo.operators(4)  # ignored by the reference build except for N
+    makers = {"naca": make_naca, "vortex": make_vortex, "advec": make_advec}
+    for name in which or list(makers):
+        makers[name](ops)
+
+
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])
