@@ -71,6 +71,7 @@ def lib():
                                           C.POINTER(vp)]),
         "dg_mesh_read_vtk": (C.c_int, [cp, C.c_int, C.POINTER(vp)]),
         "dg_mesh_naca_ogrid": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.POINTER(vp)]),
+        "dg_mesh_from_cells_device": (C.c_int, [C.c_int, dp, C.c_int, ip, C.POINTER(vp), C.POINTER(C.c_float)]),
         "dg_mesh_vortex_square": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_ulonglong, C.POINTER(vp)]),
         "dg_mesh_size": (C.c_int, [vp, C.c_int]),
         "dg_mesh_get": (C.c_int, [vp, cp, vp]),
@@ -184,9 +185,18 @@ class Mesh:
             self.h = None
 
     @classmethod
-    def from_cells(cls, coords, cells):
+    def from_cells(cls, coords, cells, device=False):
+        """Edge tables from cells + coordinates, on the host or (device=True) on the GPU; the
+        two give identical tables.  After a device build, `build_ms` holds its device time."""
         coords, cells = _f64(coords), _i32(cells)
         h = C.c_void_p()
+        if device:
+            ms = C.c_float()
+            _check(lib().dg_mesh_from_cells_device(coords.shape[0], _dp(coords), cells.shape[0], _ip(cells),
+                                                   C.byref(h), C.byref(ms)))
+            out = cls(h)
+            out.build_ms = ms.value
+            return out
         _check(lib().dg_mesh_from_cells(coords.shape[0], _dp(coords), cells.shape[0], _ip(cells), C.byref(h)))
         return cls(h)
 

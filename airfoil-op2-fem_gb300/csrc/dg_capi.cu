@@ -66,6 +66,20 @@ int dg_mesh_from_cells(int n_nodes, const double *coords, int n_cells, const int
   return finish_mesh(m, out);
 }
 
+int dg_mesh_from_cells_device(int n_nodes, const double *coords, int n_cells, const int *cell2nodes,
+                              dg_mesh_t **out, float *device_ms) {
+  if (!out || !coords || !cell2nodes || n_nodes <= 0 || n_cells <= 0) return fail(DG_ERR_ARG, "bad arguments");
+  if ((long long)n_nodes * n_nodes >= (1ll << 62) || 3ll * n_cells >= (1ll << 31)) return fail(DG_ERR_ARG, "mesh too large");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(DG_ERR_CUDA, "no CUDA device");
+  dg::Mesh m;
+  m.coords.assign(coords, coords + 2 * (size_t)n_nodes);
+  m.cell2nodes.assign(cell2nodes, cell2nodes + 3 * (size_t)n_cells);
+  std::string err;
+  if (int rc = dg::build_tables_device(m, device_ms, err)) return fail(rc <= -100 ? DG_ERR_CUDA : DG_ERR_ARG, "mesh: " + err);
+  return finish_mesh(m, out);
+}
+
 int dg_mesh_from_tables(int n_nodes, const double *coords, int n_cells, const int *cell2nodes,
                         int n_edges, const int *edge2cells, const int *edgeNum, int n_bedges,
                         const int *bedge2cell, const int *bedgeNum, const int *bedge_type,

@@ -33,6 +33,10 @@ int read_vtk(const std::string &path, std::vector<double> &coords, std::vector<i
 // edge is side 0.  Interior edges and boundary edges are split in that order.
 int build_tables(Mesh &m, std::string &err);
 
+// The same tables built on the GPU (dg_mesh_device.cu); bit-identical to build_tables.
+// device_ms (optional) receives the device time of the build, copies excluded.
+int build_tables_device(Mesh &m, float *device_ms, std::string &err);
+
 // Boundary typing of src/load_mesh.cpp:147-171 for the reference's rectangular Gmsh box.
 int classify_box(Mesh &m, std::string &err);
 

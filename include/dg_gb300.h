@@ -38,6 +38,11 @@ typedef struct dg_mesh_t dg_mesh_t;
  * (counter-clockwise fix, face j = (v_j, v_j+1), edges in sorted-vertex-pair order). */
 int dg_mesh_from_cells(int n_nodes, const double *coords, int n_cells, const int *cell2nodes,
                        dg_mesh_t **out);
+/* The same tables built on the GPU (orientation fix, radix sort of the half-edges, run
+ * detection, scan, scatter), bit-identical to dg_mesh_from_cells; device_ms (may be NULL)
+ * receives the device time of the build, host<->device copies excluded. */
+int dg_mesh_from_cells_device(int n_nodes, const double *coords, int n_cells, const int *cell2nodes,
+                              dg_mesh_t **out, float *device_ms);
 /* Tables as src/load_mesh.cpp:36-192 returns them (replaces load_mesh's outputs). */
 int dg_mesh_from_tables(int n_nodes, const double *coords, int n_cells, const int *cell2nodes,
                         int n_edges, const int *edge2cells, const int *edgeNum, int n_bedges,

@@ -81,3 +81,49 @@ def test_rejects_bad_tables(pkg, golden_naca):
         pkg.Mesh.from_tables(bad)
     with pytest.raises(pkg.DGError):
         pkg.Mesh.from_cells(m["coords"], np.array([[0, 1, 1 << 20]]))
+
+
+# ---------------------------------------------------------------- edge tables built on the GPU
+def _scrambled(coords, cells, seed):
+    """The same triangles with some orientations flipped and the cells shuffled: exercises the
+    orientation fix and the side-0 rule (first cell in cell order)."""
+    rng = np.random.default_rng(seed)
+    c = np.array(cells, dtype=np.int32).reshape(-1, 3)[rng.permutation(len(cells))]
+    flip = rng.random(len(c)) < 0.5
+    c[flip] = c[flip][:, [0, 2, 1]]
+    return np.asarray(coords, dtype=np.float64), c
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["golden", "ogrid", "square", "large"])
+def test_device_edge_tables_equal_host(pkg, omesh, golden_naca, case):
+    if case == "golden":
+        coords, cells = golden_naca[1]["coords"], golden_naca[1]["cell2nodes"]
+    elif case == "ogrid":
+        m = omesh.naca_ogrid(64, 16)
+        coords, cells = m["coords"], m["cell2nodes"]
+    else:
+        n = 24 if case == "square" else 512     # 524288 cells for "large"
+        m = pkg.Mesh.vortex_square(n).arrays()
+        coords, cells = m["coords"], m["cell2nodes"]
+    coords, cells = _scrambled(coords, cells, 3)
+    host = pkg.Mesh.from_cells(coords, cells).arrays()
+    dev_mesh = pkg.Mesh.from_cells(coords, cells, device=True)
+    dev = dev_mesh.arrays()
+    for k in host:
+        assert np.array_equal(host[k], dev[k]), k
+    assert dev_mesh.build_ms > 0.0
+
+
+@pytest.mark.gpu
+def test_device_edge_tables_reject_bad_cells(pkg, golden_naca):
+    coords, cells = golden_naca[1]["coords"], np.array(golden_naca[1]["cell2nodes"])
+    bad = cells.copy()
+    bad[5, 1] = len(coords)                      # vertex out of range
+    with pytest.raises(pkg.DGError):
+        pkg.Mesh.from_cells(coords, bad, device=True)
+    tri = np.concatenate([cells, cells[:1]])     # an edge shared by three cells
+    with pytest.raises(pkg.DGError):
+        pkg.Mesh.from_cells(coords, tri, device=True)
+    ok = pkg.Mesh.from_cells(coords, cells, device=True)   # the context is still usable
+    assert ok.size("cells") == len(cells)
