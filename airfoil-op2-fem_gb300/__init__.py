@@ -141,6 +141,8 @@ def lib():
         "dg_adjoint_dt_sequence": (C.c_int, [vp, dp, C.c_int]),
         "dg_adjoint_rhs_vjp": (C.c_int, [vp, dp, dp, dp, dp]),
         "dg_adjoint_stream": (vp, [vp]),
+        "dg_adjoint_batch_forward": (C.c_int, [C.POINTER(vp), C.c_int, dp]),
+        "dg_adjoint_batch_backward": (C.c_int, [C.POINTER(vp), C.c_int, C.c_double, dp, C.POINTER(dp)]),
         "dg_adjoint_free": (None, [vp]),
         "dg_adjoint_last_error": (cp, []),
     }
@@ -428,8 +430,10 @@ class Batch:
 
 
 class LiftObjective:
-    """Lift-coefficient objective with its discrete adjoint (dg_adjoint_t), used like
-    torch.autograd.Function: J = forward(); grad_alpha, grad_q0 = backward(grad_J)."""
+    """An objective with its discrete adjoint (dg_adjoint_t), used like torch.autograd.Function:
+    J = forward(); grad_param, grad_q0 = backward(grad_J).  Airfoil (cfg.app 0): mean lift
+    coefficient over the last navg steps, parameter alpha (degrees).  Vortex (cfg.app 1):
+    final-time squared error against the analytic vortex, parameter beta."""
 
     def __init__(self, mesh, cfg, nsteps, navg, checkpoint_every=50):
         self.mesh, self.cfg, self.nsteps = mesh, cfg, nsteps
@@ -480,6 +484,24 @@ class LiftObjective:
     @property
     def stream(self):
         return lib().dg_adjoint_stream(self.h)
+
+
+def adjoint_batch_forward(objs):
+    """forward() of every objective at once (concurrent, one stream and host thread each)."""
+    hs = (C.c_void_p * len(objs))(*[o.h.value for o in objs])
+    J = np.empty(len(objs))
+    LiftObjective._check(lib().dg_adjoint_batch_forward(hs, len(objs), _dp(J)))
+    return J
+
+
+def adjoint_batch_backward(objs, grad_J=1.0, want_q0=False):
+    """backward(grad_J) of every objective at once: (grad_param[n], [grad_q0] or None)."""
+    hs = (C.c_void_p * len(objs))(*[o.h.value for o in objs])
+    g = np.empty(len(objs))
+    gq = [np.empty(o.nq) for o in objs] if want_q0 else None
+    ptrs = (C.POINTER(C.c_double) * len(objs))(*[_dp(a) for a in gq]) if want_q0 else None
+    LiftObjective._check(lib().dg_adjoint_batch_backward(hs, len(objs), grad_J, _dp(g), ptrs))
+    return g, gq
 
 
 def sweep_config(n=64, seed=20261203):

@@ -9,6 +9,12 @@
 // Gradients with respect to alpha (degrees; through the boundary states and the initial state)
 // and the initial field q0, with the dt sequence frozen from the forward run.
 //
+// Objective (isentropic vortex, app 1): the final-time sum over nodes and variables of the
+// squared error against the analytic vortex (the four sums of vortex/src/l2_error.h:3-29
+// added), J = sum (q_N - q_ex(t_N; beta))^2.  The scalar parameter is then the vortex strength
+// beta, entering through the initial state, the analytic boundary states of every stage and
+// the exact solution in J; the gradient with respect to q0 is as above.
+//
 // One reverse SSPRK3 step (Shu-Osher form: W1 = q + dt L(q); W2 = 3/4 q + 1/4 (W1 + dt L(W1));
 // q' = 1/3 q + 2/3 (W2 + dt L(W2))), with G(W, v) = (dL/dW at W)^T v:
 //   lW2 = 2/3 l' + 2/3 dt G(W2, l')
@@ -294,9 +300,31 @@ __global__ void __launch_bounds__(32 * np_of(N)) adj_elem_kernel(const Inst d, c
 // ---------------------------------------------------------------- adjoint face kernel
 // Reverse of face_node: writes the adjoint of each cell face-node trace into tracebar slots
 // [K][3][Nfp][4] (one writer each) and adds scale * (qbb . d ghost / d alpha) to galpha[tid].
+// The vortex state and its derivative with respect to beta (vortex_state with P.vbeta):
+// rho = s^(1/(g-1)), s = 1 - k beta^2, u = 1 + beta cu, v = beta cv.
+__device__ __forceinline__ void vortex_state_dbeta(double x, double y, double t, const Phys &P, double dq[4]) {
+  const double dx = x - t - P.vx0, dy = y - P.vy0;
+  const double r2 = dx * dx + dy * dy;
+  const double e1 = exp(1.0 - r2);
+  const double b = P.vbeta;
+  const double cu = -e1 * (dy / (2 * M_PI)), cv = e1 * ((x - P.vx0) / (2 * M_PI));
+  const double u = 1.0 + b * cu, v = b * cv;
+  const double k = (P.gm1 / (16 * P.gam * M_PI * M_PI)) * exp(2 * (1.0 - r2));
+  const double sb = 1.0 - k * b * b;
+  const double rho = pow(sb, 1.0 / P.gm1);
+  const double p = pow(rho, P.gam);
+  const double drho = rho / (P.gm1 * sb) * (-2.0 * k * b);
+  const double dp = P.gam * (p / rho) * drho;
+  dq[0] = drho;
+  dq[1] = drho * u + rho * cu;
+  dq[2] = drho * v + rho * cv;
+  dq[3] = dp / P.gm1 + 0.5 * drho * (u * u + v * v) + rho * (u * cu + v * cv);
+}
+
 template <int N>
 __global__ void __launch_bounds__(256) adj_face_kernel(const Inst d, const double *fluxbar, double *tracebar,
-                                                        double *galpha, const double ascale, const AlphaSens S) {
+                                                        double *galpha, const double ascale, const AlphaSens S,
+                                                        const double t_stage) {
   constexpr int Np = np_of(N), Nfp = N + 1;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int total = (d.nE + d.nB) * Nfp;
@@ -341,12 +369,22 @@ __global__ void __launch_bounds__(256) adj_face_kernel(const Inst d, const doubl
     qm[0] = a.x; qm[1] = a.y; qm[2] = bb.x; qm[3] = bb.y;
     const double *g = d.geo + (size_t)c * 16 + 4 + 3 * f;
     const double nx = g[0], ny = g[1], s = 0.5 * g[2];
-    bc_state(type, qm, nx, ny, P, qp);
     const size_t sl = (((size_t)c * 3 + f) * Nfp + i) * 4;
     const double2 la = ld2(fluxbar + sl), lb = ld2(fluxbar + sl + 2);
     fb[0] = s * la.x; fb[1] = s * la.y; fb[2] = s * lb.x; fb[3] = s * lb.y;
-    roe_flux2_adj(qm, qp, nx, ny, P, fb, qmb, qpb);
-    galpha[tid] += ascale * bc_state_adj(type, nx, ny, qpb, S, qmb);
+    if (d.app == 1) {
+      // analytic ghost state: no dependence on the interior; its beta sensitivity
+      const double *xy = d.bxy + ((size_t)b * Nfp + i) * 2;
+      double dqp[4];
+      vortex_state(xy[0], xy[1], t_stage, P, qp);
+      vortex_state_dbeta(xy[0], xy[1], t_stage, P, dqp);
+      roe_flux2_adj(qm, qp, nx, ny, P, fb, qmb, qpb);
+      galpha[tid] += ascale * (qpb[0] * dqp[0] + qpb[1] * dqp[1] + qpb[2] * dqp[2] + qpb[3] * dqp[3]);
+    } else {
+      bc_state(type, qm, nx, ny, P, qp);
+      roe_flux2_adj(qm, qp, nx, ny, P, fb, qmb, qpb);
+      galpha[tid] += ascale * bc_state_adj(type, nx, ny, qpb, S, qmb);
+    }
     st2(tracebar + sl, qmb[0], qmb[1]);
     st2(tracebar + sl + 2, qmb[2], qmb[3]);
   }
@@ -441,6 +479,56 @@ __global__ void ic_alpha_kernel(const int K, const double *lam, const AlphaSens 
   parts[e] = acc;
 }
 
+// Vortex objective per cell: sum over nodes and variables of (q - q_ex(t))^2 and its explicit
+// beta derivative; with lam non-null adds dJ/dq = 2 (q - q_ex) (one writer per node).
+template <int N>
+__global__ void vortex_obj_kernel(const Inst d, const double *coords, const int *cells, const double *q,
+                                  const double t, double *parts, double *dparts, double *lam) {
+  constexpr int Np = np_of(N);
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= d.K) return;
+  const int a = cells[3 * c], b = cells[3 * c + 1], e = cells[3 * c + 2];
+  double acc = 0.0, dacc = 0.0;
+  for (int i = 0; i < Np; i++) {
+    const double r = c_rs[N][i], s = c_rs[N][Np + i];
+    const double x = node_coord(coords[2 * a], coords[2 * b], coords[2 * e], r, s);
+    const double y = node_coord(coords[2 * a + 1], coords[2 * b + 1], coords[2 * e + 1], r, s);
+    double ex[4], dex[4];
+    vortex_state(x, y, t, d.P, ex);
+    vortex_state_dbeta(x, y, t, d.P, dex);
+    const size_t o = ((size_t)c * Np + i) * 4;
+    for (int k = 0; k < 4; k++) {
+      const double err = q[o + k] - ex[k];
+      acc += err * err;
+      dacc -= 2.0 * err * dex[k];
+      if (lam) lam[o + k] += 2.0 * err;
+    }
+  }
+  parts[c] = acc;
+  dparts[c] = dacc;
+}
+
+// sum over nodes of lam . dq0/dbeta for the vortex initial state, per cell.
+template <int N>
+__global__ void ic_beta_kernel(const Inst d, const double *coords, const int *cells, const double *lam,
+                               double *parts) {
+  constexpr int Np = np_of(N);
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= d.K) return;
+  const int a = cells[3 * c], b = cells[3 * c + 1], e = cells[3 * c + 2];
+  double acc = 0.0;
+  for (int i = 0; i < Np; i++) {
+    const double r = c_rs[N][i], s = c_rs[N][Np + i];
+    const double x = node_coord(coords[2 * a], coords[2 * b], coords[2 * e], r, s);
+    const double y = node_coord(coords[2 * a + 1], coords[2 * b + 1], coords[2 * e + 1], r, s);
+    double dq[4];
+    vortex_state_dbeta(x, y, 0.0, d.P, dq);
+    const double *l = lam + ((size_t)c * Np + i) * 4;
+    acc += l[0] * dq[0] + l[1] * dq[1] + l[2] * dq[2] + l[3] * dq[3];
+  }
+  parts[c] = acc;
+}
+
 __global__ void set_dt_kernel(StepState *st, const double *dts) {
   if (threadIdx.x | blockIdx.x) return;
   st->dt = dts[st->step];
@@ -496,9 +584,10 @@ struct Adjoint {
   }
 
   int create(const Config &c, const Mesh &m, int nsteps_, int navg_, int C_, std::string &err) {
-    if (c.app != 0) { err = "the adjoint supports the airfoil boundary types"; return -1; }
-    for (int t : m.bedge_type)
-      if (t == 3) { err = "the adjoint supports boundary types 0, 1, 2 (no characteristic farfield)"; return -1; }
+    if (c.app != 0 && c.app != 1) { err = "app must be 0 (airfoil) or 1 (vortex)"; return -1; }
+    if (c.app == 0)
+      for (int t : m.bedge_type)
+        if (t == 3) { err = "the adjoint supports boundary types 0, 1, 2 (no characteristic farfield)"; return -1; }
     if (nsteps_ < 1 || navg_ < 1 || navg_ > nsteps_ || C_ < 1) { err = "bad step counts"; return -1; }
     cfg = c;
     mesh = m;
@@ -514,7 +603,7 @@ struct Adjoint {
     lam = dalloc(nq()); lW2 = dalloc(nq()); lW1 = dalloc(nq()); lnew = dalloc(nq()); wbar = dalloc(nq());
     fluxbar = dalloc(nslot()); tracebar = dalloc(nslot());
     galpha = dalloc(std::max(nbf(), fwd->K));
-    parts = dalloc(std::max(nbf(), fwd->K)); dparts = dalloc(nbf());
+    parts = dalloc(std::max(nbf(), fwd->K)); dparts = dalloc(std::max(nbf(), fwd->K));
     scal = dalloc(8);
     for (void *p : allocs)
       if (!p) { err = "cudaMalloc failed"; return -100; }
@@ -592,7 +681,29 @@ struct Adjoint {
       });
     }
     if (ce != cudaSuccess) { err = cudaGetErrorString(ce); return -100; }
-    return 0;
+    return fwd->init(err);  // a defined state (t = 0, dt) for rhs_vjp before any forward run
+  }
+
+  // Vortex objective of q at time t with the solver s's parameters: J and its explicit beta part.
+  cudaError_t vortex_objective(const Solver &s, const double *q, double t, double *lamacc, double *J_out,
+                               double *dJ_out) {
+    DG_DISPATCH(cfg.N, (vortex_obj_kernel<NN><<<(s.K + 127) / 128, 128, 0, s.stream>>>(
+                           s.d, s.coords_d, s.cells_d, q, t, parts, dparts, lamacc)));
+    det_sum_kernel<<<1, 256, 0, s.stream>>>(parts, s.K, scal + 6);
+    det_sum_kernel<<<1, 256, 0, s.stream>>>(dparts, s.K, scal + 7);
+    double h[2];
+    cudaError_t ce = cudaMemcpyAsync(h, scal + 6, 16, cudaMemcpyDeviceToHost, s.stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(s.stream);
+    if (J_out) *J_out = h[0];
+    if (dJ_out) *dJ_out = h[1];
+    return ce;
+  }
+
+  // Times at the start of each step (t_n, accumulated in the device's order: t += dt).
+  std::vector<double> step_times() const {
+    std::vector<double> t(nsteps + 1, 0.0);
+    for (int n = 0; n < nsteps; n++) t[n + 1] = t[n] + dts[n];
+    return t;
   }
 
   // C_l of the solver's current q (device), optional gradient accumulation into lam.
@@ -621,7 +732,7 @@ struct Adjoint {
   int forward(std::string &err) {
     Solver &s = *fwd;
     if (int rc = s.init(err)) return rc;
-    s.d.dt_mode = 0;
+    s.d.dt_mode = cfg.app == 1 ? cfg.dt_mode : 0;
     s.d.dt_hist = d_dts;
     s.d.dt_hist_len = (unsigned long long)nsteps + 1;
     double acc = 0.0, dacc = 0.0;
@@ -630,7 +741,7 @@ struct Adjoint {
         if (cudaMemcpyAsync(ckpt + (size_t)(n / C) * nq(), s.d.q, nq() * 8, cudaMemcpyDeviceToDevice, s.stream) !=
             cudaSuccess) { err = "checkpoint copy"; return -100; }
       s.enqueue_step(s.stream);
-      if (n + 1 > nsteps - navg) {
+      if (cfg.app == 0 && n + 1 > nsteps - navg) {
         double cl, dcl;
         if (lift(s, nullptr, 0.0, &cl, &dcl) != cudaSuccess) { err = "lift"; return -100; }
         acc += cl;
@@ -646,8 +757,15 @@ struct Adjoint {
     if (st.err & 1u) { err = "non-positive or non-finite density in the forward run"; return -200; }
     s.d.dt_hist = nullptr;
     s.d.dt_hist_len = 0;
-    J = acc / navg;
-    dJ_dalpha = dacc / navg;  // explicit part; completed in backward()
+    if (cfg.app == 1) {
+      if (vortex_objective(s, s.d.q, step_times()[nsteps], nullptr, &J, &dJ_dalpha) != cudaSuccess) {
+        err = "vortex objective";
+        return -100;
+      }
+    } else {
+      J = acc / navg;
+      dJ_dalpha = dacc / navg;  // explicit part; completed in backward()
+    }
     have_forward = true;
     return 0;
   }
@@ -670,7 +788,7 @@ struct Adjoint {
   }
 
   // G(W, v) into wbar/tracebar, then out = combination (see adj_combine_kernel).
-  void apply_G(const double *W, const double *v, double ascale, cudaStream_t st) {
+  void apply_G(const double *W, const double *v, double ascale, cudaStream_t st, double t_stage) {
     Inst d = fwd->d;
     d.W = const_cast<double *>(W);
     const AlphaSens S = sens();
@@ -678,7 +796,7 @@ struct Adjoint {
     DG_DISPATCH(cfg.N, {
       const size_t sm = (size_t)(np_of(NN) + nk_of(NN)) * 32 * 4 * sizeof(double);
       adj_elem_kernel<NN><<<(d.K + 31) / 32, dim3(32, np_of(NN)), sm, st>>>(d, v, wbar, fluxbar);
-      adj_face_kernel<NN><<<(total + 255) / 256, 256, 0, st>>>(d, fluxbar, tracebar, galpha, ascale, S);
+      adj_face_kernel<NN><<<(total + 255) / 256, 256, 0, st>>>(d, fluxbar, tracebar, galpha, ascale, S, t_stage);
     });
   }
 
@@ -698,6 +816,7 @@ struct Adjoint {
     cudaMemsetAsync(galpha, 0, (size_t)std::max(nbf(), fwd->K) * 8, st);
     double dcl_unused;
     const int nseg = (nsteps + C - 1) / C;
+    const std::vector<double> tn = step_times();
     for (int sg = nseg - 1; sg >= 0; sg--) {
       const int n0 = sg * C, n1 = std::min(nsteps, n0 + C);
       // restore the checkpoint and recompute the segment with the frozen dt sequence
@@ -705,13 +824,20 @@ struct Adjoint {
       std::memset(&s0, 0, sizeof(s0));
       s0.cfl = cfg.cfl;
       s0.step = (unsigned long long)n0;
+      s0.t = tn[n0];
       cudaMemcpyAsync(s.d.st, &s0, sizeof(s0), cudaMemcpyHostToDevice, st);
       cudaMemcpyAsync(s.d.q, ckpt + (size_t)sg * nq(), nq() * 8, cudaMemcpyDeviceToDevice, st);
       cudaMemcpyAsync(s.d.W, s.d.q, nq() * 8, cudaMemcpyDeviceToDevice, st);
       for (int n = n0; n < n1; n++) recompute_step(n, n - n0, st);
       for (int n = n1 - 1; n >= n0; n--) {
         // objective term of q_{n+1}
-        if (n + 1 > nsteps - navg) {
+        if (cfg.app == 1) {
+          if (n + 1 == nsteps) {
+            Inst dq = s.d;
+            DG_DISPATCH(cfg.N, (vortex_obj_kernel<NN><<<(s.K + 127) / 128, 128, 0, st>>>(
+                                   dq, s.coords_d, s.cells_d, s.d.q, tn[nsteps], parts, dparts, lam)));
+          }
+        } else if (n + 1 > nsteps - navg) {
           // C_l gradient needs q_{n+1}: the next slot's q, or the final state for the last step
           const double *qn1 = (n + 1 < n1) ? seg + (size_t)(3 * (n + 1 - n0)) * nq() : s.d.q;
           Inst dq = s.d;
@@ -724,19 +850,25 @@ struct Adjoint {
         }
         const double dt = dts[n];
         const double *qj = seg + (size_t)(3 * (n - n0)) * nq(), *w1 = qj + nq(), *w2 = w1 + nq();
-        apply_G(w2, lam, (2.0 / 3.0) * dt, st);
+        // stage boundary times as the forward face kernel forms them: t, t + dt, t + dt/2
+        apply_G(w2, lam, (2.0 / 3.0) * dt, st, tn[n] + 0.5 * dt);
         combine(lW2, lam, 2.0 / 3.0, nullptr, 0.0, nullptr, 0.0, (2.0 / 3.0) * dt, st);
-        apply_G(w1, lW2, 0.25 * dt, st);
+        apply_G(w1, lW2, 0.25 * dt, st, tn[n] + 1.0 * dt);
         combine(lW1, lW2, 0.25, nullptr, 0.0, nullptr, 0.0, 0.25 * dt, st);
-        apply_G(qj, lW1, dt, st);
+        apply_G(qj, lW1, dt, st, tn[n] + 0.0 * dt);
         combine(lnew, lam, 1.0 / 3.0, lW2, 0.75, lW1, 1.0, dt, st);
         std::swap(lam, lnew);
       }
     }
     (void)dcl_unused;
-    // alpha: boundary terms (galpha, per boundary face node) + initial state + explicit C_l part
-    const AlphaSens S = sens();
-    DG_DISPATCH(cfg.N, (ic_alpha_kernel<NN><<<(fwd->K + 127) / 128, 128, 0, st>>>(fwd->K, lam, S, parts)));
+    // parameter: boundary terms (galpha, per boundary face node) + initial state + explicit part
+    if (cfg.app == 1) {
+      DG_DISPATCH(cfg.N, (ic_beta_kernel<NN><<<(fwd->K + 127) / 128, 128, 0, st>>>(fwd->d, fwd->coords_d,
+                                                                                  fwd->cells_d, lam, parts)));
+    } else {
+      const AlphaSens S = sens();
+      DG_DISPATCH(cfg.N, (ic_alpha_kernel<NN><<<(fwd->K + 127) / 128, 128, 0, st>>>(fwd->K, lam, S, parts)));
+    }
     det_sum_kernel<<<1, 256, 0, st>>>(parts, fwd->K, scal + 2);
     det_sum_kernel<<<1, 256, 0, st>>>(galpha, nbf(), scal + 3);
     double h[2];
@@ -758,7 +890,9 @@ struct Adjoint {
     cudaMemcpyAsync(dW, W_host, nq() * 8, cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(dv, v_host, nq() * 8, cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(galpha, 0, (size_t)std::max(nbf(), fwd->K) * 8, st);
-    apply_G(dW, dv, 1.0, st);
+    StepState cur;
+    if (fwd->state(cur, err)) return -100;
+    apply_G(dW, dv, 1.0, st, cur.t + 0.5 * cur.dt);  // the boundary time of Solver::rhs
     cudaMemsetAsync(lW1, 0, nq() * 8, st);
     combine(lnew, lW1, 0.0, nullptr, 0.0, nullptr, 0.0, 1.0, st);
     det_sum_kernel<<<1, 256, 0, st>>>(galpha, nbf(), scal + 5);
@@ -770,12 +904,14 @@ struct Adjoint {
     return 0;
   }
 
-  // J for a given alpha and initial state (host q0, or the freestream if null), with the dt
-  // sequence of the recording run: the function whose derivatives backward() returns.
+  // J for a given parameter (alpha in degrees, or beta for the vortex) and initial state (host
+  // q0, or the app's initial state if null), with the dt sequence of the recording run: the
+  // function whose derivatives backward() returns.
   int evaluate(double alpha_deg, const double *q0_host, double *J_out, std::string &err) {
     if (!have_forward) { err = "call forward first"; return -1; }
     Config c2 = cfg;
-    c2.alpha_deg = alpha_deg;
+    if (cfg.app == 1) c2.vortex_beta = alpha_deg;
+    else c2.alpha_deg = alpha_deg;
     c2.dt_mode = 1;
     Solver s;
     if (int rc = s.create(c2, mesh, err)) return rc;
@@ -791,7 +927,7 @@ struct Adjoint {
     for (int n = 0; n < nsteps; n++) {
       set_dt_kernel<<<1, 32, 0, s.stream>>>(s.d.st, d_dts);
       s.enqueue_step(s.stream);
-      if (n + 1 > nsteps - navg) {
+      if (cfg.app == 0 && n + 1 > nsteps - navg) {
         double elx, ely, delx, dely, iq;
         tmp.lift_dirs(elx, ely, delx, dely, iq);
         const int nb = s.d.nB * (cfg.N + 1);
@@ -808,6 +944,12 @@ struct Adjoint {
     }
     cudaError_t ce = cudaStreamSynchronize(s.stream);
     if (ce == cudaSuccess) ce = cudaGetLastError();
+    if (ce == cudaSuccess && cfg.app == 1) {
+      // s carries this evaluation's beta; the scratch (parts, scal) is this instance's
+      ce = vortex_objective(s, s.d.q, step_times()[nsteps], nullptr, J_out, nullptr);
+      if (ce != cudaSuccess) { err = cudaGetErrorString(ce); return -100; }
+      return 0;
+    }
     if (ce != cudaSuccess) { err = cudaGetErrorString(ce); return -100; }
     *J_out = acc / navg;
     return 0;
@@ -837,6 +979,8 @@ struct LiftObjective {
 }  // namespace dg
 
 // ---------------------------------------------------------------- adjoint C ABI
+#include <thread>
+
 #include "dg_handles.h"
 struct dg_adjoint_t {
   dg::LiftObjective::Context ctx;
@@ -860,8 +1004,9 @@ extern "C" int dg_adjoint_create(const dg_config_t *c, const dg_mesh_t *mesh, in
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return adj_fail(DG_ERR_CUDA, "no CUDA device");
   dg::Config cfg;
-  cfg.N = c->N; cfg.app = c->app; cfg.dt_mode = 0; cfg.cfl = c->cfl; cfg.gam = c->gam; cfg.mach = c->mach;
-  cfg.alpha_deg = c->alpha_deg; cfg.p_inf = c->p_inf; cfg.rho_inf = c->rho_inf;
+  cfg.N = c->N; cfg.app = c->app; cfg.dt_mode = c->app == 1 ? c->dt_mode : 0; cfg.cfl = c->cfl; cfg.gam = c->gam;
+  cfg.mach = c->mach; cfg.alpha_deg = c->alpha_deg; cfg.p_inf = c->p_inf; cfg.rho_inf = c->rho_inf;
+  cfg.vortex_x0 = c->vortex_x0; cfg.vortex_y0 = c->vortex_y0; cfg.vortex_beta = c->vortex_beta;
   auto *h = new (std::nothrow) dg_adjoint_t();
   if (!h) return adj_fail(DG_ERR_ARG, "out of host memory");
   std::string err;
@@ -888,6 +1033,51 @@ extern "C" int dg_adjoint_backward(dg_adjoint_t *h, double grad_J, double *grad_
   if (int rc = dg::LiftObjective::backward(h->ctx, grad_J, grad_alpha, grad_q0, err))
     return adj_fail(rc <= -100 ? DG_ERR_CUDA : DG_ERR_ARG, err);
   return 0;
+}
+
+// Runs job(i) for every instance in its own host thread on the caller's device; returns the
+// first failing instance's code and message.
+template <class F>
+static int adj_for_each(int n, F job) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return adj_fail(DG_ERR_CUDA, "no current device");
+  std::vector<int> rc(n, 0);
+  std::vector<std::string> errs(n);
+  std::vector<std::thread> th;
+  th.reserve(n);
+  for (int i = 0; i < n; i++)
+    th.emplace_back([&, i] {
+      if (cudaSetDevice(dev) != cudaSuccess) {
+        rc[i] = -100;
+        errs[i] = "cudaSetDevice";
+        return;
+      }
+      rc[i] = job(i, errs[i]);
+    });
+  for (auto &t : th) t.join();
+  for (int i = 0; i < n; i++)
+    if (rc[i]) {
+      const int code = rc[i] == -200 ? DG_ERR_NONPHYSICAL : rc[i] <= -100 ? DG_ERR_CUDA : DG_ERR_ARG;
+      return adj_fail(code, "instance " + std::to_string(i) + ": " + errs[i]);
+    }
+  return 0;
+}
+
+extern "C" int dg_adjoint_batch_forward(dg_adjoint_t *const *hs, int n, double *J) {
+  if (!hs || n < 1 || !J) return adj_fail(DG_ERR_ARG, "bad arguments");
+  for (int i = 0; i < n; i++)
+    if (!hs[i]) return adj_fail(DG_ERR_ARG, "null instance");
+  return adj_for_each(n, [&](int i, std::string &err) { return dg::LiftObjective::forward(hs[i]->ctx, err, &J[i]); });
+}
+
+extern "C" int dg_adjoint_batch_backward(dg_adjoint_t *const *hs, int n, double grad_J, double *grad_param,
+                                         double *const *grad_q0) {
+  if (!hs || n < 1 || !grad_param) return adj_fail(DG_ERR_ARG, "bad arguments");
+  for (int i = 0; i < n; i++)
+    if (!hs[i]) return adj_fail(DG_ERR_ARG, "null instance");
+  return adj_for_each(n, [&](int i, std::string &err) {
+    return dg::LiftObjective::backward(hs[i]->ctx, grad_J, &grad_param[i], grad_q0 ? grad_q0[i] : nullptr, err);
+  });
 }
 
 extern "C" int dg_adjoint_evaluate(dg_adjoint_t *h, double alpha_deg, const double *q0, double *J) {

@@ -204,6 +204,44 @@ def batched_measure(pkg, steps, n_inst=64, seed=20261203):
             "speedup_vs_plain": pms / bms}
 
 
+def batched_small_measure(pkg, steps=100, n_inst=64, seed=20261203):
+    """Where batching pays: 64 small instances (O-grids 32x8 .. 64x16, K 512 .. 2048, N=3/4,
+    the sweep's alpha and Mach), launch-bound on the plain path (7 launches per instance-step)."""
+    sc = pkg.sweep_config(n_inst, seed)
+    meshes, cfgs = [], []
+    for i, c in enumerate(sc):
+        f = i / (n_inst - 1)
+        meshes.append(pkg.Mesh.naca_ogrid(int(round(32 + 32 * f)), int(round(8 + 8 * f))))
+        cfgs.append(pkg.config(N=c["N"], cfl=CFL, mach=c["mach"], alpha_deg=c["alpha_deg"]))
+    dof = sum(m.size("cells") * np_of(c.N) * 4 for m, c in zip(meshes, cfgs))
+    b = pkg.Batch(meshes, cfgs).init()
+    b.autotune(3)
+    b.run(3)
+    b.sync()
+    e0, e1 = pkg.Event(), pkg.Event()
+    e0.record(b.stream)
+    b.run(steps)
+    e1.record(b.stream)
+    b.sync()
+    bms = e0.elapsed_ms(e1) / steps
+    solvers = [pkg.Solver(m, c).init() for m, c in zip(meshes, cfgs)]
+    for s_ in solvers:
+        s_.run(2)
+    for s_ in solvers:
+        s_.sync()
+    t0 = time.perf_counter()
+    for s_ in solvers:
+        s_.run(steps)
+    for s_ in solvers:
+        s_.sync()
+    pms = (time.perf_counter() - t0) / steps * 1e3
+    return {"value": 3 * dof / (bms * 1e-3), "unit": "DOF-stage/s", "ms_per_step": bms, "instances": n_inst,
+            "cells": sum(m.size("cells") for m in meshes), "shape": b.shape(),
+            "plain_same_instances": {"value": 3 * dof / (pms * 1e-3), "ms_per_step": pms,
+                                     "how": "64 plain solvers, graph launches on their own streams, host-timed"},
+            "speedup_vs_plain": pms / bms}
+
+
 def adjoint_measure(pkg, nsteps=2000, navg=100, C=50):
     """The adjoint case: NACA 0012 O-grid 256x64 (K=32768), N=3, M=0.5, alpha=2 deg, inflow /
     outflow farfield typing (the adjoint covers boundary types 0-2), J = mean C_l over the last
@@ -292,6 +330,57 @@ def mesh_setup_measure(pkg, n=1024):
             "note": "device_call_ms includes host<->device copies and host validation"}
 
 
+def large_vortex_measure(pkg, n=512, orders=(1, 2, 3, 4, 5), steps=200, n_inst=16, grad_order=2, C=14,
+                         seed=20261203):
+    """Large vortex convergence plus batched gradient: [-5,5]^2 cut into 2 n^2 = 524288 triangles,
+    the vortex (beta 5 at the origin, dt = 0.5/dt1 frozen) run 200 steps at each order N=1..5 with
+    its L2 error against the analytic state; then 16 instances with beta ~ U[3,7] (numpy seed
+    20261203), the gradient of each instance's final-time squared error with respect to beta in one
+    batched forward and one batched backward (order 2, checkpoints every 14 steps), and a central
+    difference check (h = 1e-6) of the first instance."""
+    mesh = pkg.Mesh.vortex_square(n)
+    conv = []
+    for N in orders:
+        cfg = pkg.config(N=N, app=pkg.APP_VORTEX, dt_mode=pkg.DT_FROZEN, cfl=CFL, vortex_x0=0.0, vortex_y0=0.0,
+                         vortex_beta=5.0)
+        s = pkg.Solver(mesh, cfg).init()
+        s.run(1)
+        s.sync()
+        s = pkg.Solver(mesh, cfg).init()
+        a, b = pkg.Event(), pkg.Event()
+        a.record(s.stream)
+        s.run(steps)
+        b.record(s.stream)
+        s.sync()
+        ms = a.elapsed_ms(b)
+        t, dt, _ = s.time()
+        err = s.l2_error()
+        dofs = mesh.size("cells") * np_of(N) * 4
+        conv.append({"N": N, "dt": dt, "t_end": t, "l2_error_sums": [float(x) for x in err],
+                     "rms_error": float(np.sqrt(err.sum() / dofs)), "ms": ms,
+                     "dof_stage_per_s": 3 * dofs * steps / (ms * 1e-3)})
+    betas = np.random.default_rng(seed).uniform(3.0, 7.0, n_inst)
+    objs = [pkg.LiftObjective(mesh, pkg.config(N=grad_order, app=pkg.APP_VORTEX, dt_mode=pkg.DT_FROZEN, cfl=CFL,
+                                               vortex_x0=0.0, vortex_y0=0.0, vortex_beta=float(bb)), steps, 1, C)
+            for bb in betas]
+    t0 = time.perf_counter()
+    J = pkg.adjoint_batch_forward(objs)
+    fwd_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    g, _ = pkg.adjoint_batch_backward(objs)
+    bwd_s = time.perf_counter() - t0
+    h = 1e-6
+    fd = (objs[0].evaluate(betas[0] + h) - objs[0].evaluate(betas[0] - h)) / (2 * h)
+    del objs
+    return {"cells": mesh.size("cells"), "steps": steps, "convergence": conv,
+            "batched_gradient": {"instances": n_inst, "order": grad_order, "checkpoint_every": C,
+                                 "beta": [float(x) for x in betas], "J": [float(x) for x in J],
+                                 "dJ_dbeta": [float(x) for x in g], "forward_s": fwd_s, "backward_s": bwd_s,
+                                 "backward_over_forward": bwd_s / fwd_s,
+                                 "fd_check_instance0": {"fd": fd, "adjoint": float(g[0]),
+                                                        "rel_diff": abs(g[0] - fd) / max(abs(fd), 1e-300)}}}
+
+
 def run_reference(args):
     """The reference arm: the reference's user kernels (restated; the reference's own build is
     N=4-only and cannot run this N=3 workload) on all host cores."""
@@ -339,6 +428,8 @@ def main():
     ap.add_argument("--batched-steps", type=int, default=20)
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-advection", action="store_true")
+    ap.add_argument("--large-vortex", action="store_true",
+                    help="also run the large vortex convergence + 16-instance batched beta gradient (~1 min)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -469,11 +560,14 @@ def main():
                                 "sample": "%d SSPRK3 steps of the full workload (%.1f s)" % (args.cpu_steps, secs)}
     if not args.no_batched:
         line["batched"] = batched_measure(pkg, args.batched_steps)
+        line["batched"]["small_instances"] = batched_small_measure(pkg)
     if not args.no_adjoint:
         line["adjoint"] = adjoint_measure(pkg)
     if not args.no_advection:
         line["advection"] = advection_measure(pkg)
         line["mesh_setup"] = mesh_setup_measure(pkg)
+    if args.large_vortex:
+        line["large_vortex"] = large_vortex_measure(pkg)
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:

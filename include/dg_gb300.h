@@ -179,7 +179,13 @@ int dg_sweep_config(int n, unsigned long long seed, int *n_theta, int *n_r, int 
  * recomputation from the checkpoints) and returns grad_J * dJ/dalpha (alpha in degrees) and
  * grad_J * dJ/dq0 ([K][Np][4], may be NULL), with the dt sequence frozen.
  * dg_adjoint_evaluate gives J for another alpha / initial state with that frozen sequence (the
- * function backward differentiates), for finite-difference checks. */
+ * function backward differentiates), for finite-difference checks.
+ *
+ * Isentropic vortex (cfg->app = 1; navg unused but must be in 1..nsteps): J is the final-time sum
+ * over nodes and variables of the squared error against the analytic vortex (the four sums of
+ * vortex/src/l2_error.h:3-29 added) and the scalar parameter is the vortex strength beta: the
+ * grad_alpha / alpha_deg / alpha_part arguments then carry dJ/dbeta, beta and v . dL/dbeta.
+ * The dt sequence (cfg->dt_mode 1: frozen at the initial state's value) is held fixed. */
 typedef struct dg_adjoint_t dg_adjoint_t;
 int dg_adjoint_create(const dg_config_t *cfg, const dg_mesh_t *mesh, int nsteps, int navg, int checkpoint_every,
                       dg_adjoint_t **out);
@@ -189,6 +195,11 @@ int dg_adjoint_evaluate(dg_adjoint_t *a, double alpha_deg, const double *q0, dou
 int dg_adjoint_dt_sequence(dg_adjoint_t *a, double *out, int n);
 /* (dL/dW at W)^T v and v . dL/dalpha of one right-hand side (host arrays [K][Np][4]). */
 int dg_adjoint_rhs_vjp(dg_adjoint_t *a, const double *W, const double *v, double *out, double *alpha_part);
+/* Many instances at once (for example 16 vortex strengths on one mesh): every instance's
+ * forward, or backward, runs concurrently on its own stream from its own host thread; one call
+ * returns all J / all gradients (grad_q0 may be NULL, else n pointers, each may be NULL). */
+int dg_adjoint_batch_forward(dg_adjoint_t *const *a, int n, double *J);
+int dg_adjoint_batch_backward(dg_adjoint_t *const *a, int n, double grad_J, double *grad_param, double *const *grad_q0);
 void *dg_adjoint_stream(dg_adjoint_t *a);
 void dg_adjoint_free(dg_adjoint_t *a);
 const char *dg_adjoint_last_error(void);

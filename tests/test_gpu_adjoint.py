@@ -81,3 +81,64 @@ def test_rejects_characteristic_farfield(pkg):
     mesh = pkg.Mesh.naca_ogrid(32, 8, farfield="characteristic")
     with pytest.raises(pkg.DGError):
         pkg.LiftObjective(mesh, pkg.config(N=3), 10, 5)
+
+
+# ---------------------------------------------------------------- isentropic vortex: d/d beta
+def vortex_setup(pkg, N=2, n=16, nsteps=40, C=7, beta=5.0):
+    mesh = pkg.Mesh.vortex_square(n)
+    cfg = pkg.config(N=N, app=pkg.APP_VORTEX, dt_mode=pkg.DT_FROZEN, cfl=0.5, vortex_x0=0.0,
+                     vortex_y0=0.0, vortex_beta=beta)
+    return mesh, cfg, pkg.LiftObjective(mesh, cfg, nsteps, 1, C)
+
+
+@pytest.mark.parametrize("N", [1, 2, 3])
+def test_vortex_rhs_vjp_dot_product(pkg, N):
+    mesh, cfg, obj = vortex_setup(pkg, N=N)
+    s = pkg.Solver(mesh, cfg).init()
+    rng = np.random.default_rng(10 + N)
+    q = s.get("q")
+    W = q * (1.0 + 0.05 * rng.standard_normal(q.size))
+    u = q * rng.standard_normal(q.size)
+    v = rng.standard_normal(q.size)
+    h = 1e-6
+    jvp = (s.rhs(W + h * u) - s.rhs(W - h * u)) / (2 * h)
+    vjp, _ = obj.rhs_vjp(W, v)
+    lhs, rhs = np.dot(v, jvp), np.dot(vjp, u)
+    assert abs(lhs - rhs) <= 1e-7 * max(abs(lhs), abs(rhs))
+
+
+def test_vortex_beta_gradient_matches_finite_differences(pkg):
+    mesh, cfg, obj = vortex_setup(pkg)
+    J = obj.forward()
+    gb, gq = obj.backward()
+    assert obj.evaluate(cfg.vortex_beta) == J
+    h = 1e-6
+    fd = (obj.evaluate(cfg.vortex_beta + h) - obj.evaluate(cfg.vortex_beta - h)) / (2 * h)
+    assert abs(gb - fd) <= 1e-7 * max(abs(fd), 1e-30), (gb, fd)
+    q0 = pkg.Solver(mesh, cfg).init().get("q")
+    delta = q0 * np.random.default_rng(6).standard_normal(q0.size) * 1e-2
+    fdq = (obj.evaluate(cfg.vortex_beta, q0 + h * delta) - obj.evaluate(cfg.vortex_beta, q0 - h * delta)) / (2 * h)
+    assert abs(np.dot(gq, delta) - fdq) <= 1e-7 * max(abs(fdq), 1e-30)
+
+
+def test_vortex_checkpoint_interval_invariance(pkg):
+    res = []
+    for C in (1, 6, 40):
+        _, _, obj = vortex_setup(pkg, C=C)
+        J = obj.forward()
+        res.append((J,) + obj.backward())
+    for J, gb, gq in res[1:]:
+        assert J == res[0][0] and gb == res[0][1] and np.array_equal(gq, res[0][2])
+
+
+def test_vortex_batched_gradient_equals_individual(pkg):
+    """Instances with different beta, forward and backward in one batched call each."""
+    betas = (3.0, 4.0, 5.0)   # stronger vortices are under-resolved on this small mesh
+    objs = [vortex_setup(pkg, beta=b)[2] for b in betas]
+    J = pkg.adjoint_batch_forward(objs)
+    g, gq = pkg.adjoint_batch_backward(objs, want_q0=True)
+    for k, b in enumerate(betas):
+        ref = vortex_setup(pkg, beta=b)[2]
+        assert ref.forward() == J[k]
+        gb, gqk = ref.backward()
+        assert gb == g[k] and np.array_equal(gqk, gq[k])
