@@ -141,6 +141,7 @@ def lib():
         "dg_adjoint_dt_sequence": (C.c_int, [vp, dp, C.c_int]),
         "dg_adjoint_rhs_vjp": (C.c_int, [vp, dp, dp, dp, dp]),
         "dg_adjoint_stream": (vp, [vp]),
+        "dg_adjoint_tangent": (C.c_int, [vp, C.c_double, dp, dp]),
         "dg_adjoint_batch_forward": (C.c_int, [C.POINTER(vp), C.c_int, dp]),
         "dg_adjoint_batch_backward": (C.c_int, [C.POINTER(vp), C.c_int, C.c_double, dp, C.POINTER(dp)]),
         "dg_adjoint_free": (None, [vp]),
@@ -469,6 +470,13 @@ class LiftObjective:
         q = None if q0 is None else _f64(q0).ravel()
         self._check(lib().dg_adjoint_evaluate(self.h, alpha_deg, _dp(q) if q is not None else None, C.byref(J)))
         return J.value
+
+    def tangent(self, d_param, dq0=None):
+        """Tangent-linear run: dJ along (d_param, dq0), independent of the reverse kernels."""
+        dJ = C.c_double()
+        q = None if dq0 is None else _f64(dq0).ravel()
+        self._check(lib().dg_adjoint_tangent(self.h, d_param, _dp(q) if q is not None else None, C.byref(dJ)))
+        return dJ.value
 
     def dt_sequence(self):
         out = np.empty(self.nsteps)

@@ -604,7 +604,7 @@ struct Adjoint {
     fluxbar = dalloc(nslot()); tracebar = dalloc(nslot());
     galpha = dalloc(std::max(nbf(), fwd->K));
     parts = dalloc(std::max(nbf(), fwd->K)); dparts = dalloc(std::max(nbf(), fwd->K));
-    scal = dalloc(8);
+    scal = dalloc(16);
     for (void *p : allocs)
       if (!p) { err = "cudaMalloc failed"; return -100; }
     // per-order tables: face quadrature weights and node -> face points

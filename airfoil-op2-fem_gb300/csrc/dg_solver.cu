@@ -1211,6 +1211,7 @@ extern "C" int dg_rhs_noalloc(const dg_config_t *cfg, int n_cells, int n_edges, 
 
 #include "dg_batch.cuh"
 #include "dg_adjoint.cuh"
+#include "dg_tangent.cuh"
 #include "dg_advec.cuh"
 
 // ---------------------------------------------------------------- batched C ABI

@@ -259,8 +259,13 @@ def adjoint_measure(pkg, nsteps=2000, navg=100, C=50):
     fwd_ms, bwd_ms = a.elapsed_ms(b), b.elapsed_ms(c)
     h = 1e-6
     fd = (obj.evaluate(2.0 + h) - obj.evaluate(2.0 - h)) / (2 * h)
+    t0 = time.perf_counter()
+    tan = obj.tangent(1.0)
+    tan_s = time.perf_counter() - t0
     return {"J_mean_cl": J, "dJ_dalpha_deg": ga, "fd_dJ_dalpha_deg": fd,
-            "fd_rel_diff": abs(ga - fd) / max(abs(fd), 1e-300), "forward_ms": fwd_ms, "backward_ms": bwd_ms,
+            "fd_rel_diff": abs(ga - fd) / max(abs(fd), 1e-300),
+            "tangent_dJ_dalpha_deg": tan, "tangent_rel_diff": abs(ga - tan) / max(abs(tan), 1e-300),
+            "tangent_s": tan_s, "forward_ms": fwd_ms, "backward_ms": bwd_ms,
             "adjoint_over_forward": bwd_ms / fwd_ms, "steps": nsteps, "avg_last": navg,
             "checkpoint_every": C, "cells": mesh.size("cells"), "order": N_ORDER,
             "note": "backward = segment recomputation from checkpoints + reverse sweep"}

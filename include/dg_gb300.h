@@ -193,6 +193,10 @@ int dg_adjoint_forward(dg_adjoint_t *a, double *J);
 int dg_adjoint_backward(dg_adjoint_t *a, double grad_J, double *grad_alpha, double *grad_q0);
 int dg_adjoint_evaluate(dg_adjoint_t *a, double alpha_deg, const double *q0, double *J);
 int dg_adjoint_dt_sequence(dg_adjoint_t *a, double *out, int n);
+/* Tangent-linear FP64 run (forward mode, independent of the reverse kernels), after
+ * dg_adjoint_forward: dJ = dJ/dparam * d_param + dJ/dq0 . dq0 (dq0 [K][Np][4] or NULL) along the
+ * same frozen dt sequence; equals the adjoint's gradient applied to that direction. */
+int dg_adjoint_tangent(dg_adjoint_t *a, double d_param, const double *dq0, double *dJ);
 /* (dL/dW at W)^T v and v . dL/dalpha of one right-hand side (host arrays [K][Np][4]). */
 int dg_adjoint_rhs_vjp(dg_adjoint_t *a, const double *W, const double *v, double *out, double *alpha_part);
 /* Many instances at once (for example 16 vortex strengths on one mesh): every instance's

@@ -142,3 +142,33 @@ def test_vortex_batched_gradient_equals_individual(pkg):
         assert ref.forward() == J[k]
         gb, gqk = ref.backward()
         assert gb == g[k] and np.array_equal(gqk, gq[k])
+
+
+# ---------------------------------------------------------------- tangent-linear FP64 run
+def test_tangent_linear_matches_adjoint(pkg):
+    """Forward-mode derivative (dual numbers through the forward formulas, hand-written ghost
+    state and stage tangents) against the reverse-mode gradient: the same discrete derivative
+    by two independent routes."""
+    mesh, cfg, obj = setup(pkg)
+    obj.forward()
+    ga, gq = obj.backward()
+    ta = obj.tangent(1.0)
+    assert abs(ta - ga) <= 1e-10 * abs(ga), (ta, ga)
+    q0 = pkg.Solver(mesh, cfg).init().get("q")
+    delta = q0 * np.random.default_rng(8).standard_normal(q0.size) * 1e-2
+    tq = obj.tangent(0.0, delta)
+    assert abs(tq - np.dot(gq, delta)) <= 1e-10 * abs(tq), (tq, np.dot(gq, delta))
+    both = obj.tangent(0.5, delta)
+    assert abs(both - (0.5 * ta + tq)) <= 1e-12 * abs(both)
+
+
+def test_vortex_tangent_linear_matches_adjoint(pkg):
+    mesh, cfg, obj = vortex_setup(pkg)
+    obj.forward()
+    gb, gq = obj.backward()
+    tb = obj.tangent(1.0)
+    assert abs(tb - gb) <= 1e-10 * abs(gb), (tb, gb)
+    q0 = pkg.Solver(mesh, cfg).init().get("q")
+    delta = q0 * np.random.default_rng(9).standard_normal(q0.size) * 1e-2
+    tq = obj.tangent(0.0, delta)
+    assert abs(tq - np.dot(gq, delta)) <= 1e-10 * abs(tq)
