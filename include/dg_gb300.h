@@ -246,6 +246,8 @@ int dg_kernels_per_step(void);
 /* Element-kernel form for launches and graphs built from now on: 1 even/odd split of
  * [Drw | Dsw | -LIFT] (default), 0 dense rows.  Both compute the same right-hand side. */
 void dg_set_elem_variant(int variant);
+/* Threads per face-kernel block of the plain path (32..256, multiple of 32; default 64). */
+void dg_set_face_block(int threads);
 
 #ifdef __cplusplus
 }
