@@ -433,6 +433,7 @@ def main():
     ap.add_argument("--batched-steps", type=int, default=20)
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-advection", action="store_true")
+    ap.add_argument("--advection-steps", type=int, default=200)
     ap.add_argument("--large-vortex", action="store_true",
                     help="also run the large vortex convergence + 16-instance batched beta gradient (~1 min)")
     args = ap.parse_args()
@@ -569,7 +570,7 @@ def main():
     if not args.no_adjoint:
         line["adjoint"] = adjoint_measure(pkg)
     if not args.no_advection:
-        line["advection"] = advection_measure(pkg)
+        line["advection"] = advection_measure(pkg, steps=args.advection_steps)
         line["mesh_setup"] = mesh_setup_measure(pkg)
     if args.large_vortex:
         line["large_vortex"] = large_vortex_measure(pkg)
