@@ -46,6 +46,7 @@ struct Consts {
   const double *r, *s, *Dr, *Ds, *Drw, *Dsw, *LIFT, *ones;
   const int *FMASK;
   double gam, bc_r, bc_u, bc_v, bc_e;
+  double vortex_x0, vortex_y0, vortex_beta;  // the vortex app's constants (vortex.cpp op_decl_const)
 };
 
 struct LoopStat {
@@ -177,6 +178,85 @@ __global__ void k_set_ic(long long n_nodes, double *q, double *W, const Consts C
   }
 }
 
+// The analytic vortex of vortex/src/set_ic.h:6-21 (also get_bedge_q.h, l2_error.h), in their
+// operation order.
+__device__ void vortex_ref(double x, double y, double t, const Consts &C, double &rho, double &u, double &v,
+                           double &ener) {
+  const double gam = C.gam, x0 = C.vortex_x0, y0 = C.vortex_y0, beta = C.vortex_beta;
+  double r = (x - t - x0) * (x - t - x0) + (y - y0) * (y - y0);
+  r = sqrt(r);
+  u = 1.0 - beta * exp(1.0 - r * r) * ((y - y0) / (2 * M_PI));
+  v = beta * exp(1.0 - r * r) * ((x - x0) / (2 * M_PI));
+  rho = 1.0 - ((gam - 1) / (16 * gam * M_PI * M_PI)) * beta * beta * exp(2 * (1.0 - r * r));
+  rho = pow(rho, 1.0 / (gam - 1));
+  const double p = pow(rho, gam);
+  ener = (p / (gam - 1)) + 0.5 * rho * (u * u + v * v);
+}
+
+// vortex/src/set_ic.h:3-28, one thread per node
+__global__ void k_set_ic_vortex(long long n_nodes, double t, const double *x, const double *y, double *q, double *W,
+                                const Consts C) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n_nodes) return;
+  double rho, u, v, ener;
+  vortex_ref(x[i], y[i], t, C, rho, u, v, ener);
+  const double val[4] = {rho, rho * u, rho * v, ener};
+  for (int k = 0; k < 4; k++) {
+    q[4 * i + k] = val[k];
+    W[4 * i + k] = val[k];
+  }
+}
+
+// vortex/src/get_bedge_q.h:3-40
+template <int N>
+__global__ void k_get_bedge_q_vortex(int n, const int *bnum, const int *map, int mdim, int i0, const double *xa,
+                                     const double *ya, double t, double *exQ, const Consts C) {
+  constexpr int Np = Ord<N>::Np, Nfp = Ord<N>::Nfp;
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n) return;
+  const int c = map[b * mdim + i0], f = bnum[b];
+  const double *x = xa + (size_t)Np * c, *y = ya + (size_t)Np * c;
+  double *e = exQ + (size_t)12 * Nfp * c + f * 4 * Nfp;
+  const int *fm = C.FMASK + f * Nfp;
+  for (int i = 0; i < Nfp; i++) {
+    double rho, u, v, ener;
+    vortex_ref(x[fm[i]], y[fm[i]], t, C, rho, u, v, ener);
+    atomicAdd(&e[i * 4], rho);
+    atomicAdd(&e[i * 4 + 1], rho * u);
+    atomicAdd(&e[i * 4 + 2], rho * v);
+    atomicAdd(&e[i * 4 + 3], ener);
+  }
+}
+
+// vortex/src/l2_error.h:3-29: per-cell sums (the kernel zeroes its accumulators on entry, so the
+// cell sums are what OP2's device backends reduce) and the per-node error dat.
+template <int N>
+__global__ void k_l2_error(int n, const double *xa, const double *ya, const double *qa, double t, double *part,
+                           double *err, const Consts C) {
+  constexpr int Np = Ord<N>::Np;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  const double *x = xa + (size_t)Np * c, *y = ya + (size_t)Np * c, *q = qa + (size_t)4 * Np * c;
+  double *error = err + (size_t)4 * Np * c;
+  double e0 = 0.0, e1 = 0.0, e2 = 0.0, e3 = 0.0;
+  for (int i = 0; i < Np; i++) {
+    double rho, u, v, ener;
+    vortex_ref(x[i], y[i], t, C, rho, u, v, ener);
+    e0 += (q[i * 4] - rho) * (q[i * 4] - rho);
+    e1 += (q[i * 4 + 1] - rho * u) * (q[i * 4 + 1] - rho * u);
+    e2 += (q[i * 4 + 2] - rho * v) * (q[i * 4 + 2] - rho * v);
+    e3 += (q[i * 4 + 3] - ener) * (q[i * 4 + 3] - ener);
+    error[i * 4] = (q[i * 4] - rho) * (q[i * 4] - rho);
+    error[i * 4 + 1] = (q[i * 4 + 1] - rho * u) * (q[i * 4 + 1] - rho * u);
+    error[i * 4 + 2] = (q[i * 4 + 2] - rho * v) * (q[i * 4 + 2] - rho * v);
+    error[i * 4 + 3] = (q[i * 4 + 3] - ener) * (q[i * 4 + 3] - ener);
+  }
+  part[4 * (size_t)c] = e0;
+  part[4 * (size_t)c + 1] = e1;
+  part[4 * (size_t)c + 2] = e2;
+  part[4 * (size_t)c + 3] = e3;
+}
+
 __global__ void k_zero(long long n, double *p) {
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t < n) p[t] = 0.0;
@@ -293,7 +373,8 @@ __global__ void __launch_bounds__(128) k_euler_rhs(int n, const double *Wa, doub
                                                     const double *rxa, const double *rya,
                                                     const double *sxa, const double *sya,
                                                     const double *fsa, const double *nxa,
-                                                    const double *nya, double *rhsa, const Consts C) {
+                                                    const double *nya, double *rhsa, const Consts C,
+                                                    const bool zero_ext) {
   constexpr int Np = Ord<N>::Np, Nfp = Ord<N>::Nfp;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= n) return;
@@ -365,7 +446,8 @@ __global__ void __launch_bounds__(128) k_euler_rhs(int n, const double *Wa, doub
     for (int k = 0; k < 4; k++) flux[i * 4 + k] *= fscale[i];
   }
   for (int i = 0; i < 4; i++) gemv(Np, 3 * Nfp, -1.0, C.LIFT, 3 * Nfp, &flux[i], 4, 1.0, qRHS + i, 4);
-  for (int i = 0; i < 12 * Nfp; i++) exQ[i] = 0.0;
+  if (zero_ext)  // the airfoil copy zeroes exteriorQ (OP_RW); the vortex copy reads it (OP_READ)
+    for (int i = 0; i < 12 * Nfp; i++) exQ[i] = 0.0;
 }
 
 // src/set_workingQ.h:1-12, one thread per value
@@ -423,16 +505,28 @@ double chost(const char *name, bool &ok) {
 }
 
 // Constants a loop of order N needs; fails with a message naming the first missing one.
-bool consts_for(int N, bool need_ops, Consts &c) {
+// Which scalar constants a loop reads: the airfoil freestream (bc_*), the vortex parameters, or
+// only gam (geometry, dt, RHS and update loops are shared by both apps).
+enum Need { kFreestream, kVortex, kGamOnly };
+
+bool consts_for(int N, bool need_ops, Consts &c, Need need = kGamOnly) {
   const int Np = (N + 1) * (N + 2) / 2, Nfp = N + 1;
   std::memset(&c, 0, sizeof(c));
   bool ok = true;
   c.gam = chost("gam", ok);
-  c.bc_r = chost("bc_r", ok);
-  c.bc_u = chost("bc_u", ok);
-  c.bc_v = chost("bc_v", ok);
-  c.bc_e = chost("bc_e", ok);
-  if (!ok) return fail("constants gam, bc_r, bc_u, bc_v, bc_e must be declared with op_decl_const2");
+  if (!ok) return fail("constant gam must be declared with op_decl_const2");
+  if (need == kVortex) {
+    c.vortex_x0 = chost("vortex_x0", ok);
+    c.vortex_y0 = chost("vortex_y0", ok);
+    c.vortex_beta = chost("vortex_beta", ok);
+    if (!ok) return fail("constants vortex_x0, vortex_y0, vortex_beta must be declared with op_decl_const2");
+  } else if (need == kFreestream) {
+    c.bc_r = chost("bc_r", ok);
+    c.bc_u = chost("bc_u", ok);
+    c.bc_v = chost("bc_v", ok);
+    c.bc_e = chost("bc_e", ok);
+    if (!ok) return fail("constants bc_r, bc_u, bc_v, bc_e must be declared with op_decl_const2");
+  }
   c.FMASK = cdev<int>("FMASK", 3 * Nfp);
   if (!c.FMASK) return fail("constant FMASK (3*Nfp ints) not declared");
   if (need_ops) {
@@ -702,7 +796,7 @@ void op_par_loop_set_ic(char const *name, op_set set, op_arg a0, op_arg a1) {
   if (order_from_np(dim / 4) < 0 || dim % 4) { fail("set_ic: q dim must be 4*Np"); return; }
   if (!arg_dat(a0, set, true, dim, true, "set_ic q") || !arg_dat(a1, set, true, dim, true, "set_ic workingQ")) return;
   Consts C;
-  if (!consts_for(order_from_np(dim / 4), false, C)) return;
+  if (!consts_for(order_from_np(dim / 4), false, C, kFreestream)) return;
   Timed t(name ? name : "set_ic");
   const long long n = (long long)set->size * dim / 4;
   k_set_ic<<<blocks(n, 256), 256, 0, S().stream>>>(n, dptr<double>(a0), dptr<double>(a1), C);
@@ -797,7 +891,7 @@ void op_par_loop_get_bedge_q(char const *name, op_set set, op_arg a0, op_arg a1,
     return (void)fail("get_bedge_q: indirect args must use one map column");
   if (a5.acc != OP_INC) return (void)fail("get_bedge_q: exteriorQ must be OP_INC");
   Consts C;
-  if (!consts_for(N, false, C)) return;
+  if (!consts_for(N, false, C, kFreestream)) return;
   Timed t(name ? name : "get_bedge_q");
   DISPATCH_N(N, (k_get_bedge_q<N><<<blocks(set->size, 128), 128, 0, S().stream>>>(
                     set->size, dptr<int>(a0), dptr<int>(a1), a2.map->d_data, a2.map->dim, a2.idx, dptr<double>(a2),
@@ -821,13 +915,15 @@ void op_par_loop_euler_rhs(char const *name, op_set set, op_arg a0, op_arg a1, o
       !arg_dat(a8, set, true, 3 * Nfp, true, "euler_rhs ny") || !arg_dat(a9, set, true, 4 * Np, true, "euler_rhs rk"))
     return;
   if (a9.dat == a0.dat) return (void)fail("euler_rhs: output aliases the input state");
+  if (a1.acc != OP_RW && a1.acc != OP_READ) return (void)fail("euler_rhs: exteriorQ must be OP_RW or OP_READ");
+  const bool zero_ext = a1.acc == OP_RW;  // src/airfoil.cpp:285 (OP_RW) vs vortex/src/vortex.cpp:268 (OP_READ)
   Consts C;
   if (!consts_for(N, true, C)) return;
   Timed t(name ? name : "euler_rhs");
   DISPATCH_N(N, (k_euler_rhs<N><<<blocks(set->size, 128), 128, 0, S().stream>>>(
                     set->size, dptr<double>(a0), dptr<double>(a1), dptr<double>(a2), dptr<double>(a3),
                     dptr<double>(a4), dptr<double>(a5), dptr<double>(a6), dptr<double>(a7), dptr<double>(a8),
-                    dptr<double>(a9), C)));
+                    dptr<double>(a9), C, zero_ext)));
   if (!ck(cudaGetLastError(), "euler_rhs launch")) return;
   t.done();
 }
@@ -872,6 +968,44 @@ void op_par_loop_update_Q(char const *name, op_set set, op_arg a0, op_arg a1, op
   t.done();
 }
 
+// vortex/src/vortex.cpp:308-318 (the per-cell error sums are added to the four globals, OP_INC)
+void op_par_loop_l2_error(char const *name, op_set set, op_arg a0, op_arg a1, op_arg a2, op_arg a3, op_arg a4,
+                          op_arg a5, op_arg a6, op_arg a7, op_arg a8) {
+  if (!set) { fail("l2_error: null set"); return; }
+  const int N = order_from_np(a0.dim);
+  if (N < 0) { fail("l2_error: x dim is not a triangle node count of order 1..6"); return; }
+  const int Np = a0.dim;
+  if (!arg_dat(a0, set, true, Np, true, "l2_error x") || !arg_dat(a1, set, true, Np, true, "l2_error y") ||
+      !arg_dat(a2, set, true, 4 * Np, true, "l2_error q") || !arg_gbl(a3, 1, true, "l2_error t") ||
+      !arg_gbl(a4, 1, true, "l2_error rho") || !arg_gbl(a5, 1, true, "l2_error rhou") ||
+      !arg_gbl(a6, 1, true, "l2_error rhov") || !arg_gbl(a7, 1, true, "l2_error ener") ||
+      !arg_dat(a8, set, true, 4 * Np, true, "l2_error error"))
+    return;
+  if (a4.acc != OP_INC || a5.acc != OP_INC || a6.acc != OP_INC || a7.acc != OP_INC)
+    return (void)fail("l2_error: the error sums must be OP_INC");
+  Consts C;
+  if (!consts_for(N, false, C, kVortex)) return;
+  double t;
+  std::memcpy(&t, a3.data, 8);
+  double *part = nullptr;
+  if (!ck(cudaMallocAsync((void **)&part, (size_t)set->size * 4 * 8 + 8, S().stream), "cudaMallocAsync")) return;
+  Timed tm(name ? name : "l2_error");
+  DISPATCH_N(N, (k_l2_error<N><<<blocks(set->size, 128), 128, 0, S().stream>>>(
+                    set->size, dptr<double>(a0), dptr<double>(a1), dptr<double>(a2), t, part, dptr<double>(a8), C)));
+  std::vector<double> h((size_t)set->size * 4);
+  bool good = ck(cudaGetLastError(), "l2_error launch") &&
+              ck(cudaMemcpyAsync(h.data(), part, h.size() * 8, cudaMemcpyDeviceToHost, S().stream), "cudaMemcpyAsync");
+  cudaFreeAsync(part, S().stream);
+  if (!good || !ck(cudaStreamSynchronize(S().stream), "l2_error sync")) return;
+  double *out[4] = {(double *)a4.data, (double *)a5.data, (double *)a6.data, (double *)a7.data};
+  for (int k = 0; k < 4; k++) {
+    double acc = 0.0;
+    for (int c = 0; c < set->size; c++) acc += h[4 * (size_t)c + k];
+    *out[k] += acc;
+  }
+  tm.done();
+}
+
 void op2_gb300_par_loop(char const *kernel, char const *name, op_set set, int nargs, const op_arg *a) {
   if (!kernel || (nargs && !a)) { fail("op2_gb300_par_loop: bad arguments"); return; }
   const std::string k(kernel);
@@ -884,15 +1018,21 @@ void op2_gb300_par_loop(char const *kernel, char const *name, op_set set, int na
       op_par_loop_init_grid(name, set, a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], a[8], a[9], a[10], a[11],
                             a[12], a[13], a[14], a[15], a[16], a[17]);
   } else if (k == "set_ic") {
-    if (need(2)) op_par_loop_set_ic(name, set, a[0], a[1]);
+    if (nargs == 5) op_par_loop_set_ic(name, set, a[0], a[1], a[2], a[3], a[4]);
+    else if (need(2)) op_par_loop_set_ic(name, set, a[0], a[1]);
   } else if (k == "neighbour_zero") {
     if (need(1)) op_par_loop_neighbour_zero(name, set, a[0]);
   } else if (k == "calc_dt") {
     if (need(3)) op_par_loop_calc_dt(name, set, a[0], a[1], a[2]);
   } else if (k == "get_neighbour_q") {
-    if (need(9)) op_par_loop_get_neighbour_q(name, set, a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], a[8]);
+    if (nargs == 11)
+      op_par_loop_get_neighbour_q(name, set, a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], a[8], a[9], a[10]);
+    else if (need(9)) op_par_loop_get_neighbour_q(name, set, a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], a[8]);
   } else if (k == "get_bedge_q") {
-    if (need(6)) op_par_loop_get_bedge_q(name, set, a[0], a[1], a[2], a[3], a[4], a[5]);
+    if (nargs == 9) op_par_loop_get_bedge_q(name, set, a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], a[8]);
+    else if (need(6)) op_par_loop_get_bedge_q(name, set, a[0], a[1], a[2], a[3], a[4], a[5]);
+  } else if (k == "l2_error") {
+    if (need(9)) op_par_loop_l2_error(name, set, a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], a[8]);
   } else if (k == "euler_rhs") {
     if (need(10)) op_par_loop_euler_rhs(name, set, a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], a[8], a[9]);
   } else if (k == "set_workingQ") {
@@ -905,3 +1045,67 @@ void op2_gb300_par_loop(char const *kernel, char const *name, op_set set, int na
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ vortex app loops
+// vortex/src/vortex.cpp calls set_ic, get_neighbour_q and get_bedge_q with other argument lists
+// than the airfoil app; a translated vortex driver binds these C++ overloads (the FFI reaches them
+// through op2_gb300_par_loop by argument count).
+
+// vortex/src/vortex.cpp:210-215: set_ic(t, x, y, q, workingQ)
+void op_par_loop_set_ic(char const *name, op_set set, op_arg a0, op_arg a1, op_arg a2, op_arg a3, op_arg a4) {
+  if (!set) { fail("set_ic: null set"); return; }
+  const int Np = a1.dim, N = order_from_np(Np);
+  if (N < 0) { fail("set_ic: x dim is not a triangle node count of order 1..6"); return; }
+  if (!arg_gbl(a0, 1, true, "set_ic t") || !arg_dat(a1, set, true, Np, true, "set_ic x") ||
+      !arg_dat(a2, set, true, Np, true, "set_ic y") || !arg_dat(a3, set, true, 4 * Np, true, "set_ic q") ||
+      !arg_dat(a4, set, true, 4 * Np, true, "set_ic workingQ"))
+    return;
+  Consts C;
+  if (!consts_for(N, false, C, kVortex)) return;
+  double t;
+  std::memcpy(&t, a0.data, 8);
+  Timed tm(name ? name : "set_ic");
+  const long long n = (long long)set->size * Np;
+  k_set_ic_vortex<<<blocks(n, 256), 256, 0, S().stream>>>(n, t, dptr<double>(a1), dptr<double>(a2), dptr<double>(a3),
+                                                         dptr<double>(a4), C);
+  if (!ck(cudaGetLastError(), "set_ic launch")) return;
+  tm.done();
+}
+
+// vortex/src/vortex.cpp:235-246: get_neighbour_q(edgeNum, n0, n1, nodeX L, nodeY L, nodeX R, nodeY R,
+// W L, W R, exteriorQ L, exteriorQ R); the edge's two vertex coordinates are not used by the kernel.
+void op_par_loop_get_neighbour_q(char const *name, op_set set, op_arg a0, op_arg a1, op_arg a2, op_arg a3,
+                                 op_arg a4, op_arg a5, op_arg a6, op_arg a7, op_arg a8, op_arg a9, op_arg a10) {
+  if (!set) { fail("get_neighbour_q: null set"); return; }
+  if (!arg_dat(a1, set, false, 2, true, "get_neighbour_q n0") || !arg_dat(a2, set, false, 2, true, "get_neighbour_q n1"))
+    return;
+  op_par_loop_get_neighbour_q(name, set, a0, a3, a4, a5, a6, a7, a8, a9, a10);
+}
+
+// vortex/src/vortex.cpp:249-260: get_bedge_q(bedgeNum, n0, n1, nodeX, nodeY, x, y, t, exteriorQ)
+void op_par_loop_get_bedge_q(char const *name, op_set set, op_arg a0, op_arg a1, op_arg a2, op_arg a3, op_arg a4,
+                             op_arg a5, op_arg a6, op_arg a7, op_arg a8) {
+  if (!set) { fail("get_bedge_q: null set"); return; }
+  const int Np = a5.dim, N = order_from_np(Np);
+  if (N < 0) { fail("get_bedge_q: x dim is not a triangle node count of order 1..6"); return; }
+  const int Nfp = N + 1;
+  if (!arg_dat(a0, set, true, 1, false, "get_bedge_q bedgeNum") || !arg_dat(a1, set, false, 2, true, "get_bedge_q n0") ||
+      !arg_dat(a2, set, false, 2, true, "get_bedge_q n1") || !arg_dat(a3, set, false, 3, true, "get_bedge_q nodeX") ||
+      !arg_dat(a4, set, false, 3, true, "get_bedge_q nodeY") || !arg_dat(a5, set, false, Np, true, "get_bedge_q x") ||
+      !arg_dat(a6, set, false, Np, true, "get_bedge_q y") || !arg_gbl(a7, 1, true, "get_bedge_q t") ||
+      !arg_dat(a8, set, false, 12 * Nfp, true, "get_bedge_q ext"))
+    return;
+  if (a5.map != a6.map || a5.map != a8.map || a5.idx != a6.idx || a5.idx != a8.idx)
+    return (void)fail("get_bedge_q: x, y and exteriorQ must use one map column");
+  if (a8.acc != OP_INC) return (void)fail("get_bedge_q: exteriorQ must be OP_INC");
+  Consts C;
+  if (!consts_for(N, false, C, kVortex)) return;
+  double t;
+  std::memcpy(&t, a7.data, 8);
+  Timed tm(name ? name : "get_bedge_q");
+  DISPATCH_N(N, (k_get_bedge_q_vortex<N><<<blocks(set->size, 128), 128, 0, S().stream>>>(
+                    set->size, dptr<int>(a0), a5.map->d_data, a5.map->dim, a5.idx, dptr<double>(a5), dptr<double>(a6),
+                    t, dptr<double>(a8), C)));
+  if (!ck(cudaGetLastError(), "get_bedge_q launch")) return;
+  tm.done();
+}

@@ -98,6 +98,11 @@ void op_par_loop_set_workingQ(char const *name, op_set set, op_arg a0, op_arg a1
                               op_arg a3, op_arg a4, op_arg a5);
 void op_par_loop_update_Q(char const *name, op_set set, op_arg a0, op_arg a1, op_arg a2,
                           op_arg a3, op_arg a4, op_arg a5);
+/* vortex/src/vortex.cpp:308-318: l2_error(x, y, q, t, 4 x OP_INC error sums, error dat).  The
+ * reference kernel zeroes its accumulators on entry (vortex/src/l2_error.h:6-9); here the
+ * per-cell sums are added to the globals, as a device backend's reduction does. */
+void op_par_loop_l2_error(char const *name, op_set set, op_arg a0, op_arg a1, op_arg a2, op_arg a3,
+                          op_arg a4, op_arg a5, op_arg a6, op_arg a7, op_arg a8);
 
 /* Extensions (no OP2 counterpart). */
 const char *op2_gb300_last_error(void);
@@ -115,4 +120,18 @@ void op2_gb300_par_loop(char const *kernel, char const *name, op_set set, int na
 #ifdef __cplusplus
 }
 #endif
+#ifdef __cplusplus
+/* The vortex app's loops that share a name with an airfoil loop but take other arguments
+ * (vortex/src/vortex.cpp:210-260), as C++ overloads:
+ *   set_ic(t, x, y, q, workingQ)                                    vortex/src/set_ic.h:3-28
+ *   get_neighbour_q(edgeNum, n0, n1, nodeX L, nodeY L, nodeX R, nodeY R, W L, W R, ext L, ext R)
+ *   get_bedge_q(bedgeNum, n0, n1, nodeX, nodeY, x, y, t, exteriorQ)  vortex/src/get_bedge_q.h:3-40
+ * The vortex euler_rhs is op_par_loop_euler_rhs with exteriorQ OP_READ (not zeroed). */
+void op_par_loop_set_ic(char const *name, op_set set, op_arg a0, op_arg a1, op_arg a2, op_arg a3, op_arg a4);
+void op_par_loop_get_neighbour_q(char const *name, op_set set, op_arg a0, op_arg a1, op_arg a2, op_arg a3,
+                                 op_arg a4, op_arg a5, op_arg a6, op_arg a7, op_arg a8, op_arg a9, op_arg a10);
+void op_par_loop_get_bedge_q(char const *name, op_set set, op_arg a0, op_arg a1, op_arg a2, op_arg a3, op_arg a4,
+                             op_arg a5, op_arg a6, op_arg a7, op_arg a8);
+#endif
+
 #endif

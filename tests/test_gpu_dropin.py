@@ -164,3 +164,155 @@ def test_dropin_rejects_bad_arguments(op2, oops, orc, omesh):
                               o.op_arg_gbl(np.zeros(1), 1, "double", o.OP_READ))
     # the runtime is still usable
     assert a.calc_dt() > 0.0
+
+
+class Vortex(Airfoil):
+    """vortex/src/vortex.cpp:112-318 on the drop-in: the vortex app's loops (set_ic, get_neighbour_q,
+    get_bedge_q with their vortex argument lists, exteriorQ zeroed every stage and read by
+    euler_rhs, dt = 0.1/dt1 frozen, l2_error at the end)."""
+
+    def __init__(self, op2, m, ops, phys, cfl=0.1):
+        self.op2, self.cfl = op2, cfl
+        N = int(ops["N"])
+        Np, Nfp = (N + 1) * (N + 2) // 2, N + 1
+        self.Np, self.Nfp = Np, Nfp
+        o = op2
+        o.op_init(0)
+        K = m["cell2nodes"].shape[0]
+        self.K = K
+        nodes = o.op_decl_set(m["coords"].shape[0], "nodes")
+        self.cells = cells = o.op_decl_set(K, "cells")
+        self.edges = edges = o.op_decl_set(m["edge2cells"].shape[0], "edges")
+        self.bedges = bedges = o.op_decl_set(m["bedge2cell"].shape[0], "bedges")
+        cell2nodes = o.op_decl_map(cells, nodes, 3, m["cell2nodes"], "cell2nodes")
+        self.edge2nodes = o.op_decl_map(edges, nodes, 2, m["edge2nodes"], "edge2nodes")
+        self.edge2cells = o.op_decl_map(edges, cells, 2, m["edge2cells"], "edge2cells")
+        self.bedge2nodes = o.op_decl_map(bedges, nodes, 2, m["bedge2nodes"], "bedge2nodes")
+        self.bedge2cells = o.op_decl_map(bedges, cells, 1, m["bedge2cell"], "bedge2cells")
+        self.node_coords = node_coords = o.op_decl_dat(nodes, 2, "double", m["coords"], "node_coords")
+        d = {}
+        for name, dim in (("nodeX", 3), ("nodeY", 3), ("x", Np), ("y", Np), ("xr", Np), ("yr", Np),
+                          ("xs", Np), ("ys", Np), ("rx", Np), ("ry", Np), ("sx", Np), ("sy", Np),
+                          ("nx", 3 * Nfp), ("ny", 3 * Nfp), ("fscale", 3 * Nfp), ("q", 4 * Np),
+                          ("workingQ", 4 * Np), ("rk1", 4 * Np), ("rk2", 4 * Np), ("rk3", 4 * Np),
+                          ("exteriorQ", 12 * Nfp), ("error", 4 * Np)):
+            d[name] = (o.op_decl_dat(cells, dim, "double", np.zeros(K * dim), name), dim)
+        self.d = d
+        self.edgeNum = o.op_decl_dat(edges, 2, "int", m["edgeNum"], "edgeNum")
+        self.bedgeNum = o.op_decl_dat(bedges, 1, "int", m["bedgeNum"], "bedgeNum")
+        for k in ("gam", "vortex_x0", "vortex_y0", "vortex_beta"):
+            o.op_decl_const2(k, 1, "double", phys[k])
+        o.op_decl_const2("ones", Np, "double", np.ones(Np))
+        for k in ("r", "s", "Dr", "Ds", "Drw", "Dsw", "LIFT"):
+            o.op_decl_const2(k, np.asarray(ops[k]).size, "double", np.asarray(ops[k]).ravel())
+        o.op_decl_const2("FMASK", 3 * Nfp, "int", np.asarray(ops["FMASK"], dtype=np.int32))
+        A = self.A
+        o.op_par_loop_init_grid("init_grid", cells,
+                                o.op_arg_dat(node_coords, 0, cell2nodes, 2, "double", o.OP_READ),
+                                o.op_arg_dat(node_coords, 1, cell2nodes, 2, "double", o.OP_READ),
+                                o.op_arg_dat(node_coords, 2, cell2nodes, 2, "double", o.OP_READ),
+                                *[A(n, o.OP_WRITE) for n in ("nodeX", "nodeY", "x", "y", "xr", "yr", "xs", "ys",
+                                                             "rx", "ry", "sx", "sy", "nx", "ny", "fscale")])
+        o.op_par_loop_set_ic("set_ic", cells, o.op_arg_gbl(np.zeros(1), 1, "double", o.OP_READ),
+                             A("x", o.OP_READ), A("y", o.OP_READ), A("q", o.OP_WRITE), A("workingQ", o.OP_WRITE))
+        self.dt = (1.0 / self.calc_dt()) * cfl
+        self.t = 0.0
+
+    def run(self, iters):
+        """vortex/src/vortex.cpp:226-305"""
+        o, A, e2c, b2c = self.op2, self.A, self.edge2cells, self.bedge2cells
+        nc = self.node_coords
+        rk_t_frac = (0.0, 1.0, 0.5)
+        for _ in range(iters):
+            dt = np.array([self.dt])
+            for j in range(3):
+                o.op_par_loop_neighbour_zero("neighbour_zero", self.cells, A("exteriorQ", o.OP_WRITE))
+                o.op_par_loop_get_neighbour_q(
+                    "get_neighbour_q", self.edges, o.op_arg_dat(self.edgeNum, -1, None, 2, "int", o.OP_READ),
+                    o.op_arg_dat(nc, 0, self.edge2nodes, 2, "double", o.OP_READ),
+                    o.op_arg_dat(nc, 1, self.edge2nodes, 2, "double", o.OP_READ),
+                    A("nodeX", o.OP_READ, 0, e2c), A("nodeY", o.OP_READ, 0, e2c),
+                    A("nodeX", o.OP_READ, 1, e2c), A("nodeY", o.OP_READ, 1, e2c),
+                    A("workingQ", o.OP_READ, 0, e2c), A("workingQ", o.OP_READ, 1, e2c),
+                    A("exteriorQ", o.OP_INC, 0, e2c), A("exteriorQ", o.OP_INC, 1, e2c))
+                t1 = np.array([self.t + rk_t_frac[j] * self.dt])
+                o.op_par_loop_get_bedge_q(
+                    "get_bedge_q", self.bedges, o.op_arg_dat(self.bedgeNum, -1, None, 1, "int", o.OP_READ),
+                    o.op_arg_dat(nc, 0, self.bedge2nodes, 2, "double", o.OP_READ),
+                    o.op_arg_dat(nc, 1, self.bedge2nodes, 2, "double", o.OP_READ),
+                    A("nodeX", o.OP_READ, 0, b2c), A("nodeY", o.OP_READ, 0, b2c),
+                    A("x", o.OP_READ, 0, b2c), A("y", o.OP_READ, 0, b2c),
+                    o.op_arg_gbl(t1, 1, "double", o.OP_READ), A("exteriorQ", o.OP_INC, 0, b2c))
+                o.op_par_loop_euler_rhs(
+                    "euler_rhs", self.cells, A("workingQ", o.OP_READ), A("exteriorQ", o.OP_READ),
+                    A("rx", o.OP_READ), A("ry", o.OP_READ), A("sx", o.OP_READ), A("sy", o.OP_READ),
+                    A("fscale", o.OP_READ), A("nx", o.OP_READ), A("ny", o.OP_READ), A("rk%d" % (j + 1), o.OP_WRITE))
+                if j != 2:
+                    o.op_par_loop_set_workingQ(
+                        "set_workingQ", self.cells, o.op_arg_gbl(dt, 1, "double", o.OP_READ),
+                        o.op_arg_gbl(np.array([j], dtype=np.int32), 1, "int", o.OP_READ),
+                        A("q", o.OP_READ), A("rk1", o.OP_READ), A("rk2", o.OP_READ), A("workingQ", o.OP_WRITE))
+            o.op_par_loop_update_Q("update_Q", self.cells, o.op_arg_gbl(dt, 1, "double", o.OP_READ),
+                                   A("q", o.OP_RW), A("rk1", o.OP_READ), A("rk2", o.OP_READ), A("rk3", o.OP_READ),
+                                   A("workingQ", o.OP_WRITE))
+            self.t += self.dt
+
+    def l2_error(self):
+        o = self.op2
+        e = [np.zeros(1) for _ in range(4)]
+        o.op_par_loop_l2_error("l2_error", self.cells, self.A("x", o.OP_READ), self.A("y", o.OP_READ),
+                               self.A("q", o.OP_READ), o.op_arg_gbl(np.array([self.t]), 1, "double", o.OP_READ),
+                               *[o.op_arg_gbl(x, 1, "double", o.OP_INC) for x in e], self.A("error", o.OP_WRITE))
+        return np.array([float(x[0]) for x in e])
+
+
+@pytest.mark.parametrize("N", [3, 4])
+def test_dropin_vortex_matches_oracle(op2, orc, oops, omesh, N):
+    """The vortex app's loop sequence: geometry and dt bit-exact; q after 20 steps and the L2
+    error sums to rounding (exp/pow of the analytic state differ in the last bits between the
+    device and host maths libraries)."""
+    m = omesh.vortex_square(16)
+    phys = orc.freestream(0.4, 0.0)
+    phys.update(vortex_x0=0.0, vortex_y0=0.0, vortex_beta=5.0)
+    ops = oops.operators(N)
+    v = Vortex(op2, m, ops, phys)
+    o = orc.Oracle(m, ops, phys, app=orc.APP_VORTEX, kind="port")
+    o.init(0.1)
+    for name in ("x", "y", "rx", "sy", "nx", "fscale"):
+        assert np.array_equal(v.fetch(name), o.get(name)), name
+    assert orc.rel_l2(v.fetch("q"), o.get("q")) < 1e-15
+    assert abs(v.dt / o.dt - 1) < 1e-15
+    v.run(20)
+    o.run(20, dt_mode=orc.DT_FROZEN, nthreads=1)
+    assert orc.rel_l2(v.fetch("q"), o.get("q")) < 1e-13
+    assert np.abs(v.l2_error() / o.l2_error() - 1).max() < 1e-9
+    sums = v.l2_error()
+    err = v.fetch("error").reshape(-1, 4)  # the per-node squared errors the loop also writes
+    assert np.allclose(err.sum(0), sums, rtol=1e-12, atol=0)
+
+
+def test_dropin_vortex_golden(op2, orc, oops, golden_vortex):
+    """The reference's vortex mesh and state (x0=5, beta=5, dt=0.1/dt1), 100 steps."""
+    g, m = golden_vortex
+    phys = orc.freestream(0.4, 0.0)
+    phys.update(vortex_x0=5.0, vortex_y0=0.0, vortex_beta=5.0)
+    v = Vortex(op2, m, oops.operators(4), phys)
+    assert abs(v.dt / g["dt"] - 1) < 1e-10
+    v.run(100)
+    assert orc.rel_l2(v.fetch("q"), g["q100"]) < 1e-11
+    assert np.abs(v.l2_error() / g["l2_100"] - 1).max() < 1e-7
+
+
+def test_dropin_vortex_rejects_missing_constants(op2, omesh, oops):
+    """A vortex loop without the vortex constants is an error, as OP2's would be."""
+    op2.op_init(0)
+    m = omesh.vortex_square(4)
+    cells = op2.op_decl_set(m["cell2nodes"].shape[0], "cells")
+    x = op2.op_decl_dat(cells, 10, "double", np.zeros(10 * len(m["cell2nodes"])), "x")
+    q = op2.op_decl_dat(cells, 40, "double", np.zeros(40 * len(m["cell2nodes"])), "q")
+    with pytest.raises(op2.Op2Error):
+        op2.op_par_loop_set_ic("set_ic", cells, op2.op_arg_gbl(np.zeros(1), 1, "double", op2.OP_READ),
+                               op2.op_arg_dat(x, -1, None, 10, "double", op2.OP_READ),
+                               op2.op_arg_dat(x, -1, None, 10, "double", op2.OP_READ),
+                               op2.op_arg_dat(q, -1, None, 40, "double", op2.OP_WRITE),
+                               op2.op_arg_dat(q, -1, None, 40, "double", op2.OP_WRITE))
