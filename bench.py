@@ -540,6 +540,7 @@ def main():
                    "l2": "flushed between timed steps (512 MB write outside the events)",
                    "graph": "one CUDA graph launch per step (7 kernels)"},
         "gpu_launches": 7 * args.steps,
+        "nodes_per_s": value / 4,
         "roofline": {"bound": "fp64", "kernel": dominant, "achieved": elem_tf if dominant == "elem_kernel" else face_tf,
                      "peak": peak_tf, "unit": "TFLOP/s",
                      "frac": (elem_tf if dominant == "elem_kernel" else face_tf) / peak_tf,
@@ -564,6 +565,10 @@ def main():
         rate, secs = cpu_oracle_rate(args.cpu_steps, nthreads)
         line["cpu_baseline"] = {"value": rate, "unit": "DOF-stage/s", "cores": nthreads, "kind": "port",
                                 "sample": "%d SSPRK3 steps of the full workload (%.1f s)" % (args.cpu_steps, secs)}
+        one_steps = max(1, args.cpu_steps // 16)
+        rate1, secs1 = cpu_oracle_rate(one_steps, 1)
+        line["cpu_baseline"]["single_core"] = {"value": rate1, "cores": 1,
+                                               "sample": "%d steps (%.1f s)" % (one_steps, secs1)}
     if not args.no_batched:
         line["batched"] = batched_measure(pkg, args.batched_steps)
         line["batched"]["small_instances"] = batched_small_measure(pkg)
