@@ -8,7 +8,8 @@
 //                      face node, with the trace of the neighbour (advec/src/get_neighbour_q.h)
 //                      or the constant ghost value 4.5e-5 (advec/src/get_bedge_q.h), written
 //                      into both cells' face slots scaled by each side's fscale;
-//   advec_elem_kernel  32 cells x Np node-warps: rhs = cr Drw q + cs Dsw q - LIFT flux with
+//   advec_elem_kernel  32 cells x Np node-warps (even/odd form by default, advec_elem_kernel_sym):
+//                      rhs = cr Drw q + cs Dsw q - LIFT flux with
 //                      cr = vx rx + vy ry, cs = vx sx + vy sy (F = vx q, G = vy q on affine
 //                      cells; advec_rhs.h:11-34), then the RK4 combine: W = q + dt frac k for
 //                      stages 0-2 (advec/src/set_workingQ.h) with frac {1/2, 1/2, 1}, and
@@ -117,6 +118,88 @@ __global__ void __launch_bounds__(32 * np_of(N)) advec_elem_kernel(const AdvInst
   }
 }
 
+// The element kernel in even/odd form (the reflection r <-> s splits [Drw | Dsw | -LIFT] into an
+// even and an odd block; see elem_tile_sym in dg_solver.cu): the inputs [cr q; cs q; flux] are
+// staged in the pair order of that split, added and subtracted pairwise, contracted with the
+// even and odd blocks (about half the multiply-adds of the dense rows) and recombined.  Same
+// right-hand side as advec_elem_kernel up to rounding; the RK4 combine is the same.
+template <int N>
+__global__ void __launch_bounds__(32 * np_of(N)) advec_elem_kernel_sym(const AdvInst d, const int stage) {
+  constexpr int Np = np_of(N), NF = 3 * (N + 1), NK = nk_of(N), LD = 33;
+  constexpr int NUe = Sym<N>::NUe, NUo = Sym<N>::NUo, NRe = Sym<N>::NRe;
+  __shared__ double X[NK * LD];   // [slot][cell]
+  __shared__ double Y[Np * LD];   // even / odd row results [row][cell]
+  __shared__ double R[32 * Np];   // right-hand sides [cell][node]
+  const int t = threadIdx.x;
+  const int e0 = blockIdx.x * 32;
+  const int nc = min(32, d.K - e0);
+  const size_t base = (size_t)e0 * Np;
+  {
+    const int el = t / Np, k = t - el * Np;
+    double cr = 0.0, cs = 0.0, w = 0.0;
+    if (el < nc) {
+      const double *g = d.geo + (size_t)(e0 + el) * 16;
+      cr = d.vx * g[0] + d.vy * g[1];
+      cs = d.vx * g[2] + d.vy * g[3];
+      w = d.W[base + t];
+    }
+    X[c_pos[N][k] * LD + el] = cr * w;
+    X[c_pos[N][Np + k] * LD + el] = cs * w;
+    for (int j = t; j < 32 * NF; j += 32 * Np) {
+      const int ef = j / NF, f = j - ef * NF;
+      X[c_pos[N][2 * Np + f] * LD + ef] = ef < nc ? d.flux[(size_t)e0 * NF + j] : 0.0;
+    }
+  }
+  __syncthreads();
+  for (int j = t; j < NUo * 32; j += 32 * Np) {  // butterfly over the input pairs
+    const int p = j >> 5, el = j & 31;
+    const double a = X[p * LD + el], b = X[(NUe + p) * LD + el];
+    X[p * LD + el] = a + b;
+    X[(NUe + p) * LD + el] = a - b;
+  }
+  __syncthreads();
+  const int lane = t & 31, i = t >> 5;
+  {
+    double acc = 0.0;
+    if (i < NRe) {
+#pragma unroll
+      for (int k = 0; k < NUe; k++) acc = fma(opS<N>(i * NUe + k), X[k * LD + lane], acc);
+    } else {
+#pragma unroll
+      for (int k = 0; k < NUo; k++) acc = fma(opS<N>(NRe * NUe + (i - NRe) * NUo + k), X[(NUe + k) * LD + lane], acc);
+    }
+    Y[i * LD + lane] = acc;
+  }
+  __syncthreads();
+  {
+    const int re = c_out[N][3 * i], ro = c_out[N][3 * i + 1], sg = c_out[N][3 * i + 2];
+    double r = Y[re * LD + lane];
+    if (ro >= 0) r = sg > 0 ? r + Y[ro * LD + lane] : r - Y[ro * LD + lane];
+    R[lane * Np + i] = r;
+  }
+  __syncthreads();
+  const int el = t / Np;
+  if (el >= nc) return;
+  const size_t o = base + t;
+  const double r = R[t];
+  if (stage == 4) {
+    d.rhs_out[o] = r;
+    return;
+  }
+  const double q = d.q[o], dt = d.dt;
+  if (stage == 0) {
+    d.acc[o] = r;
+    d.W[o] = __dadd_rn(q, __dmul_rn(dt * 0.5, r));
+  } else if (stage < 3) {
+    d.acc[o] = __dadd_rn(d.acc[o], 2.0 * r);
+    d.W[o] = __dadd_rn(q, __dmul_rn(stage == 1 ? dt * 0.5 : dt, r));
+  } else {
+    const double qn = __dadd_rn(q, __dmul_rn((1.0 / 6.0) * dt, __dadd_rn(d.acc[o], r)));
+    d.q[o] = qn;
+    d.W[o] = qn;
+  }
+}
+
 // advec/src/set_ic.h:3-10 at the node positions of src/init_grid.h.
 template <int N>
 __global__ void advec_ic_kernel(const AdvInst d, const double *coords, const int *cells) {
@@ -148,10 +231,16 @@ __global__ void advec_vertex_kernel(int K, const int *cells, const int *owner, c
 }
 
 template <int N>
+static void advec_launch_elem(const AdvInst &d, int stage, cudaStream_t s) {
+  if (g_elem_variant) advec_elem_kernel_sym<N><<<(d.K + 31) / 32, 32 * np_of(N), 0, s>>>(d, stage);
+  else advec_elem_kernel<N><<<(d.K + 31) / 32, 32 * np_of(N), 0, s>>>(d, stage);
+}
+
+template <int N>
 static void advec_launch_stage(const AdvInst &d, int stage, cudaStream_t s) {
   const int nf = (d.nE + d.nB) * (N + 1);
   if (nf) advec_face_kernel<N><<<(nf + 255) / 256, 256, 0, s>>>(d);
-  advec_elem_kernel<N><<<(d.K + 31) / 32, 32 * np_of(N), 0, s>>>(d, stage);
+  advec_launch_elem<N>(d, stage, s);
 }
 
 Advection::~Advection() {
@@ -240,7 +329,7 @@ void Advection::enqueue_step_events(cudaStream_t s, cudaEvent_t *ev) {
   for (int stage = 0; stage < 4; stage++) {
     DG_DISPATCH(N, (advec_face_kernel<NN><<<(nf + 255) / 256, 256, 0, s>>>(d)));
     cudaEventRecord(ev[1 + 2 * stage], s);
-    DG_DISPATCH(N, (advec_elem_kernel<NN><<<(d.K + 31) / 32, 32 * np_of(NN), 0, s>>>(d, stage)));
+    DG_DISPATCH(N, advec_launch_elem<NN>(d, stage, s));
     cudaEventRecord(ev[2 + 2 * stage], s);
   }
 }

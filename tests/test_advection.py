@@ -157,3 +157,25 @@ def test_device_vertex_values_and_vtk(pkg, orc, omesh, tmp_path):
     assert np.array_equal(a.vertex_values(), want)
     a.write_vtk(tmp_path / "advec.vtk")
     assert np.array_equal(orc.read_vtk_point_data(tmp_path / "advec.vtk")["q"], want)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("N", [1, 2, 3, 4, 5, 6])
+def test_device_even_odd_equals_dense(pkg, orc, omesh, N):
+    """The even/odd element kernel (default) and the dense one: same RHS and steps."""
+    m = omesh.vortex_square(12, 0.0, 1.0)
+    out = []
+    for variant in (0, 1):
+        pkg.lib().dg_set_elem_variant(variant)
+        try:
+            a = pkg.Advection(pkg.Mesh.from_tables(m), N=N, vel_x=0.9, vel_y=-0.4).init()
+            q = a.get("q")
+            r = a.rhs(perturbed(q, N, 0.5))
+            a.set("workingQ", q)
+            a.run(15)
+            a.sync()
+            out.append((r, a.get("q")))
+        finally:
+            pkg.lib().dg_set_elem_variant(1)
+    assert orc.rel_l2(out[1][0], out[0][0]) < 1e-13
+    assert orc.rel_l2(out[1][1], out[0][1]) < 1e-13
