@@ -122,6 +122,7 @@ def lib():
         "dg_kernels_per_step": (C.c_int, []),
         "dg_set_elem_variant": (None, [C.c_int]),
         "dg_set_face_block": (None, [C.c_int]),
+        "dg_set_pdl": (None, [C.c_int]),
         "dg_batch_create": (C.c_int, [C.c_int, C.POINTER(Config), C.POINTER(vp), C.POINTER(vp)]),
         "dg_batch_init": (C.c_int, [vp]),
         "dg_batch_autotune": (C.c_int, [vp, C.c_int, dp]),

@@ -109,6 +109,14 @@ __device__ __forceinline__ double opS(int idx) {
 }
 
 __device__ __forceinline__ double2 ld2(const double *p) { return *reinterpret_cast<const double2 *>(p); }
+
+// Programmatic dependent launch (griddepcontrol): a kernel launched with programmatic stream
+// serialisation may start while its predecessor drains.  pdl_wait() returns once the
+// predecessor grid has completed and its writes are visible (a no-op without that launch
+// attribute); pdl_trigger() lets this grid's successor be scheduled once every block of this
+// grid has issued it or exited.  The waits are the hardware's, not spins of ours.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 __device__ __forceinline__ void st2(double *p, double a, double b) {
   *reinterpret_cast<double2 *>(p) = make_double2(a, b);
 }
@@ -172,6 +180,8 @@ __device__ __forceinline__ void face_node(const Inst &d, const int stage, const 
 
 template <int N>
 __global__ void __launch_bounds__(256) face_kernel(const Inst d, const int stage) {
+  pdl_wait();     // W (and the step state) of the previous kernel
+  pdl_trigger();  // the element kernel may start its face-independent part
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   if (tid >= (d.nE + d.nB) * (N + 1)) return;
   face_node<N>(d, stage, tid);
@@ -301,6 +311,7 @@ __global__ void __launch_bounds__(32 * np_of(N)) elem_kernel(const Inst d, const
   const int e = e0 + lane;
   const bool live = e < d.K;
   const Phys &P = d.P;
+  pdl_trigger();
 
   double w[4] = {0.0, 0.0, 0.0, 0.0};
   double g[4] = {0.0, 0.0, 0.0, 0.0};
@@ -336,6 +347,7 @@ __global__ void __launch_bounds__(32 * np_of(N)) elem_kernel(const Inst d, const
     X[((Np + i) * 32 + lane) * 2] = make_double2(fs0, fs1);
     X[((Np + i) * 32 + lane) * 2 + 1] = make_double2(fs2, fs3);
   }
+  pdl_wait();  // the face fluxes are the face kernel's output
   // Face fluxes of the block's 32 cells: contiguous in HBM, scattered into [k][cell] order.
   {
     const int nthr = 32 * Np, tid = i * 32 + lane;
@@ -372,7 +384,7 @@ __global__ void __launch_bounds__(32 * np_of(N)) elem_kernel(const Inst d, const
 // differences give y_i - y_P(i).  The contraction shrinks to 0.55-0.62 of the dense one.
 // One tile of 32 cells starting at e0, thread (lane, node i) of a block with at least Np
 // node-warps (warps with i >= Np only take part in the barriers).
-template <int N>
+template <int N, bool PDL = false>
 __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, const int e0, const int lane,
                                               const int i, double2 *X) {
   constexpr int Np = np_of(N), Nfp = N + 1, NK = nk_of(N);
@@ -420,6 +432,9 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
       X[(ps * 32 + lane) * 2 + 1] = make_double2(fs2, fs3);
     }
   }
+  // Everything above reads only W and the metrics (written before the face kernel ran); the face
+  // fluxes below are the face kernel's output.
+  if constexpr (PDL) pdl_wait();
   // face fluxes: j = tid + m*nthr, so the face point f = j / 32 is uniform in a warp
   for (int j = active ? tid : 3 * Nfp * 32; j < 3 * Nfp * 32; j += nthr) {
     const int f = j >> 5, el = j & 31;
@@ -494,7 +509,8 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
 template <int N>
 __global__ void __launch_bounds__(32 * np_of(N)) elem_kernel_sym(const Inst d, const int stage) {
   extern __shared__ double2 Xs[];  // [NK][32] x 4 doubles, then [Np][32] x 4 doubles
-  elem_tile_sym<N>(d, stage, blockIdx.x * 32, threadIdx.x, threadIdx.y, Xs);
+  pdl_trigger();  // the next face kernel may be scheduled (it waits for this grid's writes)
+  elem_tile_sym<N, true>(d, stage, blockIdx.x * 32, threadIdx.x, threadIdx.y, Xs);
 }
 
 // ---------------------------------------------------------------- per-step finalize
@@ -682,11 +698,31 @@ __global__ void vertex_fields_kernel(int K, const int *cells, const int *owner, 
 // 65.9 / 74.0 us with 256.
 static int g_face_block = 64;
 
+// 1: face and element kernels of the plain path are launched with programmatic stream
+// serialisation (each may start while its predecessor drains), 0: plain stream order.
+static int g_pdl = 1;
+
+template <class... KArgs, class... Args>
+static void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                       Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = g_pdl ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 template <int N>
 static void launch_face(const Inst &d, int stage, cudaStream_t s) {
   const int nf = (d.nE + d.nB) * (N + 1);
   const int bs = g_face_block;
-  face_kernel<N><<<(nf + bs - 1) / bs, bs, 0, s>>>(d, stage);
+  launch_pdl(face_kernel<N>, dim3((nf + bs - 1) / bs), dim3(bs), 0, s, d, stage);
 }
 
 // 1: even/odd element kernel (default), 0: dense element kernel.
@@ -697,10 +733,10 @@ static void launch_elem(const Inst &d, int stage, cudaStream_t s) {
   constexpr int Np = np_of(N), NK = nk_of(N);
   if (g_elem_variant) {
     const size_t smem = (size_t)(NK + Np) * 32 * 4 * sizeof(double);
-    elem_kernel_sym<N><<<(d.K + 31) / 32, dim3(32, Np), smem, s>>>(d, stage);
+    launch_pdl(elem_kernel_sym<N>, dim3((d.K + 31) / 32), dim3(32, Np), smem, s, d, stage);
   } else {
     const size_t smem = (size_t)NK * 32 * 4 * sizeof(double);
-    elem_kernel<N><<<(d.K + 31) / 32, dim3(32, Np), smem, s>>>(d, stage);
+    launch_pdl(elem_kernel<N>, dim3((d.K + 31) / 32), dim3(32, Np), smem, s, d, stage);
   }
 }
 
@@ -845,6 +881,7 @@ int load_order_constants(int N, std::string &err) {
 }
 
 void set_elem_variant(int v) { g_elem_variant = v ? 1 : 0; }
+void set_pdl(int on) { g_pdl = on ? 1 : 0; }
 void set_face_block(int b) { g_face_block = (b >= 32 && b <= 256 && b % 32 == 0) ? b : 64; }
 
 // ---------------------------------------------------------------- Solver (host)

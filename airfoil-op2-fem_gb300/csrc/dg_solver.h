@@ -52,6 +52,8 @@ int load_order_constants(int N, std::string &err);
 void set_elem_variant(int v);
 // Threads per face-kernel block for launches enqueued from now on (32..256, multiple of 32).
 void set_face_block(int b);
+// Programmatic dependent launch of the plain path's face and element kernels (default on).
+void set_pdl(int on);
 
 struct Solver {
   Config cfg;

@@ -248,6 +248,10 @@ int dg_kernels_per_step(void);
 void dg_set_elem_variant(int variant);
 /* Threads per face-kernel block of the plain path (32..256, multiple of 32; default 64). */
 void dg_set_face_block(int threads);
+/* Launch the plain path's face and element kernels with programmatic dependent launch (1, the
+ * default: each may start while its predecessor drains) or in plain stream order (0).  Both give
+ * bit-identical results; applies to launches and graphs built from now on. */
+void dg_set_pdl(int on);
 
 #ifdef __cplusplus
 }
