@@ -22,6 +22,7 @@ LIB_PATH = os.path.join(HERE, "lib", "libdg_gb300.so")
 APP_AIRFOIL, APP_VORTEX = 0, 1
 DT_EVERY_STEP, DT_FROZEN = 0, 1
 ERR_NONPHYSICAL = -200
+BATCH_GROUPED = 99  # dg_batch variant id of the grouped launches
 
 _lib = None
 
@@ -132,6 +133,7 @@ def lib():
         "dg_batch_time": (C.c_int, [vp, C.c_int, dp, dp, C.POINTER(C.c_ulonglong)]),
         "dg_batch_shape": (C.c_int, [vp, ip, ip, ip, ip]),
         "dg_batch_uses_graph": (C.c_int, [vp]),
+        "dg_batch_use_shape": (C.c_int, [vp, C.c_int, C.c_int]),
         "dg_batch_stream": (vp, [vp]),
         "dg_batch_free": (None, [vp]),
         "dg_batch_last_error": (cp, []),
@@ -425,7 +427,12 @@ class Batch:
         v = [C.c_int() for _ in range(4)]
         self._check(lib().dg_batch_shape(self.h, *[C.byref(x) for x in v]))
         return dict(variant=v[0].value, block=v[1].value, face_tile=v[2].value, grid=v[3].value,
+                    kind="grouped" if v[0].value == BATCH_GROUPED else "persistent",
                     graph=bool(lib().dg_batch_uses_graph(self.h)))
+
+    def use_shape(self, variant, face_tile):
+        """Select a launch shape without timing (variant BATCH_GROUPED for grouped launches)."""
+        self._check(lib().dg_batch_use_shape(self.h, variant, face_tile))
 
     @property
     def stream(self):

@@ -84,6 +84,23 @@ __global__ void __launch_bounds__(BS, MINB) batch_stage_kernel(const Inst *insts
   }
 }
 
+// The grouped alternative the autotuner also times: per stage one ordinary launch over every
+// instance's face tiles, then one launch per order over that order's element tiles (no grid
+// barrier: the kernel boundary orders the two phases).  Same device functions, same results.
+__global__ void __launch_bounds__(256) batch_face_kernel(const Inst *insts, const int4 *ftiles, const int stage) {
+  const int4 ft = ftiles[blockIdx.x];
+  if ((int)threadIdx.x >= ft.z) return;
+  DG_DISPATCH_RT(ft.w, face_node<NN>(insts[ft.x], stage, ft.y + threadIdx.x));
+}
+
+template <int N>
+__global__ void __launch_bounds__(32 * np_of(N)) batch_elem_kernel(const Inst *insts, const int4 *etiles,
+                                                                    const int first, const int stage) {
+  extern __shared__ double2 Xg[];
+  const int4 et = etiles[first + blockIdx.x];
+  elem_tile_sym<N>(insts[et.x], stage, et.y, threadIdx.x & 31, threadIdx.x >> 5, Xg);
+}
+
 __global__ void batch_finalize_kernel(const Inst *insts, const int n) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
@@ -113,8 +130,11 @@ static std::vector<BatchVariant> batch_variants() {
   return {batch_variant<512, 1>(), batch_variant<512, 2>(), batch_variant<1024, 1>()};
 }
 
+// Variant id of the grouped launches (not a persistent kernel).
+constexpr int kGroupedVariant = 99;
+
 struct BatchShape {
-  int variant = -1;  // index into batch_variants()
+  int variant = -1;  // index into batch_variants(), or kGroupedVariant
   int face_tile = 0; // face nodes per face tile
   int grid = 0;      // blocks
   size_t smem = 0;
@@ -131,6 +151,7 @@ struct Batch {
   Inst *d_insts = nullptr;
   int4 *d_ftiles = nullptr, *d_etiles = nullptr;
   int nft = 0, net = 0;
+  int ord_first[7] = {0}, ord_count[7] = {0};  // element tiles of each order (contiguous)
   GridBarrier *d_bar = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   cudaGraph_t graph = nullptr;
@@ -178,12 +199,15 @@ struct Batch {
   // Element tiles (32 cells of one instance), higher orders first; face tiles of ft nodes.
   int build_tiles(int ft, std::string &err) {
     std::vector<int4> et, fts;
-    for (int n = 6; n >= 1; n--)
+    for (int n = 6; n >= 1; n--) {
+      ord_first[n] = (int)et.size();
       for (size_t k = 0; k < solvers.size(); k++) {
         if (cfgs[k].N != n) continue;
         const int K = solvers[k]->K;
         for (int e0 = 0; e0 < K; e0 += 32) et.push_back(make_int4((int)k, e0, 0, n));
       }
+      ord_count[n] = (int)et.size() - ord_first[n];
+    }
     for (size_t k = 0; k < solvers.size(); k++) {
       const Inst &d = solvers[k]->d;
       const int total = (d.nE + d.nB) * (d.N + 1);
@@ -213,6 +237,22 @@ struct Batch {
 
   // Configure one launch shape; grid = resident blocks (cooperative launches need all resident).
   int set_shape(int variant, int ft, BatchShape &out, std::string &err) {
+    if (variant == kGroupedVariant) {
+      if (ft < 32 || ft > 256 || ft % 32) { err = "grouped face tiles are 32..256 nodes, a multiple of 32"; return -1; }
+      for (int n = 1; n <= 6; n++) {
+        const size_t sm = (size_t)(nk_of(n) + np_of(n)) * 32 * 4 * sizeof(double);
+        cudaError_t ce = cudaSuccess;
+        DG_DISPATCH(n, ce = cudaFuncSetAttribute(batch_elem_kernel<NN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)sm));
+        if (ce != cudaSuccess) { err = cudaGetErrorString(ce); return -100; }
+      }
+      if (int rc = build_tiles(ft, err)) return rc;
+      out.variant = variant;
+      out.face_tile = ft;
+      out.grid = 0;
+      out.smem = 0;
+      return 0;
+    }
     const auto vs = batch_variants();
     if (variant < 0 || variant >= (int)vs.size()) { err = "bad variant"; return -1; }
     const BatchVariant &v = vs[variant];
@@ -256,9 +296,20 @@ struct Batch {
     return cudaLaunchKernelExC(&lc, v.fn, args);
   }
 
+  cudaError_t launch_grouped(const BatchShape &sh, int stage, cudaStream_t s) {
+    batch_face_kernel<<<nft, sh.face_tile, 0, s>>>(d_insts, d_ftiles, stage);
+    for (int n = 6; n >= 1; n--) {
+      if (!ord_count[n]) continue;
+      const size_t sm = (size_t)(nk_of(n) + np_of(n)) * 32 * 4 * sizeof(double);
+      DG_DISPATCH(n, (batch_elem_kernel<NN><<<ord_count[n], 32 * np_of(NN), sm, s>>>(d_insts, d_etiles,
+                                                                                       ord_first[n], stage)));
+    }
+    return cudaGetLastError();
+  }
+
   cudaError_t enqueue_step(const BatchShape &sh, cudaStream_t s) {
     for (int stage = 0; stage < 3; stage++) {
-      cudaError_t ce = launch_stage(sh, stage, s);
+      cudaError_t ce = sh.variant == kGroupedVariant ? launch_grouped(sh, stage, s) : launch_stage(sh, stage, s);
       if (ce != cudaSuccess) return ce;
     }
     const int n = (int)solvers.size();
@@ -287,12 +338,17 @@ struct Batch {
     cudaEvent_t a, b;
     cudaEventCreate(&a);
     cudaEventCreate(&b);
-    for (int v = 0; v < (int)vs.size(); v++) {
-      if (vs[v].bs < 32 * maxNp) continue;
-      for (int mult : {1, 2, 4}) {
+    std::vector<std::pair<int, int>> cands;
+    for (int v = 0; v < (int)vs.size(); v++)
+      if (vs[v].bs >= 32 * maxNp)
+        for (int mult : {1, 2, 4}) cands.push_back({v, vs[v].bs * mult});
+    for (int ft : {64, 128, 256}) cands.push_back({kGroupedVariant, ft});
+    for (const auto &cand : cands) {
+      const int v = cand.first;
+      {
         BatchShape sh;
         std::string e2;
-        if (set_shape(v, vs[v].bs * mult, sh, e2)) continue;
+        if (set_shape(v, cand.second, sh, e2)) continue;
         if (enqueue_step(sh, stream) != cudaSuccess) { cudaGetLastError(); continue; }  // warm-up
         cudaEventRecord(a, stream);
         bool ok = true;
@@ -332,9 +388,27 @@ struct Batch {
     return -1;
   }
 
-  // The step graph built node by node: stream capture does not take cooperative launches, a
-  // kernel node with the cooperative attribute does.
+  // The step graph.  Grouped launches are stream-captured; the persistent kernel's graph is
+  // built node by node: stream capture does not take cooperative launches, a kernel node with
+  // the cooperative attribute does.
   int build_graph(std::string &err) {
+    if (shape.variant == kGroupedVariant) {
+      cudaError_t ce = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
+      if (ce == cudaSuccess) enqueue_step(shape, stream);
+      cudaGraph_t g = nullptr;
+      const cudaError_t ce2 = cudaStreamEndCapture(stream, &g);
+      if (ce == cudaSuccess) ce = ce2;
+      if (ce == cudaSuccess) ce = cudaGraphInstantiate(&graph_exec, g, 0);
+      if (ce != cudaSuccess) {
+        cudaGetLastError();
+        if (g) cudaGraphDestroy(g);
+        graph_exec = nullptr;
+        err = cudaGetErrorString(ce);
+        return -1;
+      }
+      graph = g;
+      return 0;
+    }
     const BatchVariant v = batch_variants()[shape.variant];
     cudaGraph_t g = nullptr;
     cudaError_t ce = cudaGraphCreate(&g, 0);

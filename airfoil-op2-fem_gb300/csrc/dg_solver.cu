@@ -1364,10 +1364,24 @@ extern "C" int dg_batch_shape(dg_batch_t *h, int *variant, int *block, int *face
   std::string err;
   if (h->b.ensure_shape(err)) return batch_fail(DG_ERR_ARG, err);
   const auto vs = dg::batch_variants();
+  const bool grouped = h->b.shape.variant == dg::kGroupedVariant;
   if (variant) *variant = h->b.shape.variant;
-  if (block) *block = vs[h->b.shape.variant].bs;
+  // grouped launches: the element block of the highest order, and the face-kernel grid
+  if (block) *block = grouped ? 32 * dg::np_of(h->b.maxN) : vs[h->b.shape.variant].bs;
   if (face_tile) *face_tile = h->b.shape.face_tile;
-  if (grid) *grid = h->b.shape.grid;
+  if (grid) *grid = grouped ? h->b.nft : h->b.shape.grid;
+  return 0;
+}
+
+extern "C" int dg_batch_use_shape(dg_batch_t *h, int variant, int face_tile) {
+  if (!h) return batch_fail(DG_ERR_ARG, "null batch");
+  std::string err;
+  dg::BatchShape sh;
+  if (h->b.set_shape(variant, face_tile, sh, err)) return batch_fail(DG_ERR_ARG, err);
+  h->b.shape = sh;
+  if (h->b.graph_exec) { cudaGraphExecDestroy(h->b.graph_exec); h->b.graph_exec = nullptr; }
+  if (h->b.graph) { cudaGraphDestroy(h->b.graph); h->b.graph = nullptr; }
+  h->b.graph_ok = true;
   return 0;
 }
 

@@ -152,14 +152,19 @@ void dg_solver_free(dg_solver_t *s);
 typedef struct dg_batch_t dg_batch_t;
 int dg_batch_create(int n, const dg_config_t *cfgs, const dg_mesh_t *const *meshes, dg_batch_t **out);
 int dg_batch_init(dg_batch_t *b);
-/* Time every launch shape (kernel variant x face-tile size) over `steps` steps, keep the
- * fastest; the instances' state is restored afterwards. */
+/* Time every launch shape over `steps` steps, keep the fastest; the instances' state is
+ * restored afterwards.  Shapes: the persistent cooperative kernel (variants 0..2: 512 threads x
+ * 1 or 2 resident blocks, 1024 x 1) with face tiles of 1, 2 or 4 blocks' worth of nodes, and
+ * grouped launches (variant 99: per stage one face launch over all instances and one element
+ * launch per order) with face tiles of 64, 128 or 256 nodes. */
 int dg_batch_autotune(dg_batch_t *b, int steps, double *best_ms_per_step);
 int dg_batch_run(dg_batch_t *b, int nsteps);
 int dg_batch_sync(dg_batch_t *b);
 int dg_batch_get(dg_batch_t *b, int instance, const char *name, double *host);
 int dg_batch_time(dg_batch_t *b, int instance, double *t, double *dt, unsigned long long *step);
 int dg_batch_shape(dg_batch_t *b, int *variant, int *block, int *face_tile, int *grid);
+/* Use one launch shape (variant as above) without timing. */
+int dg_batch_use_shape(dg_batch_t *b, int variant, int face_tile);
 int dg_batch_uses_graph(dg_batch_t *b);
 void *dg_batch_stream(dg_batch_t *b);
 void dg_batch_free(dg_batch_t *b);

@@ -56,6 +56,21 @@ def test_batch_autotuned_equals_plain(pkg):
         assert np.array_equal(b.get(k, "q"), ref[k][0]), k
 
 
+@pytest.mark.parametrize("shape", [(0, 512), (2, 2048), (99, 64), (99, 256)])
+def test_batch_every_shape_equals_plain(pkg, shape):
+    """Persistent-kernel variants and the grouped launches: bitwise the plain solvers' results."""
+    meshes, cfgs = instances(pkg)
+    ref = plain(pkg, meshes, cfgs, 10)
+    b = pkg.Batch(meshes, cfgs).init()
+    b.use_shape(*shape)
+    b.run(10)
+    b.sync()
+    sh = b.shape()
+    assert sh["variant"] == shape[0] and sh["graph"]
+    for k in range(len(cfgs)):
+        assert np.array_equal(b.get(k, "q"), ref[k][0]), k
+
+
 def test_batch_reports_nonphysical(pkg):
     meshes, cfgs = instances(pkg)
     b = pkg.Batch(meshes[:2], cfgs[:2]).init()
