@@ -18,7 +18,7 @@ def setup(pkg, N=3, ntheta=32, nr=8, nsteps=60, navg=20, C=7, alpha=2.0, mach=0.
     return mesh, cfg, pkg.LiftObjective(mesh, cfg, nsteps, navg, C)
 
 
-@pytest.mark.parametrize("N", [2, 3, 4])
+@pytest.mark.parametrize("N", [1, 2, 3, 4, 5, 6])
 def test_rhs_vjp_dot_product(pkg, N):
     mesh, cfg, obj = setup(pkg, N=N)
     s = pkg.Solver(mesh, cfg).init()

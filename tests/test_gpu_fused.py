@@ -89,6 +89,19 @@ def test_ogrid_steps_match_oracle(pkg, orc, oops, omesh, farfield):
     assert np.abs(s.dt_history(300) / dts - 1).max() < 1e-12
 
 
+@pytest.mark.parametrize("N", [1, 2, 4, 5, 6])
+def test_steps_every_order_match_oracle(pkg, orc, oops, omesh, N):
+    """100 SSPRK3 steps with dt recomputed every step, every order."""
+    m = omesh.naca_ogrid(32, 8, farfield="characteristic")
+    s, o = solver_and_oracle(pkg, orc, oops, m, N, 0.5, mach=0.45, alpha_deg=1.0)
+    s.record_dt(100)
+    s.run(100)
+    s.sync()
+    dts = o.run(100, nthreads=0)
+    assert orc.rel_l2(s.get("q"), o.get("q")) < 1e-12
+    assert np.abs(s.dt_history(100) / dts - 1).max() < 1e-12
+
+
 def test_vortex_config_matches_oracle(pkg, orc, oops, omesh):
     """The vortex case: [-5,5]^2, 2048 cells, N=3, beta=5, dt = 0.5/dt1 frozen."""
     m = omesh.vortex_square(32)
