@@ -212,6 +212,41 @@ __device__ __forceinline__ double bc_state_adj(const int type, const double nx, 
 }
 
 // ---------------------------------------------------------------- adjoint element kernel
+// Transposed Jacobian of one node's metric-combined fluxes (Fr = rx F + ry G, Fs = sx F + sy G)
+// applied to their adjoints (r, s), written to out[4].
+__device__ __forceinline__ void nodal_flux_adj(const double gm1, const double w0, const double w1, const double w2,
+                                               const double w3, const double rx, const double ry, const double sx,
+                                               const double sy, const double2 r01, const double2 r23,
+                                               const double2 s01, const double2 s23, double *out) {
+  const double ir = rcp(w0);
+  const double u = w1 * ir, v = w2 * ir;
+  const double p = gm1 * fma(-0.5, fma(w1, u, w2 * v), w3);
+  const double ep = w3 + p;
+  const double U = fma(rx, u, ry * v), V = fma(sx, u, sy * v);
+  double w1b = rx * r01.x + sx * s01.x, w2b = ry * r01.x + sy * s01.x;
+  w1b += r01.y * U + s01.y * V;
+  w2b += r23.x * U + s23.x * V;
+  const double Ub = r01.y * w1 + r23.x * w2 + r23.y * ep;
+  const double Vb = s01.y * w1 + s23.x * w2 + s23.y * ep;
+  double pb = rx * r01.y + ry * r23.x + sx * s01.y + sy * s23.x;
+  const double epb = r23.y * U + s23.y * V;
+  double w3b = epb;
+  pb += epb;
+  double ub = rx * Ub + sx * Vb, vb = ry * Ub + sy * Vb;
+  w3b += gm1 * pb;
+  const double kk = -0.5 * gm1 * pb;
+  w1b += kk * u;
+  ub += kk * w1;
+  w2b += kk * v;
+  vb += kk * w2;
+  w1b += ub * ir;
+  w2b += vb * ir;
+  const double irb = ub * w1 + vb * w2;
+  const double w0b = -irb * ir * ir;
+  st2(out, w0b, w1b);
+  st2(out + 2, w2b, w3b);
+}
+
 // mu: adjoint of L (per node); W: the primal state L was evaluated at.  Writes wbar (the volume
 // part of G) and fluxbar (adjoint of each face slot's scaled flux).
 template <int N>
@@ -267,39 +302,118 @@ __global__ void __launch_bounds__(32 * np_of(N)) adj_elem_kernel(const Inst d, c
   const double rx = ga.x, ry = ga.y, sx = gb.x, sy = gb.y;
   const double2 r01 = Xb[(i * 32 + lane) * 2], r23 = Xb[(i * 32 + lane) * 2 + 1];
   const double2 s01 = Xb[((Np + i) * 32 + lane) * 2], s23 = Xb[((Np + i) * 32 + lane) * 2 + 1];
-  const double ir = rcp(w0);
-  const double u = w1 * ir, v = w2 * ir;
-  const double p = d.P.gm1 * fma(-0.5, fma(w1, u, w2 * v), w3);
-  const double ep = w3 + p;
-  const double U = fma(rx, u, ry * v), V = fma(sx, u, sy * v);
-  double w1b = rx * r01.x + sx * s01.x, w2b = ry * r01.x + sy * s01.x;
-  w1b += r01.y * U + s01.y * V;
-  w2b += r23.x * U + s23.x * V;
-  const double Ub = r01.y * w1 + r23.x * w2 + r23.y * ep;
-  const double Vb = s01.y * w1 + s23.x * w2 + s23.y * ep;
-  double pb = rx * r01.y + ry * r23.x + sx * s01.y + sy * s23.x;
-  const double epb = r23.y * U + s23.y * V;
-  double w3b = epb;
-  pb += epb;
-  double ub = rx * Ub + sx * Vb, vb = ry * Ub + sy * Vb;
-  w3b += d.P.gm1 * pb;
-  const double kk = -0.5 * d.P.gm1 * pb;
-  w1b += kk * u;
-  ub += kk * w1;
-  w2b += kk * v;
-  vb += kk * w2;
-  w1b += ub * ir;
-  w2b += vb * ir;
-  const double irb = ub * w1 + vb * w2;
-  const double w0b = -irb * ir * ir;
-  double *o = wbar + ((size_t)e * Np + i) * 4;
-  st2(o, w0b, w1b);
-  st2(o + 2, w2b, w3b);
+  nodal_flux_adj(d.P.gm1, w0, w1, w2, w3, rx, ry, sx, sy, r01, r23, s01, s23,
+                 wbar + ((size_t)e * Np + i) * 4);
 }
 
-// ---------------------------------------------------------------- adjoint face kernel
-// Reverse of face_node: writes the adjoint of each cell face-node trace into tracebar slots
-// [K][3][Nfp][4] (one writer each) and adds scale * (qbb . d ghost / d alpha) to galpha[tid].
+
+// adj_elem_kernel in even/odd form.  The forward operator factors as A = R S B (B: input
+// butterfly, S: the even and odd blocks, R: output recombination), so A^T = B^T S^T R^T: the
+// node adjoints are combined pairwise into even and odd rows (R^T), the blocks are applied
+// transposed (about half the multiply-adds of the dense columns) and each original column is
+// read back as a sum or difference of an even and an odd column (B^T).
+template <int N>
+__global__ void __launch_bounds__(32 * np_of(N)) adj_elem_kernel_sym(const Inst d, const double *mu, double *wbar,
+                                                                      double *fluxbar) {
+  constexpr int Np = np_of(N), Nfp = N + 1, NK = nk_of(N);
+  constexpr int NUe = Sym<N>::NUe, NUo = Sym<N>::NUo, NRe = Sym<N>::NRe;
+  extern __shared__ double2 sm[];
+  double2 *M = sm;                      // [Np][32] x 4 doubles: mu per node
+  double2 *MS = sm + Np * 32 * 2;       // [Np][32] x 4: even rows, then odd rows
+  double2 *XS = sm + 2 * Np * 32 * 2;   // [NK][32] x 4: even columns, then odd columns
+  const int lane = threadIdx.x, i = threadIdx.y;
+  const int e0 = blockIdx.x * 32, e = e0 + lane;
+  const bool live = e < d.K;
+  {
+    double2 m01 = make_double2(0.0, 0.0), m23 = make_double2(0.0, 0.0);
+    if (live) {
+      m01 = ld2(mu + ((size_t)e * Np + i) * 4);
+      m23 = ld2(mu + ((size_t)e * Np + i) * 4 + 2);
+    }
+    M[(i * 32 + lane) * 2] = m01;
+    M[(i * 32 + lane) * 2 + 1] = m23;
+  }
+  __syncthreads();
+  {  // R^T: row i of the split from its node pair
+    const int a = c_rin[N][2 * i], b = c_rin[N][2 * i + 1];
+    double2 v01 = M[(a * 32 + lane) * 2], v23 = M[(a * 32 + lane) * 2 + 1];
+    if (b >= 0) {
+      const double2 w01 = M[(b * 32 + lane) * 2], w23 = M[(b * 32 + lane) * 2 + 1];
+      if (i < NRe) {
+        v01.x += w01.x; v01.y += w01.y; v23.x += w23.x; v23.y += w23.y;
+      } else {
+        v01.x -= w01.x; v01.y -= w01.y; v23.x -= w23.x; v23.y -= w23.y;
+      }
+    }
+    MS[(i * 32 + lane) * 2] = v01;
+    MS[(i * 32 + lane) * 2 + 1] = v23;
+  }
+  __syncthreads();
+  // S^T: column k of the even block (k < NUe) or of the odd block
+  for (int k = i; k < NK; k += Np) {
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    if (k < NUe) {
+#pragma unroll
+      for (int r = 0; r < NRe; r++) {
+        const double cc = opS<N>(r * NUe + k);
+        const double2 x01 = MS[(r * 32 + lane) * 2], x23 = MS[(r * 32 + lane) * 2 + 1];
+        a0 = fma(cc, x01.x, a0); a1 = fma(cc, x01.y, a1); a2 = fma(cc, x23.x, a2); a3 = fma(cc, x23.y, a3);
+      }
+    } else {
+      const int kk = k - NUe;
+#pragma unroll
+      for (int q = 0; q < Np - NRe; q++) {
+        const double cc = opS<N>(NRe * NUe + q * NUo + kk);
+        const double2 x01 = MS[((NRe + q) * 32 + lane) * 2], x23 = MS[((NRe + q) * 32 + lane) * 2 + 1];
+        a0 = fma(cc, x01.x, a0); a1 = fma(cc, x01.y, a1); a2 = fma(cc, x23.x, a2); a3 = fma(cc, x23.y, a3);
+      }
+    }
+    XS[(k * 32 + lane) * 2] = make_double2(a0, a1);
+    XS[(k * 32 + lane) * 2 + 1] = make_double2(a2, a3);
+  }
+  __syncthreads();
+  // B^T: the adjoint of original input column c for cell el
+  auto col = [&](const int c, const int el, double2 &o01, double2 &o23) {
+    const int pos = c_pos[N][c];
+    if (pos >= NUo && pos < NUe) {  // a column fixed by the reflection
+      o01 = XS[(pos * 32 + el) * 2];
+      o23 = XS[(pos * 32 + el) * 2 + 1];
+      return;
+    }
+    const int p = pos < NUo ? pos : pos - NUe;
+    const double2 e01 = XS[(p * 32 + el) * 2], e23 = XS[(p * 32 + el) * 2 + 1];
+    const double2 d01 = XS[((NUe + p) * 32 + el) * 2], d23 = XS[((NUe + p) * 32 + el) * 2 + 1];
+    if (pos < NUo) {
+      o01 = make_double2(e01.x + d01.x, e01.y + d01.y);
+      o23 = make_double2(e23.x + d23.x, e23.y + d23.y);
+    } else {
+      o01 = make_double2(e01.x - d01.x, e01.y - d01.y);
+      o23 = make_double2(e23.x - d23.x, e23.y - d23.y);
+    }
+  };
+  for (int j = i * 32 + lane; j < 3 * Nfp * 32; j += 32 * Np) {
+    const int f = j >> 5, el = j & 31;
+    if (e0 + el < d.K) {
+      double2 a, b;
+      col(2 * Np + f, el, a, b);
+      double *o = fluxbar + (((size_t)(e0 + el)) * 3 * Nfp + f) * 4;
+      st2(o, a.x, a.y);
+      st2(o + 2, b.x, b.y);
+    }
+  }
+  if (!live) return;
+  double2 r01, r23, s01, s23;
+  col(i, lane, r01, r23);
+  col(Np + i, lane, s01, s23);
+  const double *wp = d.W + ((size_t)e * Np + i) * 4;
+  const double2 wa = ld2(wp), wb = ld2(wp + 2);
+  const double w0 = wa.x, w1 = wa.y, w2 = wb.x, w3 = wb.y;
+  const double2 ga = ld2(d.geo + (size_t)e * 16), gb = ld2(d.geo + (size_t)e * 16 + 2);
+  const double rx = ga.x, ry = ga.y, sx = gb.x, sy = gb.y;
+  nodal_flux_adj(d.P.gm1, w0, w1, w2, w3, rx, ry, sx, sy, r01, r23, s01, s23,
+                 wbar + ((size_t)e * Np + i) * 4);
+}
+
 // The vortex state and its derivative with respect to beta (vortex_state with P.vbeta):
 // rho = s^(1/(g-1)), s = 1 - k beta^2, u = 1 + beta cu, v = beta cv.
 __device__ __forceinline__ void vortex_state_dbeta(double x, double y, double t, const Phys &P, double dq[4]) {
@@ -321,6 +435,9 @@ __device__ __forceinline__ void vortex_state_dbeta(double x, double y, double t,
   dq[3] = dp / P.gm1 + 0.5 * drho * (u * u + v * v) + rho * (u * cu + v * cv);
 }
 
+// ---------------------------------------------------------------- adjoint face kernel
+// Reverse of face_node: writes the adjoint of each cell face-node trace into tracebar slots
+// [K][3][Nfp][4] (one writer each) and adds scale * (qbb . d ghost / d alpha) to galpha[tid].
 template <int N>
 __global__ void __launch_bounds__(256) adj_face_kernel(const Inst d, const double *fluxbar, double *tracebar,
                                                         double *galpha, const double ascale, const AlphaSens S,
@@ -678,6 +795,9 @@ struct Adjoint {
       DG_DISPATCH(cfg.N, {
         const size_t sm = (size_t)(np_of(NN) + nk_of(NN)) * 32 * 4 * sizeof(double);
         ce = cudaFuncSetAttribute(adj_elem_kernel<NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (ce == cudaSuccess)
+          ce = cudaFuncSetAttribute(adj_elem_kernel_sym<NN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)((size_t)(2 * np_of(NN) + nk_of(NN)) * 32 * 4 * sizeof(double)));
       });
     }
     if (ce != cudaSuccess) { err = cudaGetErrorString(ce); return -100; }
@@ -794,9 +914,15 @@ struct Adjoint {
     const AlphaSens S = sens();
     const int total = (d.nE + d.nB) * (cfg.N + 1);
     DG_DISPATCH(cfg.N, {
-      const size_t sm = (size_t)(np_of(NN) + nk_of(NN)) * 32 * 4 * sizeof(double);
-      adj_elem_kernel<NN><<<(d.K + 31) / 32, dim3(32, np_of(NN)), sm, st>>>(d, v, wbar, fluxbar);
-      adj_face_kernel<NN><<<(total + 255) / 256, 256, 0, st>>>(d, fluxbar, tracebar, galpha, ascale, S, t_stage);
+      if (g_elem_variant) {
+        const size_t sm = (size_t)(2 * np_of(NN) + nk_of(NN)) * 32 * 4 * sizeof(double);
+        adj_elem_kernel_sym<NN><<<(d.K + 31) / 32, dim3(32, np_of(NN)), sm, st>>>(d, v, wbar, fluxbar);
+      } else {
+        const size_t sm = (size_t)(np_of(NN) + nk_of(NN)) * 32 * 4 * sizeof(double);
+        adj_elem_kernel<NN><<<(d.K + 31) / 32, dim3(32, np_of(NN)), sm, st>>>(d, v, wbar, fluxbar);
+      }
+      // 124 registers: 64-thread blocks (8 per SM) balance the last wave better than 256
+      adj_face_kernel<NN><<<(total + 63) / 64, 64, 0, st>>>(d, fluxbar, tracebar, galpha, ascale, S, t_stage);
     });
   }
 

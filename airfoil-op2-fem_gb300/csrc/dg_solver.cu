@@ -81,6 +81,7 @@ __constant__ double c_S5[sym_size(30, 30, 12, 9)];
 __constant__ double c_S6[sym_size(39, 38, 16, 12)];
 __constant__ int c_pos[7][77];      // staging slot of input column k (Fr 0..Np-1, Fs Np.., faces 2Np..)
 __constant__ int c_out[7][28 * 3];  // per node: even row, odd row or -1, sign (+1 / -1)
+__constant__ int c_rin[7][28 * 2];  // per row (even rows, then odd rows): its node pair (a, b or -1)
 
 // calc_dt face points of each volume node: up to two faces whose fscale multiplies the node's
 // wave speed (-1 = none), after the index rule of src/calc_dt.h:11.
@@ -823,8 +824,21 @@ static int sym_tables(const Operators &o, const std::vector<double> &A, std::str
     const int a = outfix[j];
     out[3 * a] = NPo + (int)j; out[3 * a + 1] = -1; out[3 * a + 2] = 1;
   }
+  // rows -> nodes, for transposed products: even row r is the pair outp[r] (or a fixed node),
+  // odd row NRe + q the pair outp[q]
+  int rin[28 * 2];
+  for (int k = 0; k < 56; k++) rin[k] = -1;
+  for (int r = 0; r < NRe; r++) {
+    rin[2 * r] = r < NPo ? outp[r].first : outfix[r - NPo];
+    rin[2 * r + 1] = r < NPo ? outp[r].second : -1;
+  }
+  for (int q = 0; q < NRo; q++) {
+    rin[2 * (NRe + q)] = outp[q].first;
+    rin[2 * (NRe + q) + 1] = outp[q].second;
+  }
   const void *syms[7] = {nullptr, c_S1, c_S2, c_S3, c_S4, c_S5, c_S6};
   cudaError_t ce = cudaMemcpyToSymbol(syms[N], S.data(), S.size() * sizeof(double));
+  if (ce == cudaSuccess) ce = cudaMemcpyToSymbol(c_rin, rin, sizeof(rin), (size_t)N * sizeof(rin));
   if (ce == cudaSuccess) ce = cudaMemcpyToSymbol(c_pos, pos, sizeof(pos), (size_t)N * sizeof(pos));
   if (ce == cudaSuccess) ce = cudaMemcpyToSymbol(c_out, out, sizeof(out), (size_t)N * sizeof(out));
   if (ce != cudaSuccess) { err = std::string("constant upload: ") + cudaGetErrorString(ce); return -3; }

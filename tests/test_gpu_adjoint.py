@@ -172,3 +172,29 @@ def test_vortex_tangent_linear_matches_adjoint(pkg):
     delta = q0 * np.random.default_rng(9).standard_normal(q0.size) * 1e-2
     tq = obj.tangent(0.0, delta)
     assert abs(tq - np.dot(gq, delta)) <= 1e-10 * abs(tq)
+
+
+@pytest.mark.parametrize("N", [1, 2, 3, 4, 5, 6])
+def test_even_odd_adjoint_equals_dense(pkg, N):
+    """The transposed even/odd element adjoint (default) and the dense one: same vector-Jacobian
+    product to rounding, and the same whole-trajectory gradient."""
+    mesh, cfg, _ = setup(pkg, N=N)
+    rng = np.random.default_rng(40 + N)
+    out = []
+    for variant in (0, 1):
+        pkg.lib().dg_set_elem_variant(variant)
+        try:
+            obj = pkg.LiftObjective(mesh, cfg, 12, 4, 5)
+            q = pkg.Solver(mesh, cfg).init().get("q")
+            W = q * (1.0 + 0.05 * np.random.default_rng(N).standard_normal(q.size))
+            v = np.random.default_rng(N + 1).standard_normal(q.size)
+            vjp, ap = obj.rhs_vjp(W, v)
+            obj.forward()
+            out.append((vjp, ap) + obj.backward())
+        finally:
+            pkg.lib().dg_set_elem_variant(1)
+    a, b = out
+    assert np.linalg.norm(a[0] - b[0]) <= 1e-13 * np.linalg.norm(a[0])
+    assert abs(a[1] - b[1]) <= 1e-12 * abs(a[1])
+    assert abs(a[2] - b[2]) <= 1e-12 * abs(a[2])
+    assert np.linalg.norm(a[3] - b[3]) <= 1e-12 * np.linalg.norm(a[3])
