@@ -20,8 +20,9 @@
  *    (src/cuda/airfoil_kernels.cu:105); op2_gb300_set_exit_on_error(0) makes
  *    them return silently with the message in op2_gb300_last_error().
  *
- * Only the loop kernels of the airfoil application are provided; their
- * argument lists are those of src/airfoil.cpp:204-331.
+ * The loop kernels of the airfoil application are provided with the argument
+ * lists of src/airfoil.cpp:204-331, and those of the vortex application
+ * (vortex/src/vortex.cpp:210-318) as C++ overloads and op_par_loop_l2_error.
  *
  * For C++ callers that include the reference's generated declarations
  * (src/airfoil_op.cpp:17-94 declare the loops with C++ linkage unless
