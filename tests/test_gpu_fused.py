@@ -161,6 +161,23 @@ def test_step_host_equals_run(pkg, omesh):
     assert np.array_equal(out, b.get("q"))
 
 
+@pytest.mark.parametrize("nsteps", [1, 3])
+def test_step_host_pinned_buffers_equal_run(pkg, omesh, nsteps):
+    """Pinned host buffers in and out, one and several steps per call."""
+    m = omesh.naca_ogrid(64, 16)
+    a = pkg.Solver(pkg.Mesh.from_tables(m), pkg.config(N=3, cfl=0.5)).init()
+    b = pkg.Solver(pkg.Mesh.from_tables(m), pkg.config(N=3, cfl=0.5)).init()
+    q = a.get("q")
+    h_in, h_out = pkg.PinnedArray(q.size), pkg.PinnedArray(q.size)
+    h_in.array[:] = q
+    h_out.array[:] = np.nan
+    a.step_host(h_in.array, nsteps, h_out.array)
+    b.run(nsteps)
+    b.sync()
+    assert np.array_equal(h_out.array, b.get("q"))
+    assert np.array_equal(a.get("q"), b.get("q")) and a.time() == b.time()
+
+
 def test_nonphysical_state_is_reported(pkg, omesh):
     """Host-side fault injection: a negative density makes the kernel's guard flag fire and
     the host call return DG_ERR_NONPHYSICAL; the context stays usable."""
