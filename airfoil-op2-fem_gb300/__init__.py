@@ -120,6 +120,7 @@ def lib():
         "dg_stream_sync": (C.c_int, [vp]),
         "dg_l2_flush": (C.c_int, [vp]),
         "dg_fp64_peak_gflops": (C.c_double, []),
+        "dg_fp64_mma_peak_gflops": (C.c_double, []),
         "dg_kernels_per_step": (C.c_int, []),
         "dg_set_elem_variant": (None, [C.c_int]),
         "dg_set_face_block": (None, [C.c_int]),
@@ -634,3 +635,8 @@ def l2_flush(stream):
 
 def fp64_peak_gflops():
     return lib().dg_fp64_peak_gflops()
+
+
+def fp64_mma_peak_gflops():
+    """FP64 tensor-core (DMMA, mma.sync m8n8k4) throughput measured on this GPU, GFLOP/s."""
+    return lib().dg_fp64_mma_peak_gflops()

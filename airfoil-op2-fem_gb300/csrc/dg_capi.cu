@@ -47,6 +47,40 @@ __global__ void dfma_peak_kernel(double *out, int iters, double a, double b) {
   out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
 
+// FP64 tensor-core (DMMA) throughput probe: mma.sync m8n8k4 f64, four independent accumulator
+// chains per thread.  512 flops per warp-level mma.
+__global__ void dmma_peak_kernel(double *out, int iters, double a, double b) {
+  double c[4][2];
+  for (int k = 0; k < 4; k++) c[k][0] = c[k][1] = threadIdx.x * 1e-3 + k;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+      asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};\n"
+                   : "+d"(c[k][0]), "+d"(c[k][1])
+                   : "d"(a), "d"(b));
+  }
+  double acc = 0.0;
+  for (int k = 0; k < 4; k++) acc += c[k][0] + c[k][1];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = acc;
+}
+
+template <class F>
+double time_peak(F launch, double flops) {
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  launch();
+  cudaEventRecord(a);
+  launch();
+  cudaEventRecord(b);
+  cudaEventSynchronize(b);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return ms > 0 ? flops / (ms * 1e-3) * 1e-9 : -1.0;
+}
+
 void *g_flush_buf = nullptr;
 const size_t kFlushBytes = 512ull << 20;  // 4x the 129 MB L2
 }  // namespace
@@ -557,20 +591,24 @@ double dg_fp64_peak_gflops(void) {
   const int blocks = sms * 8, threads = 256, iters = 4096;
   double *out = nullptr;
   if (cudaMalloc(&out, sizeof(double) * blocks * threads) != cudaSuccess) return -1.0;
-  cudaEvent_t a, b;
-  cudaEventCreate(&a);
-  cudaEventCreate(&b);
-  dfma_peak_kernel<<<blocks, threads>>>(out, iters, 0.999, 1e-3);
-  cudaEventRecord(a);
-  dfma_peak_kernel<<<blocks, threads>>>(out, iters, 0.999, 1e-3);
-  cudaEventRecord(b);
-  cudaEventSynchronize(b);
-  float ms = 0;
-  cudaEventElapsedTime(&ms, a, b);
-  cudaEventDestroy(a);
-  cudaEventDestroy(b);
+  const double g = time_peak([&] { dfma_peak_kernel<<<blocks, threads>>>(out, iters, 0.999, 1e-3); },
+                             16.0 * iters * (double)blocks * threads);
   cudaFree(out);
-  return 16.0 * iters * (double)blocks * threads / (ms * 1e-3) * 1e-9;
+  return g;
+}
+
+double dg_fp64_mma_peak_gflops(void) {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return -1.0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = sms * 8, threads = 256, iters = 2048;
+  double *out = nullptr;
+  if (cudaMalloc(&out, sizeof(double) * blocks * threads) != cudaSuccess) return -1.0;
+  const double warps = (double)blocks * threads / 32;
+  const double g = time_peak([&] { dmma_peak_kernel<<<blocks, threads>>>(out, iters, 0.999, 1e-3); },
+                             512.0 * 4 * iters * warps);
+  cudaFree(out);
+  return g;
 }
 int dg_kernels_per_step(void) { return 7; }
 void dg_set_elem_variant(int variant) { dg::set_elem_variant(variant); }

@@ -461,6 +461,7 @@ def main():
     dof_stage_per_step = 3 * 4 * K * Np
     stream = s.stream
     peak_gflops = pkg.fp64_peak_gflops()
+    dmma_gflops = pkg.fp64_mma_peak_gflops()
 
     # warm-up (graph capture happens on the first run)
     s.run(args.warmup)
@@ -549,6 +550,8 @@ def main():
                      "traffic": traffic if dominant == "elem_kernel" else None,
                      "traffic_source": "ncu dram__bytes_read+write per launch, stage average (profiles/)",
                      "peak_source": "DFMA throughput measured live on this GPU (MEASURED_PEAKS.json has no FP64 figure)",
+                     "fp64_tensor_peak_tflops": dmma_gflops * 1e-3,
+                     "fp64_tensor_note": "DMMA (mma.sync m8n8k4 f64) measured live; below DFMA and on the same pipe, so unused",
                      "flops_per_unit": elem_flops(N_ORDER) if dominant == "elem_kernel" else face_flops(N_ORDER),
                      "unit_def": "cell-stage" if dominant == "elem_kernel" else "face node",
                      "kernel_ms": {"face": face_ms, "elem": elem_ms, "elem_stage2": float(kt[5]),

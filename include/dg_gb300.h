@@ -246,6 +246,8 @@ int dg_stream_sync(void *stream);
 int dg_l2_flush(void *stream);
 /* Measured FP64 DFMA throughput of this GPU, GFLOP/s (FMA = 2 flops). */
 double dg_fp64_peak_gflops(void);
+/* Measured FP64 tensor-core (mma.sync m8n8k4 f64) throughput of this GPU, GFLOP/s. */
+double dg_fp64_mma_peak_gflops(void);
 /* Number of kernels one dg_solver_run step launches. */
 int dg_kernels_per_step(void);
 /* Element-kernel form for launches and graphs built from now on: 1 even/odd split of
