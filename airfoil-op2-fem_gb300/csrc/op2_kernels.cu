@@ -10,6 +10,7 @@
 #include <sys/time.h>
 #include <time.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -367,87 +368,107 @@ __device__ __forceinline__ void euler_flux(const double *q, double *F, double *G
   G[3] = v * (q[3] + p);
 }
 
-// src/euler_rhs.h:222-291 with roe (:120-220) inlined per face point
+// src/euler_rhs.h:120-220: the Roe flux at face point i of a cell, times fscale, into out[4].
 template <int N>
-__global__ void __launch_bounds__(128) k_euler_rhs(int n, const double *Wa, double *exQa,
+__device__ __forceinline__ void roe_point(const double *q, const double *exQ, const double *nx, const double *ny,
+                                          const double *fscale, const int i, const Consts &C, double *out) {
+  const double gam = C.gam;
+  const int ind = C.FMASK[i] * 4;
+  const double *pq = &exQ[i * 4];
+  double mRoeQ[4], pRoeQ[4];
+  mRoeQ[0] = q[ind];
+  mRoeQ[1] = nx[i] * q[ind + 1] + ny[i] * q[ind + 2];
+  mRoeQ[2] = -ny[i] * q[ind + 1] + nx[i] * q[ind + 2];
+  mRoeQ[3] = q[ind + 3];
+  pRoeQ[0] = pq[0];
+  pRoeQ[1] = nx[i] * pq[1] + ny[i] * pq[2];
+  pRoeQ[2] = -ny[i] * pq[1] + nx[i] * pq[2];
+  pRoeQ[3] = pq[3];
+  double fxMQ[4], fyMQ[4], mRoeRho, mRoeU, mRoeV, mRoeP;
+  euler_flux(mRoeQ, fxMQ, fyMQ, mRoeRho, mRoeU, mRoeV, mRoeP, gam);
+  double fxPQ[4], fyPQ[4], pRoeRho, pRoeU, pRoeV, pRoeP;
+  euler_flux(pRoeQ, fxPQ, fyPQ, pRoeRho, pRoeU, pRoeV, pRoeP, gam);
+  double mH = (mRoeQ[3] + mRoeP) / mRoeRho;
+  double pH = (pRoeQ[3] + pRoeP) / pRoeRho;
+  double mS = sqrt(mRoeRho), pS = sqrt(pRoeRho);
+  double rho = mS * pS;
+  double u = (mS * mRoeU + pS * pRoeU) / (mS + pS);
+  double v = (mS * mRoeV + pS * pRoeV) / (mS + pS);
+  double H = (mS * mH + pS * pH) / (mS + pS);
+  double c2 = (gam - 1) * (H - 0.5 * (u * u + v * v));
+  double cc = sqrt(c2);
+  double dW1 = -0.5 * rho * (pRoeU - mRoeU) / cc + 0.5 * (pRoeP - mRoeP) / c2;
+  double dW2 = (pRoeRho - mRoeRho) - (pRoeP - mRoeP) / c2;
+  double dW3 = rho * (pRoeV - mRoeV);
+  double dW4 = 0.5 * rho * (pRoeU - mRoeU) / cc + 0.5 * (pRoeP - mRoeP) / c2;
+  dW1 = fabs(u - cc) * dW1;
+  dW2 = fabs(u) * dW2;
+  dW3 = fabs(u) * dW3;
+  dW4 = fabs(u + cc) * dW4;
+  double fx[4];
+  for (int k = 0; k < 4; k++) fx[k] = (fxMQ[k] + fxPQ[k]) / 2.0;
+  fx[0] = fx[0] - (dW1 + dW2 + dW4) / 2.0;
+  fx[1] = fx[1] - (dW1 * (u - cc) + dW2 * u + dW4 * (u + cc)) / 2.0;
+  fx[2] = fx[2] - (dW1 * v + dW2 * v + dW3 + dW4 * v) / 2.0;
+  fx[3] = fx[3] - (dW1 * (H - u * cc) + dW2 * (u * u + v * v) + dW3 * v + dW4 * (H + u * cc)) / 2.0;
+  out[0] = fx[0] * fscale[i];
+  out[1] = (nx[i] * fx[1] - ny[i] * fx[2]) * fscale[i];
+  out[2] = (ny[i] * fx[1] + nx[i] * fx[2]) * fscale[i];
+  out[3] = fx[3] * fscale[i];
+}
+
+// src/euler_rhs.h:222-291 for a tile of T cells per block, work spread over the tile's nodes and
+// face points: (1) nodal fluxes F, G (:226-229), (2) the Roe flux of every face point
+// (:281-282), (3) per node and variable the four weak-derivative dot products (:240-243, each in
+// ascending order, as the ascending-index dgemv), their metric combination (:245-247) and the
+// LIFT dot product (:284-286), (4) exteriorQ zeroed when the loop has it OP_RW (:288-290).  Every
+// value is formed by the same operations in the same order as the one-cell kernel.
+template <int N>
+__global__ void __launch_bounds__(128) k_euler_rhs(int n, int T, const double *Wa, double *exQa,
                                                     const double *rxa, const double *rya,
                                                     const double *sxa, const double *sya,
                                                     const double *fsa, const double *nxa,
                                                     const double *nya, double *rhsa, const Consts C,
                                                     const bool zero_ext) {
   constexpr int Np = Ord<N>::Np, Nfp = Ord<N>::Nfp;
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= n) return;
-  const double gam = C.gam;
-  const double *q = Wa + (size_t)4 * Np * c;
-  double *exQ = exQa + (size_t)12 * Nfp * c;
-  const double *rx = rxa + (size_t)Np * c, *ry = rya + (size_t)Np * c;
-  const double *sx = sxa + (size_t)Np * c, *sy = sya + (size_t)Np * c;
-  const double *fscale = fsa + (size_t)3 * Nfp * c, *nx = nxa + (size_t)3 * Nfp * c, *ny = nya + (size_t)3 * Nfp * c;
-  double *qRHS = rhsa + (size_t)4 * Np * c;
-  double F[4 * Np], G[4 * Np];
-  for (int i = 0; i < Np; i++) {
+  extern __shared__ double sh[];
+  double *F = sh, *G = sh + (size_t)T * 4 * Np, *FL = sh + (size_t)T * 8 * Np;  // [T][4Np], [T][4Np], [T][12Nfp]
+  const int c0 = blockIdx.x * T;
+  const int nc = min(T, n - c0);
+  for (int t = threadIdx.x; t < nc * Np; t += blockDim.x) {
+    const int cl = t / Np, j = t - cl * Np;
     double rho, u, v, p;
-    euler_flux(&q[i * 4], &F[i * 4], &G[i * 4], rho, u, v, p, gam);
+    euler_flux(Wa + (size_t)4 * Np * (c0 + cl) + 4 * j, F + (size_t)cl * 4 * Np + 4 * j, G + (size_t)cl * 4 * Np + 4 * j,
+               rho, u, v, p, C.gam);
   }
-  for (int i = 0; i < 4; i++) {
-    double dFdr[Np], dFds[Np], dGdr[Np], dGds[Np];
-    gemv(Np, Np, 1.0, C.Drw, Np, &F[i], 4, 0.0, dFdr, 1);
-    gemv(Np, Np, 1.0, C.Dsw, Np, &F[i], 4, 0.0, dFds, 1);
-    gemv(Np, Np, 1.0, C.Drw, Np, &G[i], 4, 0.0, dGdr, 1);
-    gemv(Np, Np, 1.0, C.Dsw, Np, &G[i], 4, 0.0, dGds, 1);
-    for (int j = 0; j < Np; j++)
-      qRHS[i + j * 4] = (rx[j] * dFdr[j] + sx[j] * dFds[j]) + (ry[j] * dGdr[j] + sy[j] * dGds[j]);
+  for (int t = threadIdx.x; t < nc * 3 * Nfp; t += blockDim.x) {
+    const int cl = t / (3 * Nfp), i = t - cl * 3 * Nfp;
+    const size_t c = c0 + cl;
+    roe_point<N>(Wa + 4 * Np * c, exQa + 12 * Nfp * c, nxa + 3 * Nfp * c, nya + 3 * Nfp * c, fsa + 3 * Nfp * c, i, C,
+                 FL + (size_t)cl * 12 * Nfp + 4 * i);
   }
-  double flux[4 * 3 * Nfp];
-  for (int i = 0; i < 3 * Nfp; i++) {
-    const int ind = C.FMASK[i] * 4;
-    const double *pq = &exQ[i * 4];
-    double mRoeQ[4], pRoeQ[4];
-    mRoeQ[0] = q[ind];
-    mRoeQ[1] = nx[i] * q[ind + 1] + ny[i] * q[ind + 2];
-    mRoeQ[2] = -ny[i] * q[ind + 1] + nx[i] * q[ind + 2];
-    mRoeQ[3] = q[ind + 3];
-    pRoeQ[0] = pq[0];
-    pRoeQ[1] = nx[i] * pq[1] + ny[i] * pq[2];
-    pRoeQ[2] = -ny[i] * pq[1] + nx[i] * pq[2];
-    pRoeQ[3] = pq[3];
-    double fxMQ[4], fyMQ[4], mRoeRho, mRoeU, mRoeV, mRoeP;
-    euler_flux(mRoeQ, fxMQ, fyMQ, mRoeRho, mRoeU, mRoeV, mRoeP, gam);
-    double fxPQ[4], fyPQ[4], pRoeRho, pRoeU, pRoeV, pRoeP;
-    euler_flux(pRoeQ, fxPQ, fyPQ, pRoeRho, pRoeU, pRoeV, pRoeP, gam);
-    double mH = (mRoeQ[3] + mRoeP) / mRoeRho;
-    double pH = (pRoeQ[3] + pRoeP) / pRoeRho;
-    double mS = sqrt(mRoeRho), pS = sqrt(pRoeRho);
-    double rho = mS * pS;
-    double u = (mS * mRoeU + pS * pRoeU) / (mS + pS);
-    double v = (mS * mRoeV + pS * pRoeV) / (mS + pS);
-    double H = (mS * mH + pS * pH) / (mS + pS);
-    double c2 = (gam - 1) * (H - 0.5 * (u * u + v * v));
-    double cc = sqrt(c2);
-    double dW1 = -0.5 * rho * (pRoeU - mRoeU) / cc + 0.5 * (pRoeP - mRoeP) / c2;
-    double dW2 = (pRoeRho - mRoeRho) - (pRoeP - mRoeP) / c2;
-    double dW3 = rho * (pRoeV - mRoeV);
-    double dW4 = 0.5 * rho * (pRoeU - mRoeU) / cc + 0.5 * (pRoeP - mRoeP) / c2;
-    dW1 = fabs(u - cc) * dW1;
-    dW2 = fabs(u) * dW2;
-    dW3 = fabs(u) * dW3;
-    dW4 = fabs(u + cc) * dW4;
-    double fx[4];
-    for (int k = 0; k < 4; k++) fx[k] = (fxMQ[k] + fxPQ[k]) / 2.0;
-    fx[0] = fx[0] - (dW1 + dW2 + dW4) / 2.0;
-    fx[1] = fx[1] - (dW1 * (u - cc) + dW2 * u + dW4 * (u + cc)) / 2.0;
-    fx[2] = fx[2] - (dW1 * v + dW2 * v + dW3 + dW4 * v) / 2.0;
-    fx[3] = fx[3] - (dW1 * (H - u * cc) + dW2 * (u * u + v * v) + dW3 * v + dW4 * (H + u * cc)) / 2.0;
-    flux[i * 4] = fx[0];
-    flux[i * 4 + 1] = nx[i] * fx[1] - ny[i] * fx[2];
-    flux[i * 4 + 2] = ny[i] * fx[1] + nx[i] * fx[2];
-    flux[i * 4 + 3] = fx[3];
-    for (int k = 0; k < 4; k++) flux[i * 4 + k] *= fscale[i];
+  __syncthreads();
+  for (int t = threadIdx.x; t < nc * Np * 4; t += blockDim.x) {
+    const int cl = t / (4 * Np), r = t - cl * 4 * Np, j = r >> 2, var = r & 3;
+    const size_t c = c0 + cl;
+    const double *Fc = F + (size_t)cl * 4 * Np, *Gc = G + (size_t)cl * 4 * Np;
+    double dFdr = 0.0, dFds = 0.0, dGdr = 0.0, dGds = 0.0;
+    for (int k = 0; k < Np; k++) dFdr += C.Drw[j * Np + k] * Fc[k * 4 + var];
+    for (int k = 0; k < Np; k++) dFds += C.Dsw[j * Np + k] * Fc[k * 4 + var];
+    for (int k = 0; k < Np; k++) dGdr += C.Drw[j * Np + k] * Gc[k * 4 + var];
+    for (int k = 0; k < Np; k++) dGds += C.Dsw[j * Np + k] * Gc[k * 4 + var];
+    dFdr = 1.0 * dFdr; dFds = 1.0 * dFds; dGdr = 1.0 * dGdr; dGds = 1.0 * dGds;
+    const size_t o = (size_t)Np * c + j;
+    const double vol = (rxa[o] * dFdr + sxa[o] * dFds) + (rya[o] * dGdr + sya[o] * dGds);
+    const double *fl = FL + (size_t)cl * 12 * Nfp;
+    double lift = 0.0;
+    for (int k = 0; k < 3 * Nfp; k++) lift += C.LIFT[j * 3 * Nfp + k] * fl[k * 4 + var];
+    rhsa[4 * Np * c + 4 * j + var] = -1.0 * lift + 1.0 * vol;
   }
-  for (int i = 0; i < 4; i++) gemv(Np, 3 * Nfp, -1.0, C.LIFT, 3 * Nfp, &flux[i], 4, 1.0, qRHS + i, 4);
-  if (zero_ext)  // the airfoil copy zeroes exteriorQ (OP_RW); the vortex copy reads it (OP_READ)
-    for (int i = 0; i < 12 * Nfp; i++) exQ[i] = 0.0;
+  if (zero_ext) {  // the airfoil copy zeroes exteriorQ (OP_RW); the vortex copy reads it (OP_READ)
+    __syncthreads();
+    for (int t = threadIdx.x; t < nc * 12 * Nfp; t += blockDim.x) exQa[(size_t)12 * Nfp * c0 + t] = 0.0;
+  }
 }
 
 // src/set_workingQ.h:1-12, one thread per value
@@ -920,8 +941,12 @@ void op_par_loop_euler_rhs(char const *name, op_set set, op_arg a0, op_arg a1, o
   Consts C;
   if (!consts_for(N, true, C)) return;
   Timed t(name ? name : "euler_rhs");
-  DISPATCH_N(N, (k_euler_rhs<N><<<blocks(set->size, 128), 128, 0, S().stream>>>(
-                    set->size, dptr<double>(a0), dptr<double>(a1), dptr<double>(a2), dptr<double>(a3),
+  // tile of T cells per 128-thread block, T chosen so that the tile's fluxes fit in 48 KB
+  const int per_cell = (12 * Np + 12 * Nfp) * 8;
+  const int T = std::max(1, std::min(32, 49152 / per_cell));
+  const size_t smem = (size_t)T * per_cell;
+  DISPATCH_N(N, (k_euler_rhs<N><<<blocks(set->size, T), 128, smem, S().stream>>>(
+                    set->size, T, dptr<double>(a0), dptr<double>(a1), dptr<double>(a2), dptr<double>(a3),
                     dptr<double>(a4), dptr<double>(a5), dptr<double>(a6), dptr<double>(a7), dptr<double>(a8),
                     dptr<double>(a9), C, zero_ext)));
   if (!ck(cudaGetLastError(), "euler_rhs launch")) return;
