@@ -22,6 +22,7 @@ LIB_PATH = os.path.join(HERE, "lib", "libdg_gb300.so")
 APP_AIRFOIL, APP_VORTEX = 0, 1
 DT_EVERY_STEP, DT_FROZEN = 0, 1
 ERR_NONPHYSICAL = -200
+ERR_TIMEOUT = -300
 BATCH_GROUPED = 99  # dg_batch variant id of the grouped launches
 
 _lib = None
@@ -135,6 +136,7 @@ def lib():
         "dg_batch_shape": (C.c_int, [vp, ip, ip, ip, ip]),
         "dg_batch_uses_graph": (C.c_int, [vp]),
         "dg_batch_use_shape": (C.c_int, [vp, C.c_int, C.c_int]),
+        "dg_batch_inject_barrier_timeout": (C.c_int, [vp]),
         "dg_batch_stream": (vp, [vp]),
         "dg_batch_free": (None, [vp]),
         "dg_batch_last_error": (cp, []),

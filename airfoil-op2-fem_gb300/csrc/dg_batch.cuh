@@ -479,7 +479,13 @@ struct Batch {
     GridBarrier b;
     ce = cudaMemcpy(&b, d_bar, sizeof(b), cudaMemcpyDeviceToHost);
     if (ce != cudaSuccess) { err = cudaGetErrorString(ce); return -100; }
-    if (b.err) { err = "a grid barrier wait timed out: results of that step are invalid"; return -8; }
+    if (b.err) {
+      // report once: the flag is cleared so that the batch can be re-initialised and run again
+      GridBarrier z = {};
+      cudaMemcpy(d_bar, &z, sizeof(z), cudaMemcpyHostToDevice);
+      err = "a grid barrier wait timed out: results of that step are invalid";
+      return -8;
+    }
     for (size_t k = 0; k < solvers.size(); k++) {
       StepState st;
       if (solvers[k]->state(st, err)) return -100;

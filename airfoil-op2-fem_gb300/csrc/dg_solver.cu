@@ -1345,7 +1345,19 @@ extern "C" int dg_batch_sync(dg_batch_t *h) {
   std::string err;
   const int rc = h->b.sync(err);
   if (rc == -200) return batch_fail(DG_ERR_NONPHYSICAL, err);
+  if (rc == -8) return batch_fail(DG_ERR_TIMEOUT, err);
   if (rc) return batch_fail(DG_ERR_CUDA, err);
+  return 0;
+}
+
+// Host-side fault injection for tests: mark the grid barrier as timed out, as a kernel whose
+// bounded wait gave up would (no kernel is made to wait).
+extern "C" int dg_batch_inject_barrier_timeout(dg_batch_t *h) {
+  if (!h) return batch_fail(DG_ERR_ARG, "null batch");
+  dg::GridBarrier b = {};
+  b.err = 2u;
+  if (cudaMemcpy(h->b.d_bar, &b, sizeof(b), cudaMemcpyHostToDevice) != cudaSuccess)
+    return batch_fail(DG_ERR_CUDA, "cudaMemcpy");
   return 0;
 }
 

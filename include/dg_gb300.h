@@ -26,7 +26,8 @@ enum {
   DG_OK = 0,
   DG_ERR_ARG = -1,
   DG_ERR_CUDA = -100,
-  DG_ERR_NONPHYSICAL = -200 /* a kernel saw a non-positive or non-finite density */
+  DG_ERR_NONPHYSICAL = -200, /* a kernel saw a non-positive or non-finite density */
+  DG_ERR_TIMEOUT = -300      /* a bounded wait in a batched kernel gave up (that step is invalid) */
 };
 
 const char *dg_last_error(void);
@@ -163,6 +164,9 @@ int dg_batch_sync(dg_batch_t *b);
 int dg_batch_get(dg_batch_t *b, int instance, const char *name, double *host);
 int dg_batch_time(dg_batch_t *b, int instance, double *t, double *dt, unsigned long long *step);
 int dg_batch_shape(dg_batch_t *b, int *variant, int *block, int *face_tile, int *grid);
+/* Host-side fault injection for tests: record a grid-barrier timeout as a kernel whose bounded
+ * wait gave up would; the next dg_batch_sync reports DG_ERR_TIMEOUT and clears it. */
+int dg_batch_inject_barrier_timeout(dg_batch_t *b);
 /* Use one launch shape (variant as above) without timing. */
 int dg_batch_use_shape(dg_batch_t *b, int variant, int face_tile);
 int dg_batch_uses_graph(dg_batch_t *b);

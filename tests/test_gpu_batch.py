@@ -80,3 +80,19 @@ def test_batch_reports_nonphysical(pkg):
     bad.run(40)
     with pytest.raises(pkg.DGError):
         bad.sync()
+
+
+def test_batch_reports_barrier_timeout(pkg):
+    """Host-side injection of a timed-out grid barrier (no kernel is made to wait): sync reports
+    DG_ERR_TIMEOUT once, then the batch runs on."""
+    meshes, cfgs = instances(pkg)
+    b = pkg.Batch(meshes[:2], cfgs[:2]).init()
+    b.run(2)
+    b.sync()
+    pkg.lib().dg_batch_inject_barrier_timeout(b.h)
+    with pytest.raises(pkg.DGError) as e:
+        b.sync()
+    assert e.value.code == pkg.ERR_TIMEOUT
+    b.init()
+    b.run(2)
+    b.sync()
