@@ -48,6 +48,7 @@ struct Consts {
   const int *FMASK;
   double gam, bc_r, bc_u, bc_v, bc_e;
   double vortex_x0, vortex_y0, vortex_beta;  // the vortex app's constants (vortex.cpp op_decl_const)
+  double velX, velY;                         // the advection app's (advec/src/advec.cpp:156-157)
 };
 
 struct LoopStat {
@@ -256,6 +257,107 @@ __global__ void k_l2_error(int n, const double *xa, const double *ya, const doub
   part[4 * (size_t)c + 1] = e1;
   part[4 * (size_t)c + 2] = e2;
   part[4 * (size_t)c + 3] = e3;
+}
+
+// ------------------------------------------------------------------ advection app (advec/src)
+// advec/src/set_ic.h:3-10, one thread per node
+__global__ void k_adv_set_ic(long long n, const double *x, const double *y, double *q, double *W) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  q[i] = exp(-40.0 * (x[i] - 0.5) * (x[i] - 0.5)) * exp(-40.0 * (y[i] - 0.5) * (y[i] - 0.5));
+  W[i] = q[i];
+}
+
+// advec/src/get_neighbour_q.h:3-87
+template <int N>
+__global__ void k_adv_get_neighbour_q(int n, const int *edgeNum, const int *map, int mdim, int iL, int iR,
+                                      const double *nodeX, const double *nodeY, const double *W, double *exQ,
+                                      const Consts C) {
+  constexpr int Np = Ord<N>::Np, Nfp = Ord<N>::Nfp;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const int cL = map[e * mdim + iL], cR = map[e * mdim + iR];
+  const int edgeL = edgeNum[2 * e], edgeR = edgeNum[2 * e + 1];
+  const double *xL = nodeX + 3 * cL, *yL = nodeY + 3 * cL, *xR = nodeX + 3 * cR, *yR = nodeY + 3 * cR;
+  const bool reverse = !(xL[edgeL] == xR[edgeR] && yL[edgeL] == yR[edgeR]);
+  const double *qL = W + (size_t)Np * cL, *qR = W + (size_t)Np * cR;
+  double *eL = exQ + (size_t)3 * Nfp * cL, *eR = exQ + (size_t)3 * Nfp * cR;
+  const int *fR = C.FMASK + edgeR * Nfp, *fL = C.FMASK + edgeL * Nfp;
+  for (int i = 0; i < Nfp; i++) {
+    atomicAdd(&eL[edgeL * Nfp + i], qR[reverse ? fR[Nfp - i - 1] : fR[i]]);
+    atomicAdd(&eR[edgeR * Nfp + i], qL[reverse ? fL[Nfp - i - 1] : fL[i]]);
+  }
+}
+
+// advec/src/get_bedge_q.h:3-13
+template <int N>
+__global__ void k_adv_get_bedge_q(int n, const int *bnum, const int *map, int mdim, int i0, double *exQ) {
+  constexpr int Nfp = Ord<N>::Nfp;
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n) return;
+  double *e = exQ + (size_t)3 * Nfp * map[b * mdim + i0] + bnum[b] * Nfp;
+  for (int i = 0; i < Nfp; i++) atomicAdd(&e[i], 4.5e-5);
+}
+
+// advec/src/advec_rhs.h:7-67, one thread per (cell, node) for the volume and lift dot products
+// (each in ascending order) and per (cell, face point) for the face flux, T cells per block.
+template <int N>
+__global__ void __launch_bounds__(128) k_advec_rhs(int n, const double *qa, const double *exQa, const double *rxa,
+                                                    const double *rya, const double *sxa, const double *sya,
+                                                    const double *fsa, const double *nxa, const double *nya,
+                                                    double *rhsa, const Consts C) {
+  constexpr int Np = Ord<N>::Np, Nfp = Ord<N>::Nfp, T = 16;
+  __shared__ double F[T * Np], G[T * Np], FL[T * 3 * Nfp];
+  const int c0 = blockIdx.x * T;
+  const int nc = min(T, n - c0);
+  const double velX = C.velX, velY = C.velY;
+  for (int t = threadIdx.x; t < nc * Np; t += blockDim.x) {
+    const double q = qa[(size_t)Np * c0 + t];
+    F[t] = velX * q;
+    G[t] = velY * q;
+  }
+  const double a = sqrt(velX * velX + velY * velY);
+  for (int t = threadIdx.x; t < nc * 3 * Nfp; t += blockDim.x) {
+    const int cl = t / (3 * Nfp), j = t - cl * 3 * Nfp;
+    const size_t c = c0 + cl;
+    const double mQ = qa[(size_t)Np * c + C.FMASK[j]], pQ = exQa[(size_t)3 * Nfp * c + j];
+    const double mF = velX * mQ, mG = velY * mQ, pF = velX * pQ, pG = velY * pQ;
+    const size_t f = (size_t)3 * Nfp * c + j;
+    double nf = nxa[f] * (mF + pF) + nya[f] * (mG + pG) + a * (mQ - pQ);
+    nf *= 0.5 * fsa[f];
+    FL[t] = nf;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < nc * Np; t += blockDim.x) {
+    const int cl = t / Np, i = t - cl * Np;
+    const double *Fc = F + cl * Np, *Gc = G + cl * Np;
+    double dFdr = 0.0, dFds = 0.0, dGdr = 0.0, dGds = 0.0;
+    for (int k = 0; k < Np; k++) dFdr += C.Drw[i * Np + k] * Fc[k];
+    for (int k = 0; k < Np; k++) dFds += C.Dsw[i * Np + k] * Fc[k];
+    for (int k = 0; k < Np; k++) dGdr += C.Drw[i * Np + k] * Gc[k];
+    for (int k = 0; k < Np; k++) dGds += C.Dsw[i * Np + k] * Gc[k];
+    dFdr = 1.0 * dFdr; dFds = 1.0 * dFds; dGdr = 1.0 * dGdr; dGds = 1.0 * dGds;
+    const size_t o = (size_t)Np * c0 + t;
+    const double vol = rxa[o] * dFdr + sxa[o] * dFds + rya[o] * dGdr + sya[o] * dGds;
+    double lift = 0.0;
+    for (int k = 0; k < 3 * Nfp; k++) lift += C.LIFT[i * 3 * Nfp + k] * FL[cl * 3 * Nfp + k];
+    rhsa[o] = -1.0 * lift + 1.0 * vol;
+  }
+}
+
+// advec/src/set_workingQ.h:1-6, one thread per value
+__global__ void k_adv_set_workingQ(long long n, double dt, double frac, const double *q, const double *rk, double *W) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) W[i] = q[i] + dt * frac * rk[i];
+}
+
+// advec/src/update_Q.h:1-8, one thread per value
+__global__ void k_adv_update_Q(long long n, double dt, double *q, const double *k1, const double *k2, const double *k3,
+                               const double *k4, double *W) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  q[i] = q[i] + (1.0 / 6.0) * dt * (k1[i] + 2 * k2[i] + 2 * k3[i] + k4[i]);
+  W[i] = q[i];
 }
 
 __global__ void k_zero(long long n, double *p) {
@@ -528,14 +630,20 @@ double chost(const char *name, bool &ok) {
 // Constants a loop of order N needs; fails with a message naming the first missing one.
 // Which scalar constants a loop reads: the airfoil freestream (bc_*), the vortex parameters, or
 // only gam (geometry, dt, RHS and update loops are shared by both apps).
-enum Need { kFreestream, kVortex, kGamOnly };
+enum Need { kFreestream, kVortex, kGamOnly, kNone, kAdvec };
 
 bool consts_for(int N, bool need_ops, Consts &c, Need need = kGamOnly) {
   const int Np = (N + 1) * (N + 2) / 2, Nfp = N + 1;
   std::memset(&c, 0, sizeof(c));
   bool ok = true;
-  c.gam = chost("gam", ok);
-  if (!ok) return fail("constant gam must be declared with op_decl_const2");
+  if (need == kAdvec) {  // the advection app declares no gam
+    c.velX = chost("velX", ok);
+    c.velY = chost("velY", ok);
+    if (!ok) return fail("constants velX, velY must be declared with op_decl_const2");
+  } else if (need != kNone) {
+    c.gam = chost("gam", ok);
+    if (!ok) return fail("constant gam must be declared with op_decl_const2");
+  }
   if (need == kVortex) {
     c.vortex_x0 = chost("vortex_x0", ok);
     c.vortex_y0 = chost("vortex_y0", ok);
@@ -798,7 +906,7 @@ void op_par_loop_init_grid(char const *name, op_set set, op_arg a0, op_arg a1, o
   for (auto *a : f_args)
     if (!arg_dat(*a, set, true, 3 * Nfp, true, "init_grid face dat")) return;
   Consts C;
-  if (!consts_for(N, true, C)) return;
+  if (!consts_for(N, true, C, kNone)) return;
   Timed t(name ? name : "init_grid");
   DISPATCH_N(N, (k_init_grid<N><<<blocks(set->size, 128), 128, 0, S().stream>>>(
                     set->size, dptr<double>(a0), a0.map->d_data, a0.map->dim, a0.idx, a1.idx, a2.idx,
@@ -888,7 +996,7 @@ void op_par_loop_get_neighbour_q(char const *name, op_set set, op_arg a0, op_arg
     return (void)fail("get_neighbour_q: arguments do not follow src/airfoil.cpp:256-265");
   if (a7.acc != OP_INC || a8.acc != OP_INC) return (void)fail("get_neighbour_q: exteriorQ must be OP_INC");
   Consts C;
-  if (!consts_for(N, false, C)) return;
+  if (!consts_for(N, false, C, kNone)) return;
   Timed t(name ? name : "get_neighbour_q");
   DISPATCH_N(N, (k_get_neighbour_q<N><<<blocks(set->size, 128), 128, 0, S().stream>>>(
                     set->size, dptr<int>(a0), a1.map->d_data, a1.map->dim, a1.idx, a3.idx, dptr<double>(a1),
@@ -993,6 +1101,31 @@ void op_par_loop_update_Q(char const *name, op_set set, op_arg a0, op_arg a1, op
   t.done();
 }
 
+// advec/src/advec.cpp:232-242
+void op_par_loop_advec_rhs(char const *name, op_set set, op_arg a0, op_arg a1, op_arg a2, op_arg a3, op_arg a4,
+                           op_arg a5, op_arg a6, op_arg a7, op_arg a8, op_arg a9) {
+  if (!set) { fail("advec_rhs: null set"); return; }
+  const int Np = a0.dim, N = order_from_np(Np);
+  if (N < 0) { fail("advec_rhs: q dim is not a triangle node count of order 1..6"); return; }
+  const int Nfp = N + 1;
+  if (!arg_dat(a0, set, true, Np, true, "advec_rhs q") || !arg_dat(a1, set, true, 3 * Nfp, true, "advec_rhs exteriorQ") ||
+      !arg_dat(a2, set, true, Np, true, "advec_rhs rx") || !arg_dat(a3, set, true, Np, true, "advec_rhs ry") ||
+      !arg_dat(a4, set, true, Np, true, "advec_rhs sx") || !arg_dat(a5, set, true, Np, true, "advec_rhs sy") ||
+      !arg_dat(a6, set, true, 3 * Nfp, true, "advec_rhs fscale") || !arg_dat(a7, set, true, 3 * Nfp, true, "advec_rhs nx") ||
+      !arg_dat(a8, set, true, 3 * Nfp, true, "advec_rhs ny") || !arg_dat(a9, set, true, Np, true, "advec_rhs rk"))
+    return;
+  if (a9.dat == a0.dat) return (void)fail("advec_rhs: output aliases the input state");
+  Consts C;
+  if (!consts_for(N, true, C, kAdvec)) return;
+  Timed t(name ? name : "advec_rhs");
+  DISPATCH_N(N, (k_advec_rhs<N><<<blocks(set->size, 16), 128, 0, S().stream>>>(
+                    set->size, dptr<double>(a0), dptr<double>(a1), dptr<double>(a2), dptr<double>(a3),
+                    dptr<double>(a4), dptr<double>(a5), dptr<double>(a6), dptr<double>(a7), dptr<double>(a8),
+                    dptr<double>(a9), C)));
+  if (!ck(cudaGetLastError(), "advec_rhs launch")) return;
+  t.done();
+}
+
 // vortex/src/vortex.cpp:308-318 (the per-cell error sums are added to the four globals, OP_INC)
 void op_par_loop_l2_error(char const *name, op_set set, op_arg a0, op_arg a1, op_arg a2, op_arg a3, op_arg a4,
                           op_arg a5, op_arg a6, op_arg a7, op_arg a8) {
@@ -1044,6 +1177,7 @@ void op2_gb300_par_loop(char const *kernel, char const *name, op_set set, int na
                             a[12], a[13], a[14], a[15], a[16], a[17]);
   } else if (k == "set_ic") {
     if (nargs == 5) op_par_loop_set_ic(name, set, a[0], a[1], a[2], a[3], a[4]);
+    else if (nargs == 4) op_par_loop_set_ic(name, set, a[0], a[1], a[2], a[3]);
     else if (need(2)) op_par_loop_set_ic(name, set, a[0], a[1]);
   } else if (k == "neighbour_zero") {
     if (need(1)) op_par_loop_neighbour_zero(name, set, a[0]);
@@ -1055,15 +1189,20 @@ void op2_gb300_par_loop(char const *kernel, char const *name, op_set set, int na
     else if (need(9)) op_par_loop_get_neighbour_q(name, set, a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], a[8]);
   } else if (k == "get_bedge_q") {
     if (nargs == 9) op_par_loop_get_bedge_q(name, set, a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], a[8]);
+    else if (nargs == 8) op_par_loop_get_bedge_q(name, set, a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7]);
     else if (need(6)) op_par_loop_get_bedge_q(name, set, a[0], a[1], a[2], a[3], a[4], a[5]);
   } else if (k == "l2_error") {
     if (need(9)) op_par_loop_l2_error(name, set, a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], a[8]);
   } else if (k == "euler_rhs") {
     if (need(10)) op_par_loop_euler_rhs(name, set, a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], a[8], a[9]);
   } else if (k == "set_workingQ") {
-    if (need(6)) op_par_loop_set_workingQ(name, set, a[0], a[1], a[2], a[3], a[4], a[5]);
+    if (nargs == 5) op_par_loop_set_workingQ(name, set, a[0], a[1], a[2], a[3], a[4]);
+    else if (need(6)) op_par_loop_set_workingQ(name, set, a[0], a[1], a[2], a[3], a[4], a[5]);
   } else if (k == "update_Q") {
-    if (need(6)) op_par_loop_update_Q(name, set, a[0], a[1], a[2], a[3], a[4], a[5]);
+    if (nargs == 7) op_par_loop_update_Q(name, set, a[0], a[1], a[2], a[3], a[4], a[5], a[6]);
+    else if (need(6)) op_par_loop_update_Q(name, set, a[0], a[1], a[2], a[3], a[4], a[5]);
+  } else if (k == "advec_rhs") {
+    if (need(10)) op_par_loop_advec_rhs(name, set, a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], a[8], a[9]);
   } else {
     fail("unknown user kernel " + k);
   }
@@ -1104,7 +1243,110 @@ void op_par_loop_get_neighbour_q(char const *name, op_set set, op_arg a0, op_arg
   if (!set) { fail("get_neighbour_q: null set"); return; }
   if (!arg_dat(a1, set, false, 2, true, "get_neighbour_q n0") || !arg_dat(a2, set, false, 2, true, "get_neighbour_q n1"))
     return;
-  op_par_loop_get_neighbour_q(name, set, a0, a3, a4, a5, a6, a7, a8, a9, a10);
+  const int Nq = order_from_np(a7.dim);
+  if (Nq < 0 || a9.dim != 3 * (Nq + 1)) {  // the vortex app's (4 variables per node)
+    op_par_loop_get_neighbour_q(name, set, a0, a3, a4, a5, a6, a7, a8, a9, a10);
+    return;
+  }
+  // the advection app's (advec/src/advec.cpp:207-218): one value per node
+  const int N = Nq, Np = a7.dim, Nfp = N + 1;
+  if (!arg_dat(a0, set, true, 2, false, "get_neighbour_q edgeNum")) return;
+  if (!arg_dat(a3, set, false, 3, true, "get_neighbour_q nodeX L") || !arg_dat(a4, set, false, 3, true, "get_neighbour_q nodeY L") ||
+      !arg_dat(a5, set, false, 3, true, "get_neighbour_q nodeX R") || !arg_dat(a6, set, false, 3, true, "get_neighbour_q nodeY R") ||
+      !arg_dat(a7, set, false, Np, true, "get_neighbour_q q L") || !arg_dat(a8, set, false, Np, true, "get_neighbour_q q R") ||
+      !arg_dat(a9, set, false, 3 * Nfp, true, "get_neighbour_q ext L") || !arg_dat(a10, set, false, 3 * Nfp, true, "get_neighbour_q ext R"))
+    return;
+  const op_arg *all[8] = {&a3, &a4, &a5, &a6, &a7, &a8, &a9, &a10};
+  for (auto *a : all)
+    if (a->map != a3.map) return (void)fail("get_neighbour_q: all indirect args must use one map");
+  if (a3.idx != a4.idx || a5.idx != a6.idx || a7.idx != a3.idx || a9.idx != a3.idx || a8.idx != a5.idx ||
+      a10.idx != a5.idx || a3.dat != a5.dat || a4.dat != a6.dat || a7.dat != a8.dat || a9.dat != a10.dat)
+    return (void)fail("get_neighbour_q: arguments do not follow advec/src/advec.cpp:207-218");
+  if (a9.acc != OP_INC || a10.acc != OP_INC) return (void)fail("get_neighbour_q: exteriorQ must be OP_INC");
+  Consts C;
+  if (!consts_for(N, false, C, kNone)) return;
+  Timed t(name ? name : "get_neighbour_q");
+  DISPATCH_N(N, (k_adv_get_neighbour_q<N><<<blocks(set->size, 128), 128, 0, S().stream>>>(
+                    set->size, dptr<int>(a0), a3.map->d_data, a3.map->dim, a3.idx, a5.idx, dptr<double>(a3),
+                    dptr<double>(a4), dptr<double>(a7), dptr<double>(a9), C)));
+  if (!ck(cudaGetLastError(), "get_neighbour_q launch")) return;
+  t.done();
+}
+
+// advec/src/advec.cpp:191-195: set_ic(x, y, q, workingQ), one value per node
+void op_par_loop_set_ic(char const *name, op_set set, op_arg a0, op_arg a1, op_arg a2, op_arg a3) {
+  if (!set) { fail("set_ic: null set"); return; }
+  const int Np = a0.dim;
+  if (order_from_np(Np) < 0) { fail("set_ic: x dim is not a triangle node count of order 1..6"); return; }
+  if (!arg_dat(a0, set, true, Np, true, "set_ic x") || !arg_dat(a1, set, true, Np, true, "set_ic y") ||
+      !arg_dat(a2, set, true, Np, true, "set_ic q") || !arg_dat(a3, set, true, Np, true, "set_ic workingQ"))
+    return;
+  Timed tm(name ? name : "set_ic");
+  const long long n = (long long)set->size * Np;
+  k_adv_set_ic<<<blocks(n, 256), 256, 0, S().stream>>>(n, dptr<double>(a0), dptr<double>(a1), dptr<double>(a2),
+                                                       dptr<double>(a3));
+  if (!ck(cudaGetLastError(), "set_ic launch")) return;
+  tm.done();
+}
+
+// advec/src/advec.cpp:221-229: get_bedge_q(bedgeNum, n0, n1, nodeX, nodeY, x, y, exteriorQ)
+void op_par_loop_get_bedge_q(char const *name, op_set set, op_arg a0, op_arg a1, op_arg a2, op_arg a3, op_arg a4,
+                             op_arg a5, op_arg a6, op_arg a7) {
+  if (!set) { fail("get_bedge_q: null set"); return; }
+  const int Np = a5.dim, N = order_from_np(Np);
+  if (N < 0) { fail("get_bedge_q: x dim is not a triangle node count of order 1..6"); return; }
+  const int Nfp = N + 1;
+  if (!arg_dat(a0, set, true, 1, false, "get_bedge_q bedgeNum") || !arg_dat(a1, set, false, 2, true, "get_bedge_q n0") ||
+      !arg_dat(a2, set, false, 2, true, "get_bedge_q n1") || !arg_dat(a3, set, false, 3, true, "get_bedge_q nodeX") ||
+      !arg_dat(a4, set, false, 3, true, "get_bedge_q nodeY") || !arg_dat(a5, set, false, Np, true, "get_bedge_q x") ||
+      !arg_dat(a6, set, false, Np, true, "get_bedge_q y") || !arg_dat(a7, set, false, 3 * Nfp, true, "get_bedge_q ext"))
+    return;
+  if (a5.map != a7.map || a5.idx != a7.idx) return (void)fail("get_bedge_q: x and exteriorQ must use one map column");
+  if (a7.acc != OP_INC) return (void)fail("get_bedge_q: exteriorQ must be OP_INC");
+  Timed tm(name ? name : "get_bedge_q");
+  DISPATCH_N(N, (k_adv_get_bedge_q<N><<<blocks(set->size, 128), 128, 0, S().stream>>>(
+                    set->size, dptr<int>(a0), a7.map->d_data, a7.map->dim, a7.idx, dptr<double>(a7))));
+  if (!ck(cudaGetLastError(), "get_bedge_q launch")) return;
+  tm.done();
+}
+
+// advec/src/advec.cpp:245-250: set_workingQ(dt, q, rk, rk_frac, workingQ)
+void op_par_loop_set_workingQ(char const *name, op_set set, op_arg a0, op_arg a1, op_arg a2, op_arg a3, op_arg a4) {
+  if (!set) { fail("set_workingQ: null set"); return; }
+  const int dim = a1.dim;
+  if (!arg_gbl(a0, 1, true, "set_workingQ dt") || !arg_dat(a1, set, true, dim, true, "set_workingQ q") ||
+      !arg_dat(a2, set, true, dim, true, "set_workingQ rk") || !arg_gbl(a3, 1, true, "set_workingQ rk_frac") ||
+      !arg_dat(a4, set, true, dim, true, "set_workingQ W"))
+    return;
+  double dt, frac;
+  std::memcpy(&dt, a0.data, 8);
+  std::memcpy(&frac, a3.data, 8);
+  Timed tm(name ? name : "set_workingQ");
+  const long long n = (long long)set->size * dim;
+  k_adv_set_workingQ<<<blocks(n, 256), 256, 0, S().stream>>>(n, dt, frac, dptr<double>(a1), dptr<double>(a2),
+                                                             dptr<double>(a4));
+  if (!ck(cudaGetLastError(), "set_workingQ launch")) return;
+  tm.done();
+}
+
+// advec/src/advec.cpp:253-260: update_Q(dt, q, rk1, rk2, rk3, rk4, workingQ)
+void op_par_loop_update_Q(char const *name, op_set set, op_arg a0, op_arg a1, op_arg a2, op_arg a3, op_arg a4,
+                          op_arg a5, op_arg a6) {
+  if (!set) { fail("update_Q: null set"); return; }
+  const int dim = a1.dim;
+  if (!arg_gbl(a0, 1, true, "update_Q dt") || !arg_dat(a1, set, true, dim, true, "update_Q q") ||
+      !arg_dat(a2, set, true, dim, true, "update_Q k1") || !arg_dat(a3, set, true, dim, true, "update_Q k2") ||
+      !arg_dat(a4, set, true, dim, true, "update_Q k3") || !arg_dat(a5, set, true, dim, true, "update_Q k4") ||
+      !arg_dat(a6, set, true, dim, true, "update_Q W"))
+    return;
+  double dt;
+  std::memcpy(&dt, a0.data, 8);
+  Timed tm(name ? name : "update_Q");
+  const long long n = (long long)set->size * dim;
+  k_adv_update_Q<<<blocks(n, 256), 256, 0, S().stream>>>(n, dt, dptr<double>(a1), dptr<double>(a2), dptr<double>(a3),
+                                                         dptr<double>(a4), dptr<double>(a5), dptr<double>(a6));
+  if (!ck(cudaGetLastError(), "update_Q launch")) return;
+  tm.done();
 }
 
 // vortex/src/vortex.cpp:249-260: get_bedge_q(bedgeNum, n0, n1, nodeX, nodeY, x, y, t, exteriorQ)

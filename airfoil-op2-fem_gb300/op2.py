@@ -33,11 +33,11 @@ class op_arg(C.Structure):
                 ("type", C.c_char_p)]
 
 
-# argument counts per loop: the airfoil app's, and the vortex app's where they differ
-# (vortex/src/vortex.cpp:210-318)
-_LOOPS = {"init_grid": (18,), "set_ic": (2, 5), "neighbour_zero": (1,), "calc_dt": (3,),
-          "get_neighbour_q": (9, 11), "get_bedge_q": (6, 9), "euler_rhs": (10,), "set_workingQ": (6,),
-          "update_Q": (6,), "l2_error": (9,)}
+# argument counts per loop: the airfoil app's, and the vortex and advection apps' where they
+# differ (vortex/src/vortex.cpp:210-318, advec/src/advec.cpp:191-260)
+_LOOPS = {"init_grid": (18,), "set_ic": (2, 4, 5), "neighbour_zero": (1,), "calc_dt": (3,),
+          "get_neighbour_q": (9, 11), "get_bedge_q": (6, 8, 9), "euler_rhs": (10,), "set_workingQ": (5, 6),
+          "update_Q": (6, 7), "l2_error": (9,), "advec_rhs": (10,)}
 _configured = False
 _keep = []  # host buffers whose addresses op_arg_gbl hands to the library
 
@@ -166,3 +166,4 @@ op_par_loop_euler_rhs = _loop("euler_rhs")
 op_par_loop_set_workingQ = _loop("set_workingQ")
 op_par_loop_update_Q = _loop("update_Q")
 op_par_loop_l2_error = _loop("l2_error")
+op_par_loop_advec_rhs = _loop("advec_rhs")

@@ -21,8 +21,10 @@
  *    them return silently with the message in op2_gb300_last_error().
  *
  * The loop kernels of the airfoil application are provided with the argument
- * lists of src/airfoil.cpp:204-331, and those of the vortex application
- * (vortex/src/vortex.cpp:210-318) as C++ overloads and op_par_loop_l2_error.
+ * lists of src/airfoil.cpp:204-331, those of the vortex application
+ * (vortex/src/vortex.cpp:210-318) as C++ overloads and op_par_loop_l2_error, and
+ * those of the scalar advection application (advec/src/advec.cpp:191-260) as C++
+ * overloads and op_par_loop_advec_rhs.
  *
  * For C++ callers that include the reference's generated declarations
  * (src/airfoil_op.cpp:17-94 declare the loops with C++ linkage unless
@@ -104,6 +106,10 @@ void op_par_loop_update_Q(char const *name, op_set set, op_arg a0, op_arg a1, op
  * per-cell sums are added to the globals, as a device backend's reduction does. */
 void op_par_loop_l2_error(char const *name, op_set set, op_arg a0, op_arg a1, op_arg a2, op_arg a3,
                           op_arg a4, op_arg a5, op_arg a6, op_arg a7, op_arg a8);
+/* advec/src/advec.cpp:232-242: advec_rhs(q, exteriorQ, rx, ry, sx, sy, fscale, nx, ny, rk), one
+ * value per node; reads the constants velX, velY. */
+void op_par_loop_advec_rhs(char const *name, op_set set, op_arg a0, op_arg a1, op_arg a2, op_arg a3,
+                           op_arg a4, op_arg a5, op_arg a6, op_arg a7, op_arg a8, op_arg a9);
 
 /* Extensions (no OP2 counterpart). */
 const char *op2_gb300_last_error(void);
@@ -133,6 +139,18 @@ void op_par_loop_get_neighbour_q(char const *name, op_set set, op_arg a0, op_arg
                                  op_arg a4, op_arg a5, op_arg a6, op_arg a7, op_arg a8, op_arg a9, op_arg a10);
 void op_par_loop_get_bedge_q(char const *name, op_set set, op_arg a0, op_arg a1, op_arg a2, op_arg a3, op_arg a4,
                              op_arg a5, op_arg a6, op_arg a7, op_arg a8);
+/* The advection app's loops (advec/src/advec.cpp:191-260), one value per node, as C++ overloads:
+ *   set_ic(x, y, q, workingQ)                                        advec/src/set_ic.h:3-10
+ *   get_neighbour_q: the 11-argument overload above, taken when q has Np values per cell
+ *   get_bedge_q(bedgeNum, n0, n1, nodeX, nodeY, x, y, exteriorQ)     advec/src/get_bedge_q.h:3-13
+ *   set_workingQ(dt, q, rk, rk_frac, workingQ)                       advec/src/set_workingQ.h:1-6
+ *   update_Q(dt, q, rk1, rk2, rk3, rk4, workingQ)                    advec/src/update_Q.h:1-8 */
+void op_par_loop_set_ic(char const *name, op_set set, op_arg a0, op_arg a1, op_arg a2, op_arg a3);
+void op_par_loop_get_bedge_q(char const *name, op_set set, op_arg a0, op_arg a1, op_arg a2, op_arg a3, op_arg a4,
+                             op_arg a5, op_arg a6, op_arg a7);
+void op_par_loop_set_workingQ(char const *name, op_set set, op_arg a0, op_arg a1, op_arg a2, op_arg a3, op_arg a4);
+void op_par_loop_update_Q(char const *name, op_set set, op_arg a0, op_arg a1, op_arg a2, op_arg a3, op_arg a4,
+                          op_arg a5, op_arg a6);
 #endif
 
 #endif

@@ -316,3 +316,124 @@ def test_dropin_vortex_rejects_missing_constants(op2, omesh, oops):
                                op2.op_arg_dat(x, -1, None, 10, "double", op2.OP_READ),
                                op2.op_arg_dat(q, -1, None, 40, "double", op2.OP_WRITE),
                                op2.op_arg_dat(q, -1, None, 40, "double", op2.OP_WRITE))
+
+
+class Advec:
+    """advec/src/advec.cpp:120-260 on the drop-in: one value per node, classical RK4, dt fixed."""
+
+    def __init__(self, op2, m, ops, vel, dt, q0=None):
+        o = self.op2 = op2
+        N = int(ops["N"])
+        Np, Nfp = (N + 1) * (N + 2) // 2, N + 1
+        self.Np, self.Nfp, self.dt, self.t = Np, Nfp, dt, 0.0
+        o.op_init(0)
+        K = self.K = m["cell2nodes"].shape[0]
+        nodes = o.op_decl_set(m["coords"].shape[0], "nodes")
+        self.cells = cells = o.op_decl_set(K, "cells")
+        self.edges = o.op_decl_set(m["edge2cells"].shape[0], "edges")
+        self.bedges = o.op_decl_set(m["bedge2cell"].shape[0], "bedges")
+        cell2nodes = o.op_decl_map(cells, nodes, 3, m["cell2nodes"], "cell2nodes")
+        self.edge2nodes = o.op_decl_map(self.edges, nodes, 2, m["edge2nodes"], "edge2nodes")
+        self.edge2cells = o.op_decl_map(self.edges, cells, 2, m["edge2cells"], "edge2cells")
+        self.bedge2nodes = o.op_decl_map(self.bedges, nodes, 2, m["bedge2nodes"], "bedge2nodes")
+        self.bedge2cells = o.op_decl_map(self.bedges, cells, 1, m["bedge2cell"], "bedge2cells")
+        self.nc = nc = o.op_decl_dat(nodes, 2, "double", m["coords"], "node_coords")
+        d = {}
+        for name, dim in (("nodeX", 3), ("nodeY", 3), ("x", Np), ("y", Np), ("xr", Np), ("yr", Np),
+                          ("xs", Np), ("ys", Np), ("rx", Np), ("ry", Np), ("sx", Np), ("sy", Np),
+                          ("nx", 3 * Nfp), ("ny", 3 * Nfp), ("fscale", 3 * Nfp), ("rk1", Np), ("rk2", Np),
+                          ("rk3", Np), ("rk4", Np), ("exteriorQ", 3 * Nfp)):
+            d[name] = (o.op_decl_dat(cells, dim, "double", np.zeros(K * dim), name), dim)
+        init = np.zeros(K * Np) if q0 is None else q0
+        d["q"] = (o.op_decl_dat(cells, Np, "double", init, "q"), Np)
+        d["workingQ"] = (o.op_decl_dat(cells, Np, "double", init, "workingQ"), Np)
+        self.d = d
+        self.edgeNum = o.op_decl_dat(self.edges, 2, "int", m["edgeNum"], "edgeNum")
+        self.bedgeNum = o.op_decl_dat(self.bedges, 1, "int", m["bedgeNum"], "bedgeNum")
+        o.op_decl_const2("velX", 1, "double", vel[0])
+        o.op_decl_const2("velY", 1, "double", vel[1])
+        o.op_decl_const2("ones", Np, "double", np.ones(Np))
+        for k in ("r", "s", "Dr", "Ds", "Drw", "Dsw", "LIFT"):
+            o.op_decl_const2(k, np.asarray(ops[k]).size, "double", np.asarray(ops[k]).ravel())
+        o.op_decl_const2("FMASK", 3 * Nfp, "int", np.asarray(ops["FMASK"], dtype=np.int32))
+        A = self.A
+        o.op_par_loop_init_grid("init_grid", cells, *[o.op_arg_dat(nc, k, cell2nodes, 2, "double", o.OP_READ)
+                                                      for k in range(3)],
+                                *[A(n, o.OP_WRITE) for n in ("nodeX", "nodeY", "x", "y", "xr", "yr", "xs", "ys",
+                                                             "rx", "ry", "sx", "sy", "nx", "ny", "fscale")])
+        if q0 is None:
+            o.op_par_loop_set_ic("set_ic", cells, A("x", o.OP_READ), A("y", o.OP_READ), A("q", o.OP_WRITE),
+                                 A("workingQ", o.OP_WRITE))
+
+    def A(self, name, acc, idx=-1, mp=None):
+        dat, dim = self.d[name]
+        return self.op2.op_arg_dat(dat, idx, mp, dim, "double", acc)
+
+    def fetch(self, name):
+        dat, dim = self.d[name]
+        out = np.empty(self.K * dim)
+        self.op2.op_fetch_data(dat, out)
+        return out
+
+    def run(self, iters):
+        o, A, e2c, b2c, nc = self.op2, self.A, self.edge2cells, self.bedge2cells, self.nc
+        dt = np.array([self.dt])
+        rk_frac = (0.5, 0.5, 1.0)
+        for _ in range(iters):
+            for j in range(4):
+                o.op_par_loop_neighbour_zero("neighbour_zero", self.cells, A("exteriorQ", o.OP_WRITE))
+                o.op_par_loop_get_neighbour_q(
+                    "get_neighbour_q", self.edges, o.op_arg_dat(self.edgeNum, -1, None, 2, "int", o.OP_READ),
+                    o.op_arg_dat(nc, 0, self.edge2nodes, 2, "double", o.OP_READ),
+                    o.op_arg_dat(nc, 1, self.edge2nodes, 2, "double", o.OP_READ),
+                    A("nodeX", o.OP_READ, 0, e2c), A("nodeY", o.OP_READ, 0, e2c),
+                    A("nodeX", o.OP_READ, 1, e2c), A("nodeY", o.OP_READ, 1, e2c),
+                    A("workingQ", o.OP_READ, 0, e2c), A("workingQ", o.OP_READ, 1, e2c),
+                    A("exteriorQ", o.OP_INC, 0, e2c), A("exteriorQ", o.OP_INC, 1, e2c))
+                o.op_par_loop_get_bedge_q(
+                    "get_bedge_q", self.bedges, o.op_arg_dat(self.bedgeNum, -1, None, 1, "int", o.OP_READ),
+                    o.op_arg_dat(nc, 0, self.bedge2nodes, 2, "double", o.OP_READ),
+                    o.op_arg_dat(nc, 1, self.bedge2nodes, 2, "double", o.OP_READ),
+                    A("nodeX", o.OP_READ, 0, b2c), A("nodeY", o.OP_READ, 0, b2c),
+                    A("x", o.OP_READ, 0, b2c), A("y", o.OP_READ, 0, b2c), A("exteriorQ", o.OP_INC, 0, b2c))
+                o.op_par_loop_advec_rhs(
+                    "advec_rhs", self.cells, A("workingQ", o.OP_READ), A("exteriorQ", o.OP_READ),
+                    A("rx", o.OP_READ), A("ry", o.OP_READ), A("sx", o.OP_READ), A("sy", o.OP_READ),
+                    A("fscale", o.OP_READ), A("nx", o.OP_READ), A("ny", o.OP_READ), A("rk%d" % (j + 1), o.OP_WRITE))
+                if j != 3:
+                    o.op_par_loop_set_workingQ(
+                        "set_workingQ", self.cells, o.op_arg_gbl(dt, 1, "double", o.OP_READ), A("q", o.OP_READ),
+                        A("rk%d" % (j + 1), o.OP_READ), o.op_arg_gbl(np.array([rk_frac[j]]), 1, "double", o.OP_READ),
+                        A("workingQ", o.OP_WRITE))
+            o.op_par_loop_update_Q("update_Q", self.cells, o.op_arg_gbl(dt, 1, "double", o.OP_READ),
+                                   A("q", o.OP_RW), A("rk1", o.OP_READ), A("rk2", o.OP_READ), A("rk3", o.OP_READ),
+                                   A("rk4", o.OP_READ), A("workingQ", o.OP_WRITE))
+            self.t += self.dt
+
+
+@pytest.mark.parametrize("N", [2, 4])
+def test_dropin_advec_bitwise_equals_oracle(op2, orc, oops, omesh, N):
+    """The advection app's loops: geometry bit-exact, set_ic to the last bits of exp, and, from
+    the same initial state, q and all four stage right-hand sides bit for bit after 8 RK4 steps."""
+    m = omesh.vortex_square(12, 0.0, 1.0)
+    ops, vel, dt = oops.operators(N), (0.8, -0.35), 1e-3
+    o = orc.Advection(m, ops, *vel)
+    o.init(dt)
+    a = Advec(op2, m, ops, vel, dt)
+    for name in ("x", "y", "rx", "sy", "nx", "fscale"):
+        assert np.array_equal(a.fetch(name), o.get(name)), name
+    assert orc.rel_l2(a.fetch("q"), o.get("q")) < 1e-15
+    b = Advec(op2, m, ops, vel, dt, q0=o.get("q"))
+    b.run(8)
+    o.run(8, nthreads=1)
+    assert np.array_equal(b.fetch("q"), o.get("q"))
+    for k in range(1, 5):
+        assert np.array_equal(b.fetch("rk%d" % k), o.get("rk%d" % k)), k
+
+
+def test_dropin_advec_golden(op2, orc, oops, golden_advec):
+    """The reference's advection mesh and run (advec/grid.vtk, 100 RK4 steps) through the drop-in."""
+    g, m = golden_advec
+    a = Advec(op2, m, oops.operators(4), (1.0, 1.0), float(g["dt"]))
+    a.run(100)
+    assert orc.rel_l2(a.fetch("q"), g["q100"]) < 1e-11
