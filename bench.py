@@ -435,6 +435,7 @@ def main():
     ap.add_argument("--batched-steps", type=int, default=20)
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-advection", action="store_true")
+    ap.add_argument("--adjoint-steps", type=int, default=2000)
     ap.add_argument("--advection-steps", type=int, default=200)
     ap.add_argument("--large-vortex", action="store_true",
                     help="also run the large vortex convergence + 16-instance batched beta gradient (~1 min)")
@@ -578,7 +579,8 @@ def main():
         line["batched"] = batched_measure(pkg, args.batched_steps)
         line["batched"]["small_instances"] = batched_small_measure(pkg)
     if not args.no_adjoint:
-        line["adjoint"] = adjoint_measure(pkg)
+        steps = args.adjoint_steps
+        line["adjoint"] = adjoint_measure(pkg, nsteps=steps, navg=min(100, max(1, steps // 2)))
     if not args.no_advection:
         line["advection"] = advection_measure(pkg, steps=args.advection_steps)
         line["mesh_setup"] = mesh_setup_measure(pkg)
