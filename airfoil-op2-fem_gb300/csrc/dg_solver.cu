@@ -353,11 +353,11 @@ __global__ void __launch_bounds__(32 * np_of(N)) elem_kernel(const Inst d, const
       const double p = P.gm1 * fma(-0.5, fma(w[1], u, w[2] * v), w[3]);
       const double ep = w[3] + p;
       const double U = fma(rx, u, ry * v), V = fma(sx, u, sy * v);
-      fr0 = fma(rx, w[1], ry * w[2]);
+      fr0 = w[0] * U;  // = rx w1 + ry w2 (U = rx u + ry v), one multiply
       fr1 = fma(w[1], U, rx * p);
       fr2 = fma(w[2], U, ry * p);
       fr3 = U * ep;
-      fs0 = fma(sx, w[1], sy * w[2]);
+      fs0 = w[0] * V;
       fs1 = fma(w[1], V, sx * p);
       fs2 = fma(w[2], V, sy * p);
       fs3 = V * ep;
@@ -435,11 +435,11 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
       const double p = P.gm1 * fma(-0.5, fma(w[1], u, w[2] * v), w[3]);
       const double ep = w[3] + p;
       const double U = fma(rx, u, ry * v), V = fma(sx, u, sy * v);
-      fr0 = fma(rx, w[1], ry * w[2]);
+      fr0 = w[0] * U;  // = rx w1 + ry w2 (U = rx u + ry v), one multiply
       fr1 = fma(w[1], U, rx * p);
       fr2 = fma(w[2], U, ry * p);
       fr3 = U * ep;
-      fs0 = fma(sx, w[1], sy * w[2]);
+      fs0 = w[0] * V;
       fs1 = fma(w[1], V, sx * p);
       fs2 = fma(w[2], V, sy * p);
       fs3 = V * ep;
