@@ -14,6 +14,7 @@ struct Phys {
   double gam, gm1;               // gamma, gamma - 1
   double rinf, uinf, vinf, pinf, einf;  // freestream (src/airfoil.cpp:79-99)
   double vx0, vy0, vbeta;        // isentropic vortex centre and strength
+  float gamf, gm1f;              // gamma, gamma - 1 in single precision (the dt estimate)
 };
 
 __device__ __forceinline__ double rcp(double x) { return __drcp_rn(x); }

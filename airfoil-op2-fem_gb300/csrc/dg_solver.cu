@@ -19,7 +19,8 @@
 // Data layout in HBM (K cells, order N, Np=(N+1)(N+2)/2, Nfp=N+1):
 //   q, W   [K][Np][4] doubles (the reference's AoS, src/airfoil.cpp:171)
 //   flux   [K][3][Nfp][4]
-//   geo    [K][16]: rx, ry, sx, sy, then (nx, ny, fscale) of faces 0..2, J, 2 pad
+//   geo    [K][16]: rx, ry, sx, sy, then (nx, ny, fscale) of faces 0..2, J, and the three
+//                    fscale again as floats in the last 16 bytes (the dt estimate)
 //   edges  int4 {cL, cR, fL | fR << 2 | reverse << 4, 0};  bedges int4 {cell, face, type, 0}
 //   bxy    [nB][Nfp][2] boundary face-node coordinates (vortex boundary)
 #include <cuda_runtime.h>
@@ -252,20 +253,20 @@ __device__ __forceinline__ void stage_combine(const Inst &d, const int stage, co
     // those within 1e-4 of the block's estimated maximum are evaluated in FP64.  The FP32
     // estimate is within ~1e-6 of the FP64 value, so the block's true maximum is always a
     // candidate and the result equals the all-FP64 maximum.  (Measured cost of the whole
-    // reduction on the K=32768, N=3 benchmark: 8.4 us of a 90 us stage-2 launch.)
+    // reduction on the K=32768, N=3 benchmark: 6.2 us of an 86 us stage-2 launch.)
     __shared__ float s_wmax[32];
     __shared__ int s_ncand;
     const int fa = active ? c_dtf[N][2 * i] : -1, fb = active ? c_dtf[N][2 * i + 1] : -1;
-    const double *ge = d.geo + (size_t)(live ? e : 0) * 16 + 6;
+    const double *ge = d.geo + (size_t)(live ? e : 0) * 16;
     float est = 0.0f;
-    double fs = 0.0;
     if (live && fa >= 0) {
-      fs = fb >= 0 ? fmax(ge[3 * fa], ge[3 * fb]) : ge[3 * fa];
+      const float *gf = reinterpret_cast<const float *>(ge + 14);  // fscale per face, single precision
+      const float fsf = fb >= 0 ? fmaxf(gf[fa], gf[fb]) : gf[fa];
       const float rho = (float)n0, ir = 1.0f / rho, u = (float)n1 * ir, v = (float)n2 * ir;
       const float v2 = u * u + v * v;
-      const float p = (float)P.gm1 * ((float)n3 - 0.5f * rho * v2);
-      const float cs = sqrtf(fabsf((float)P.gam * p * ir));
-      est = ((N + 1) * (N + 1) * 0.5f) * (sqrtf(v2) + cs) * (float)fs;
+      const float p = P.gm1f * ((float)n3 - 0.5f * rho * v2);
+      const float cs = sqrtf(fabsf(P.gamf * p * ir));
+      est = ((N + 1) * (N + 1) * 0.5f) * (sqrtf(v2) + cs) * fsf;
       if (!(est == est) || est > 3.0e38f) est = 3.0e38f;  // non-finite: always a candidate
     }
     if (active) {
@@ -286,7 +287,8 @@ __device__ __forceinline__ void stage_combine(const Inst &d, const int stage, co
       if (est >= bm * 0.9999f) {
         const int slot = atomicAdd(&s_ncand, 1);
         double *c = cand + 5 * slot;
-        c[0] = n0; c[1] = n1; c[2] = n2; c[3] = n3; c[4] = fs;
+        c[0] = n0; c[1] = n1; c[2] = n2; c[3] = n3;
+        c[4] = fb >= 0 ? fmax(ge[6 + 3 * fa], ge[6 + 3 * fb]) : ge[6 + 3 * fa];
       }
     }
     __syncthreads();
@@ -575,7 +577,12 @@ __global__ void geometry_kernel(int K, const double *coords, const int *cells, d
     g[6 + 3 * f] = __ddiv_rn(sJ, J);
   }
   g[13] = J;  // cell Jacobian: face arc-length element sJ = fscale * J
-  g[14] = g[15] = 0.0;
+  // fscale of the three faces again in single precision (the dt estimate), in the padding
+  float *gf = reinterpret_cast<float *>(g + 14);
+  gf[0] = (float)g[6];
+  gf[1] = (float)g[9];
+  gf[2] = (float)g[12];
+  gf[3] = 0.0f;
 }
 
 // Node position with the operation order of src/init_grid.h:19-54 (cblas dcopy/daxpy/dscal).
@@ -976,6 +983,8 @@ int Solver::create(const Config &c, const Mesh &m, std::string &err) {
   const double gam = c.gam;
   d.P.gam = gam;
   d.P.gm1 = gam - 1.0;
+  d.P.gamf = (float)gam;
+  d.P.gm1f = (float)(gam - 1.0);
   // Freestream as src/airfoil.cpp:79-99.
   double u, v, e;
   if (c.alpha_deg != 0.0) {
@@ -1234,6 +1243,8 @@ int rhs_noalloc(const Config &c, int K, int nE, int nB, const double *W, const d
   }
   d.P.gam = gam;
   d.P.gm1 = gam - 1.0;
+  d.P.gamf = (float)gam;
+  d.P.gm1f = (float)(gam - 1.0);
   d.P.rinf = c.rho_inf;
   d.P.uinf = u;
   d.P.vinf = v;
