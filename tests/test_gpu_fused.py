@@ -240,3 +240,18 @@ def test_programmatic_launch_equals_stream_order(pkg, omesh, N):
     assert np.array_equal(res[0][0], res[1][0])
     assert np.array_equal(res[0][1], res[1][1])
     assert res[0][2] == res[1][2]
+
+
+@pytest.mark.parametrize("cells", [[[0, 1, 2]], [[0, 1, 2], [0, 2, 3]]])
+def test_tiny_meshes_match_oracle(pkg, orc, oops, omesh, cells):
+    """One and two cells (every face, or all but one, on the boundary; grids of one block)."""
+    coords = np.array([[0.0, 0.0], [1.0, 0.0], [1.0, 1.0], [0.0, 1.0]])[: max(max(c) for c in cells) + 1]
+    m = omesh.build_tables(coords, np.array(cells, dtype=np.int32))
+    m["bedge_type"] = np.array([2, 0, 1, 2][: len(m["bedge2cell"])], dtype=np.int32)
+    s, o = solver_and_oracle(pkg, orc, oops, m, 3, 0.3, mach=0.3, alpha_deg=5.0)
+    s.record_dt(10)
+    s.run(10)
+    s.sync()
+    dts = o.run(10, nthreads=1)
+    assert orc.rel_l2(s.get("q"), o.get("q")) < 1e-12
+    assert np.abs(s.dt_history(10) / dts - 1).max() < 1e-12
