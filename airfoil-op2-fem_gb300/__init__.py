@@ -450,6 +450,7 @@ class LiftObjective:
 
     def __init__(self, mesh, cfg, nsteps, navg, checkpoint_every=50):
         self.mesh, self.cfg, self.nsteps = mesh, cfg, nsteps
+        self.param = cfg.vortex_beta if cfg.app == APP_VORTEX else cfg.alpha_deg
         self.K = mesh.size("cells")
         self.nq = self.K * (cfg.N + 1) * (cfg.N + 2) // 2 * 4
         h = C.c_void_p()
@@ -504,6 +505,30 @@ class LiftObjective:
     @property
     def stream(self):
         return lib().dg_adjoint_stream(self.h)
+
+
+def torch_objective(obj):
+    """A torch.autograd.Function over a LiftObjective: f(p) -> J, with p the objective's scalar
+    parameter (alpha in degrees for the airfoil, beta for the vortex) as a 0-d float64 tensor.
+    forward() runs the recording forward solve at p; backward() the discrete adjoint, so
+    torch.autograd composes it with other torch code.  The solve itself stays in the library;
+    torch only carries the scalars."""
+    import torch
+
+    class _Objective(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, p):
+            if float(p) != obj.param:
+                raise ValueError("the objective was created at parameter %g" % obj.param)
+            J = obj.forward()
+            return torch.tensor(J, dtype=torch.float64, device=p.device)
+
+        @staticmethod
+        def backward(ctx, grad_J):
+            g, _ = obj.backward(float(grad_J), want_q0=False)
+            return torch.tensor(g, dtype=torch.float64, device=grad_J.device)
+
+    return _Objective.apply
 
 
 def adjoint_batch_forward(objs):

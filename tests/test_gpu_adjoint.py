@@ -198,3 +198,17 @@ def test_even_odd_adjoint_equals_dense(pkg, N):
     assert abs(a[1] - b[1]) <= 1e-12 * abs(a[1])
     assert abs(a[2] - b[2]) <= 1e-12 * abs(a[2])
     assert np.linalg.norm(a[3] - b[3]) <= 1e-12 * np.linalg.norm(a[3])
+
+
+def test_torch_autograd_function(pkg):
+    """The objective as a torch.autograd.Function: autograd's gradient is the adjoint's."""
+    torch = pytest.importorskip("torch")
+    mesh, cfg, obj = setup(pkg, nsteps=30, navg=10, C=7)
+    f = pkg.torch_objective(obj)
+    p = torch.tensor(cfg.alpha_deg, dtype=torch.float64, requires_grad=True)
+    J = f(p)
+    (3.0 * J).backward()
+    ref = pkg.LiftObjective(mesh, cfg, 30, 10, 7)
+    assert float(J.detach()) == ref.forward()
+    ga, _ = ref.backward(3.0, want_q0=False)
+    assert float(p.grad) == ga
