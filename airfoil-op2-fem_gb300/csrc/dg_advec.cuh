@@ -1,4 +1,4 @@
-// Scalar advection app (advec/src/advec.cpp:187-296) on the device.  Included at the end of
+// Scalar advection app (advec/src/advec.cpp:171-262) on the device.  Included at the end of
 // dg_solver.cu: it shares the per-order operators [Drw | Dsw | -LIFT] in constant memory, the
 // reference-node coordinates, the affine geometry kernel and the edge records of the Euler path.
 //
@@ -345,7 +345,7 @@ int Advection::step(int nsteps, bool use_graph, std::string &err) {
   for (int i = 0; i < nsteps; i++) {
     if (use_graph) CK(cudaGraphLaunch(graph_exec, stream));
     else enqueue_step(stream);
-    t += d.dt;  // advec/src/advec.cpp:295
+    t += d.dt;  // advec/src/advec.cpp:262
     steps++;
   }
   CK(cudaGetLastError());

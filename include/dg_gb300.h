@@ -119,7 +119,7 @@ int dg_solver_write_vtk(dg_solver_t *s, const dg_mesh_t *mesh, const char *path)
  * advec/src/advec.cpp: one scalar per node (q [n_cells][Np] doubles), flux (vx q, vy q) with the
  * Lax-Friedrichs face flux of advec/src/advec_rhs.h:36-63, the constant ghost value 4.5e-5 on
  * every boundary face (advec/src/get_bedge_q.h), the Gaussian pulse of advec/src/set_ic.h and
- * classical RK4 with a fixed dt (advec.cpp:230-296; -vx/-vy/-iter there are vel_x, vel_y and the
+ * classical RK4 with a fixed dt (advec.cpp:197-262; -vx/-vy/-iter there are vel_x, vel_y and the
  * step count here).  Same operators, geometry and edge records as the Euler solver; order 1..6. */
 typedef struct dg_advec_t dg_advec_t;
 int dg_advec_create(const dg_mesh_t *mesh, int order, double vel_x, double vel_y, double dt, dg_advec_t **out);

@@ -1,9 +1,9 @@
 /* Oracle driver of the scalar advection app — TEST INFRASTRUCTURE ONLY (see
- * dg_oracle.h).  AdvInstance<KP> owns the app's dats (advec/src/advec.cpp:90-160)
- * and runs its loop sequence (advec/src/advec.cpp:187-296): init_grid, set_ic,
+ * dg_oracle.h).  AdvInstance<KP> owns the app's dats (advec/src/advec.cpp:80-153)
+ * and runs its loop sequence (advec/src/advec.cpp:171-262): init_grid, set_ic,
  * then per step four stages of neighbour_zero, get_neighbour_q, get_bedge_q,
  * advec_rhs and (stages 0-2) set_workingQ with rk_frac {0.5, 0.5, 1.0},
- * closed by the RK4 update_Q; dt is fixed (advec.cpp:230, 0.001 there).
+ * closed by the RK4 update_Q; dt is fixed (advec.cpp:197, 0.001 there).
  * Loops run the way driver.h runs them (direct loops in static OpenMP chunks,
  * edge loops by colour).  Every face slot is written by exactly one edge or
  * boundary edge onto a zeroed slot, so the result is independent of the loop

@@ -85,7 +85,7 @@ int orc_refresh_dt(void *h);
 
 /* Scalar advection app (advec/src/advec.cpp): one value per node, q[c*Np + node].
  * adv_init runs init_grid and set_ic and fixes dt; adv_rhs evaluates one stage's right-hand
- * side of workingQ into rk<stage+1>; adv_run takes classical RK4 steps (advec.cpp:237-296).
+ * side of workingQ into rk<stage+1>; adv_run takes classical RK4 steps (advec.cpp:202-262).
  * Dats by name: q, workingQ, rk1..rk4, exteriorQ and the geometry dats of orc_get. */
 void *adv_create(const orc_ops *ops, const orc_mesh *mesh, double vel_x, double vel_y);
 void adv_destroy(void *h);

@@ -14,7 +14,7 @@ on the reference's own meshes:
                    dt = 0.1/dt1 frozen (vortex/src/vortex.cpp:209-306): q and the
                    L2 error sums after 100 steps.
   advec_n4.npz     advec/grid.vtk (K=23252, N=4), scalar advection with velocity
-                   (1, 1) and dt = 0.001 (advec/src/advec.cpp:230): the RHS of a
+                   (1, 1) and dt = 0.001 (advec/src/advec.cpp:197): the RHS of a
                    seeded perturbed state and q after 100 RK4 steps (the app's
                    default -iter).  Both are stored sparse (entries of magnitude at least
                    1e-16 of the largest, with the relative L2 of the rest, below 4e-16):

@@ -319,7 +319,7 @@ def test_dropin_vortex_rejects_missing_constants(op2, omesh, oops):
 
 
 class Advec:
-    """advec/src/advec.cpp:120-260 on the drop-in: one value per node, classical RK4, dt fixed."""
+    """advec/src/advec.cpp:107-262 on the drop-in: one value per node, classical RK4, dt fixed."""
 
     def __init__(self, op2, m, ops, vel, dt, q0=None):
         o = self.op2 = op2
