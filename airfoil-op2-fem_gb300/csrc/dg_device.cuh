@@ -6,6 +6,7 @@
 // reused, and constant factors are folded.  The results equal the reference's expressions up
 // to rounding.
 #pragma once
+#include <cmath>
 #include <cstdint>
 
 namespace dg {
@@ -14,7 +15,25 @@ struct Phys {
   double gam, gm1;               // gamma, gamma - 1
   double rinf, uinf, vinf, pinf, einf;  // freestream (src/airfoil.cpp:79-99)
   double vx0, vy0, vbeta;        // isentropic vortex centre and strength
+  // Set by derive(): freestream sound speed and its reciprocal, 2/(gamma-1), 1/gamma,
+  // 1/(gamma-1), and the vortex's density coefficient (gamma-1)/(16 gamma pi^2).
+  double cinf, rcinf, tgm1, igam, igm1, kvort;
   float gamf, gm1f;              // gamma, gamma - 1 in single precision (the dt estimate)
+  // 2/(gamma-1) is 5 (gamma = 1.4; 5 + 9e-16 after the rounding of gamma - 1 in double): the
+  // powers x^(2/(gamma-1)) and x^(1/(gamma-1)) are taken as x^5 and x^2 sqrt(x).
+  int pow5;
+
+  void derive() {
+    gamf = (float)gam;
+    gm1f = (float)gm1;
+    cinf = sqrt(gam * pinf / rinf);
+    rcinf = 1.0 / cinf;
+    tgm1 = 2.0 / gm1;
+    igam = 1.0 / gam;
+    igm1 = 1.0 / gm1;
+    kvort = gm1 / (16 * gam * M_PI * M_PI);
+    pow5 = fabs(tgm1 - 5.0) < 1e-12 ? 1 : 0;
+  }
 };
 
 __device__ __forceinline__ double rcp(double x) { return __drcp_rn(x); }
@@ -90,13 +109,15 @@ __device__ __forceinline__ void vortex_state(double x, double y, double t, const
   const double e1 = exp(1.0 - r2);
   const double u = 1.0 - P.vbeta * e1 * (dy / (2 * M_PI));
   const double v = P.vbeta * e1 * ((x - P.vx0) / (2 * M_PI));
-  double rho = 1.0 - (P.gm1 / (16 * P.gam * M_PI * M_PI)) * P.vbeta * P.vbeta * exp(2 * (1.0 - r2));
-  rho = pow(rho, 1.0 / P.gm1);
-  const double p = pow(rho, P.gam);
+  // b = 1 - k beta^2 exp(2 (1 - r2)), rho = b^(1/(gamma-1)), p = rho^gamma = b^(gamma/(gamma-1)),
+  // which is rho * b: one exp and at most one pow instead of two and two.
+  const double b = 1.0 - P.kvort * P.vbeta * P.vbeta * (e1 * e1);
+  const double rho = P.pow5 ? b * b * sqrt(b) : pow(b, P.igm1);
+  const double p = rho * b;
   q[0] = rho;
   q[1] = rho * u;
   q[2] = rho * v;
-  q[3] = p / P.gm1 + 0.5 * rho * (u * u + v * v);
+  q[3] = fma(p, P.igm1, 0.5 * rho * (u * u + v * v));
 }
 
 // Characteristic farfield ghost state (boundary type 3).  No reference counterpart: Riemann
@@ -104,10 +125,12 @@ __device__ __forceinline__ void vortex_state(double x, double y, double t, const
 // from the upwind side; supersonic inflow/outflow take freestream/interior.
 __device__ __forceinline__ void farfield_state(const double qi[4], double nx, double ny,
                                                const Phys &P, double qb[4]) {
-  const double rhoi = qi[0], ui = qi[1] / rhoi, vi = qi[2] / rhoi;
-  const double pi = P.gm1 * (qi[3] - 0.5 * rhoi * (ui * ui + vi * vi));
-  const double ci = sqrt(fabs(P.gam * pi / rhoi));
-  const double vni = ui * nx + vi * ny;
+  const double rhoi = qi[0], ir = rcp(rhoi);
+  const double ui = qi[1] * ir, vi = qi[2] * ir;
+  const double pi = P.gm1 * fma(-0.5, fma(qi[1], ui, qi[2] * vi), qi[3]);
+  const double c2i = fabs(P.gam * pi * ir);
+  const double rci = rsqrt(c2i), ci = c2i * rci;
+  const double vni = fma(ui, nx, vi * ny);
   if (vni <= -ci) {
     qb[0] = P.rinf; qb[1] = P.rinf * P.uinf; qb[2] = P.rinf * P.vinf; qb[3] = P.einf;
     return;
@@ -116,29 +139,32 @@ __device__ __forceinline__ void farfield_state(const double qi[4], double nx, do
     qb[0] = qi[0]; qb[1] = qi[1]; qb[2] = qi[2]; qb[3] = qi[3];
     return;
   }
-  const double cinf = sqrt(P.gam * P.pinf / P.rinf);
-  const double vninf = P.uinf * nx + P.vinf * ny;
-  const double rp = vni + 2.0 * ci / P.gm1;
-  const double rm = vninf - 2.0 * cinf / P.gm1;
+  const double vninf = fma(P.uinf, nx, P.vinf * ny);
+  const double rp = fma(P.tgm1, ci, vni);
+  const double rm = fma(-P.tgm1, P.cinf, vninf);
   const double vnb = 0.5 * (rp + rm);
   const double cb = 0.25 * P.gm1 * (rp - rm);
-  double sref, ut, vt;
-  if (vnb > 0.0) {
-    sref = pi / pow(rhoi, P.gam);
-    ut = ui - vni * nx;
-    vt = vi - vni * ny;
+  // Entropy s = p_u / rho_u^gamma and tangential velocity from the upwind side u (interior for
+  // outflow, freestream for inflow).  rho_b = (cb^2 / (gamma s))^(1/(gamma-1)) is, since
+  // c_u^2 = gamma p_u / rho_u, rho_u (|cb| / c_u)^(2/(gamma-1)): no pow for gamma = 1.4.
+  const bool out = vnb > 0.0;
+  const double rho_u = out ? rhoi : P.rinf;
+  const double ratio = fabs(cb) * (out ? rci : P.rcinf);
+  double rhob;
+  if (P.pow5) {
+    const double r2 = ratio * ratio;
+    rhob = rho_u * (r2 * r2 * ratio);
   } else {
-    sref = P.pinf / pow(P.rinf, P.gam);
-    ut = P.uinf - vninf * nx;
-    vt = P.vinf - vninf * ny;
+    rhob = rho_u * pow(ratio, P.tgm1);
   }
-  const double rhob = pow(cb * cb / (P.gam * sref), 1.0 / P.gm1);
-  const double ub = ut + vnb * nx, vb = vt + vnb * ny;
-  const double pb = rhob * cb * cb / P.gam;
+  const double ut = out ? fma(-vni, nx, ui) : fma(-vninf, nx, P.uinf);
+  const double vt = out ? fma(-vni, ny, vi) : fma(-vninf, ny, P.vinf);
+  const double ub = fma(vnb, nx, ut), vb = fma(vnb, ny, vt);
+  const double pb = rhob * cb * cb * P.igam;
   qb[0] = rhob;
   qb[1] = rhob * ub;
   qb[2] = rhob * vb;
-  qb[3] = pb / P.gm1 + 0.5 * rhob * (ub * ub + vb * vb);
+  qb[3] = fma(pb, P.igm1, 0.5 * rhob * fma(ub, ub, vb * vb));
 }
 
 // Ghost state of src/get_bedge_q.h:23-50 (types 0 inflow, 1 outflow, 2 wall) and type 3.

@@ -128,7 +128,7 @@ __device__ __forceinline__ void st2(double *p, double a, double b) {
 template <int N>
 __device__ __forceinline__ void face_node(const Inst &d, const int stage, const int tid) {
   constexpr int Np = np_of(N), Nfp = N + 1;
-  // Boundary face nodes come first: their ghost states (farfield pow, vortex exp/pow) cost
+  // Boundary face nodes come first: their ghost states (characteristic farfield, vortex exp) cost
   // several times an interior node, and last they would leave a tail on a near-idle GPU.
   const int nbf = d.nB * Nfp;
   const Phys &P = d.P;
@@ -983,8 +983,6 @@ int Solver::create(const Config &c, const Mesh &m, std::string &err) {
   const double gam = c.gam;
   d.P.gam = gam;
   d.P.gm1 = gam - 1.0;
-  d.P.gamf = (float)gam;
-  d.P.gm1f = (float)(gam - 1.0);
   // Freestream as src/airfoil.cpp:79-99.
   double u, v, e;
   if (c.alpha_deg != 0.0) {
@@ -1004,6 +1002,7 @@ int Solver::create(const Config &c, const Mesh &m, std::string &err) {
   d.P.vx0 = c.vortex_x0;
   d.P.vy0 = c.vortex_y0;
   d.P.vbeta = c.vortex_beta;
+  d.P.derive();
 
   std::vector<int4> edges, bedges;
   edge_records(m, edges, bedges);
@@ -1243,13 +1242,12 @@ int rhs_noalloc(const Config &c, int K, int nE, int nB, const double *W, const d
   }
   d.P.gam = gam;
   d.P.gm1 = gam - 1.0;
-  d.P.gamf = (float)gam;
-  d.P.gm1f = (float)(gam - 1.0);
   d.P.rinf = c.rho_inf;
   d.P.uinf = u;
   d.P.vinf = v;
   d.P.pinf = c.p_inf;
   d.P.einf = e;
+  d.P.derive();
   ce = cudaMemsetAsync(nd.flux, 0, need, stream);
   if (ce != cudaSuccess) { err = std::string("cudaMemsetAsync: ") + cudaGetErrorString(ce); return -100; }
   DG_DISPATCH(N, (launch_stage<NN>(d, 3, stream)));
