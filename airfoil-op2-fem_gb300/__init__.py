@@ -124,6 +124,7 @@ def lib():
         "dg_fp64_mma_peak_gflops": (C.c_double, []),
         "dg_kernels_per_step": (C.c_int, []),
         "dg_set_elem_variant": (None, [C.c_int]),
+        "dg_elem_variant": (C.c_int, []),
         "dg_set_face_block": (None, [C.c_int]),
         "dg_set_pdl": (None, [C.c_int]),
         "dg_batch_create": (C.c_int, [C.c_int, C.POINTER(Config), C.POINTER(vp), C.POINTER(vp)]),

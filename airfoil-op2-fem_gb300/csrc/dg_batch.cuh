@@ -66,7 +66,8 @@ __device__ __forceinline__ bool grid_barrier(GridBarrier *b, const unsigned nblo
   }
 
 // ftiles: {instance, first face node, count, order}; etiles: {instance, first cell, 0, order}.
-template <int BS, int MINB>
+// TC: the element contraction on the tensor cores (element-kernel form 2), as the plain path.
+template <int BS, int MINB, bool TC>
 __global__ void __launch_bounds__(BS, MINB) batch_stage_kernel(const Inst *insts, const int4 *ftiles, const int nft,
                                                                 const int4 *etiles, const int net, const int stage,
                                                                 GridBarrier *bar) {
@@ -80,7 +81,7 @@ __global__ void __launch_bounds__(BS, MINB) batch_stage_kernel(const Inst *insts
   for (int t = blockIdx.x; t < net; t += gridDim.x) {
     const int4 et = etiles[t];
     const Inst &d = insts[et.x];
-    DG_DISPATCH_RT(et.w, elem_tile_sym<NN>(d, stage, et.y, threadIdx.x & 31, threadIdx.x >> 5, Xb));
+    DG_DISPATCH_RT(et.w, (elem_tile_sym<NN, false, TC>(d, stage, et.y, threadIdx.x & 31, threadIdx.x >> 5, Xb)));
   }
 }
 
@@ -93,12 +94,12 @@ __global__ void __launch_bounds__(256) batch_face_kernel(const Inst *insts, cons
   DG_DISPATCH_RT(ft.w, face_node<NN>(insts[ft.x], stage, ft.y + threadIdx.x));
 }
 
-template <int N>
-__global__ void __launch_bounds__(32 * np_of(N)) batch_elem_kernel(const Inst *insts, const int4 *etiles,
-                                                                    const int first, const int stage) {
+template <int N, bool TC>
+__global__ void __launch_bounds__(32 * np_of(N), oz_used(N, TC) ? 3 : 1) batch_elem_kernel(const Inst *insts, const int4 *etiles,
+                                                                                const int first, const int stage) {
   extern __shared__ double2 Xg[];
   const int4 et = etiles[first + blockIdx.x];
-  elem_tile_sym<N>(insts[et.x], stage, et.y, threadIdx.x & 31, threadIdx.x >> 5, Xg);
+  elem_tile_sym<N, false, TC>(insts[et.x], stage, et.y, threadIdx.x & 31, threadIdx.x >> 5, Xg);
 }
 
 __global__ void batch_finalize_kernel(const Inst *insts, const int n) {
@@ -121,13 +122,17 @@ struct BatchVariant {
   const void *fn;
 };
 
-template <int BS, int MINB>
+template <int BS, int MINB, bool TC>
 static BatchVariant batch_variant() {
-  return BatchVariant{BS, MINB, (const void *)batch_stage_kernel<BS, MINB>};
+  return BatchVariant{BS, MINB, (const void *)batch_stage_kernel<BS, MINB, TC>};
 }
 
+// The persistent kernels of the current element-kernel form (the batch computes exactly what the
+// plain solvers compute).
 static std::vector<BatchVariant> batch_variants() {
-  return {batch_variant<512, 1>(), batch_variant<512, 2>(), batch_variant<1024, 1>()};
+  if (g_elem_variant == 2)
+    return {batch_variant<512, 1, true>(), batch_variant<512, 2, true>(), batch_variant<1024, 1, true>()};
+  return {batch_variant<512, 1, false>(), batch_variant<512, 2, false>(), batch_variant<1024, 1, false>()};
 }
 
 // Variant id of the grouped launches (not a persistent kernel).
@@ -242,8 +247,12 @@ struct Batch {
       for (int n = 1; n <= 6; n++) {
         const size_t sm = (size_t)(nk_of(n) + np_of(n)) * 32 * 4 * sizeof(double);
         cudaError_t ce = cudaSuccess;
-        DG_DISPATCH(n, ce = cudaFuncSetAttribute(batch_elem_kernel<NN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)sm));
+        DG_DISPATCH(n, ce = cudaFuncSetAttribute(batch_elem_kernel<NN, false>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        if (ce == cudaSuccess) {
+          DG_DISPATCH(n, ce = cudaFuncSetAttribute(batch_elem_kernel<NN, true>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        }
         if (ce != cudaSuccess) { err = cudaGetErrorString(ce); return -100; }
       }
       if (int rc = build_tiles(ft, err)) return rc;
@@ -301,8 +310,13 @@ struct Batch {
     for (int n = 6; n >= 1; n--) {
       if (!ord_count[n]) continue;
       const size_t sm = (size_t)(nk_of(n) + np_of(n)) * 32 * 4 * sizeof(double);
-      DG_DISPATCH(n, (batch_elem_kernel<NN><<<ord_count[n], 32 * np_of(NN), sm, s>>>(d_insts, d_etiles,
-                                                                                       ord_first[n], stage)));
+      if (g_elem_variant == 2) {
+        DG_DISPATCH(n, (batch_elem_kernel<NN, true><<<ord_count[n], 32 * np_of(NN), sm, s>>>(d_insts, d_etiles,
+                                                                                             ord_first[n], stage)));
+      } else {
+        DG_DISPATCH(n, (batch_elem_kernel<NN, false><<<ord_count[n], 32 * np_of(NN), sm, s>>>(d_insts, d_etiles,
+                                                                                              ord_first[n], stage)));
+      }
     }
     return cudaGetLastError();
   }

@@ -612,6 +612,7 @@ double dg_fp64_mma_peak_gflops(void) {
 }
 int dg_kernels_per_step(void) { return 7; }
 void dg_set_elem_variant(int variant) { dg::set_elem_variant(variant); }
+int dg_elem_variant(void) { return dg::elem_variant(); }
 void dg_set_face_block(int threads) { dg::set_face_block(threads); }
 void dg_set_pdl(int on) { dg::set_pdl(on); }
 

@@ -1,0 +1,242 @@
+// Element-kernel contraction on the bf16 tensor cores, exact to FP64 accuracy (included by
+// dg_solver.cu inside namespace dg).
+//
+// On GB300 the FP64 pipe issues about 2 DFMA lanes per clock per SM, while mma.sync on bf16
+// operands runs at ~600 TFLOP/s with FP32 accumulation.  The even/odd contraction of the
+// element kernel, Y_p = S_p X_p for the even (p = 0) and odd (p = 1) halves (rows of the operator
+// S_p, columns of X_p = one (cell, variable) over the staged slots), is therefore done as an
+// integer product in the manner of Ozaki's error-free splitting (Ozaki, Ogita, Oishi, Rump,
+// "Error-free transformations of matrix multiplication by using fast routines of matrix
+// multiplication and its applications", Numer. Algorithms 59, 2012):
+//
+//  * every column of X_p (16 or 32 values) is scaled by its largest binary exponent E, so each
+//    value is x = m 2^(E-55) with m an integer, |m| < 2^56 (the bits below 2^(E-55) are cut);
+//    every operator row by its own F likewise (done once on the host).  m is written in base 256
+//    as seven signed digits d_0..d_6 (|d| <= 255, all with the sign of x), each exact in bf16.
+//  * digit products d_j c_s with j + s = L are summed into one FP32 accumulator per level L
+//    (L = 0..6; the levels L >= 7 lie below 2^-56 of the leading term and are dropped).  A level
+//    sums at most 7 pairs x 32 slots x 255^2 < 2^24, so every accumulation is an exact integer
+//    (checked on the GPU: bit-exact against 64-bit integer sums up to 1.46e7).
+//  * the seven level sums are joined as integers, T = sum_L lev_L 256^(6-L), split in two 64-bit
+//    parts of < 2^49 each, turned into doubles scaled by 2^(E+F-62) exactly (bit-pattern
+//    addition, no int-to-double conversion: those take several FP64 issue slots each on this
+//    part) and added with one rounding.  The result is the correctly rounded dot product of the
+//    56-bit truncations:
+//    its error is below 2^-55 max|x| sum|s|, under the FP64 dot product's own error bound.
+//
+// Units of work: parity x 8 groups of 4 cells (x 4 variables) = 16 m16n8k16 row tiles per
+// 32-cell tile; each needs 28 mma per k-step of 16 slots.  Non-finite inputs in a column give NaN.
+// Supported for N <= 3 (each parity has at most 8 operator rows: one n-tile); used at N = 3.
+
+__constant__ int c_ozf[7][2][8];  // biased binary exponent F of every operator row (order, parity, row)
+__device__ uint2 g_ozb[7][2][7][2][32];  // B fragments: order, parity, digit s, k-step, lane
+
+// Orders that use it: N = 3 (measured on the K=32768 O-grid: step 367 -> 331 us).  At N = 1 and 2
+// the contraction is too small a share of the element kernel and the split costs more than it
+// saves (N = 1: 184 -> 192 us, N = 2: 236 -> 252 us); N >= 4 needs more than one n-tile.
+constexpr int kOzMinN = 3, kOzMaxN = 3;
+constexpr bool oz_used(int N, bool tc) { return tc && N >= kOzMinN && N <= kOzMaxN; }
+
+__device__ __forceinline__ void mma_bf16_16816(float c[4], const uint32_t a[4], const uint2 b) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b.x), "r"(b.y));
+}
+
+// Digit j (0 = most significant) of a magnitude m (hi:lo, < 2^56) as a float: byte (6 - j) goes
+// below the float 2^23, and subtracting 2^23 leaves exactly d.
+__device__ __forceinline__ float oz_digit(const uint32_t hi, const uint32_t lo, const int j) {
+  const uint32_t w = j < 3 ? hi : lo;
+  const uint32_t b = j < 3 ? (uint32_t)(2 - j) : (uint32_t)(6 - j);
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7650u | b)) - 8388608.0f;
+}
+
+// The upper halves (bf16) of two floats holding small integers, low k first, with the sign
+// pattern of the pair (bit 15: low, bit 31: high) applied.
+__device__ __forceinline__ uint32_t oz_pack(const float f_lo, const float f_hi, const uint32_t sign) {
+  return __byte_perm(__float_as_uint(f_lo), __float_as_uint(f_hi), 0x7632u) ^ sign;
+}
+
+// One 16-row tile: cells c0..c0+3 x the four variables (row r: cell c0 + r / 4, variable r % 4, so
+// the eight row lanes of a fragment read eight consecutive doubles), slots SLOT0..SLOT0+K-1
+// (K <= 16 KST), times the R operator rows of this parity, written to Y rows YROW0 + n.
+template <int NORD, int K, int R, int SLOT0, int YROW0, int KST, int P>
+__device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *__restrict__ Yd, const int c0,
+                                        const int lane) {
+  static_assert(R <= 8 && KST <= 2 && K <= 16 * KST, "one n-tile, at most two k-steps");
+  const int g = lane >> 2, t = lane & 3;
+  const int col = c0 * 4 + g;  // (cell, variable) of row g; row g + 8 is col + 8
+  // staged values of rows (columns of X) c0+g and c0+g+8 at slots 16 ks + {2t, 2t+1, 2t+8, 2t+9}
+  uint32_t hi[KST][2][4], lo[KST][2][4];
+  int em[2] = {0, 0};
+#pragma unroll
+  for (int ks = 0; ks < KST; ks++)
+#pragma unroll
+    for (int r = 0; r < 2; r++)
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const int k = 16 * ks + 2 * t + (q & 1) + ((q >> 1) << 3);
+        const double x = k < K ? Xd[(SLOT0 + k) * 128 + col + 8 * r] : 0.0;
+        const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+        hi[ks][r][q] = (uint32_t)(b >> 32);
+        lo[ks][r][q] = (uint32_t)b;
+        em[r] = max(em[r], (int)((b >> 52) & 0x7FF));
+      }
+#pragma unroll
+  for (int r = 0; r < 2; r++) {
+    em[r] = max(em[r], __shfl_xor_sync(0xffffffffu, em[r], 1));
+    em[r] = max(em[r], __shfl_xor_sync(0xffffffffu, em[r], 2));
+  }
+  // aligned magnitudes m = M 2^(e - E + 3) (M the 53-bit significand) and the sign pattern of
+  // every A-fragment register (pairs (g: q0 q1), (g+8: q0 q1), (g: q2 q3), (g+8: q2 q3))
+  uint32_t sgn[KST][4];
+#pragma unroll
+  for (int ks = 0; ks < KST; ks++) {
+#pragma unroll
+    for (int x = 0; x < 4; x++) {
+      const int r = x & 1, q0 = (x >> 1) * 2;
+      sgn[ks][x] = ((hi[ks][r][q0] >> 16) & 0x8000u) | (hi[ks][r][q0 + 1] & 0x80000000u);
+    }
+#pragma unroll
+    for (int r = 0; r < 2; r++)
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const uint32_t h = hi[ks][r][q];
+        const int e = (int)((h >> 20) & 0x7FF);
+        const unsigned long long M =
+            e ? ((((unsigned long long)(h & 0xFFFFFu)) << 32) | lo[ks][r][q]) | (1ull << 52) : 0ull;
+        const int sh = e - em[r] + 3;
+        const unsigned long long m = sh >= 0 ? (M << sh) : (sh > -64 ? (M >> -sh) : 0ull);
+        hi[ks][r][q] = (uint32_t)(m >> 32);
+        lo[ks][r][q] = (uint32_t)m;
+      }
+  }
+  const uint2 *bfr = &g_ozb[NORD][P][0][0][lane];
+  float acc[7][4];
+#pragma unroll
+  for (int l = 0; l < 7; l++) acc[l][0] = acc[l][1] = acc[l][2] = acc[l][3] = 0.0f;
+#pragma unroll
+  for (int j = 0; j < 7; j++) {
+#pragma unroll
+    for (int ks = 0; ks < KST; ks++) {
+      float f[2][4];
+#pragma unroll
+      for (int r = 0; r < 2; r++)
+#pragma unroll
+        for (int q = 0; q < 4; q++) f[r][q] = oz_digit(hi[ks][r][q], lo[ks][r][q], j);
+      // A fragment (row-major 16 x 16): rows g / g+8, slots 2t..2t+1 / 2t+8..2t+9
+      const uint32_t a[4] = {oz_pack(f[0][0], f[0][1], sgn[ks][0]), oz_pack(f[1][0], f[1][1], sgn[ks][1]),
+                             oz_pack(f[0][2], f[0][3], sgn[ks][2]), oz_pack(f[1][2], f[1][3], sgn[ks][3])};
+#pragma unroll
+      for (int s = 0; s + j < 7; s++) mma_bf16_16816(acc[j + s], a, __ldg(bfr + (s * 2 + ks) * 32));
+    }
+  }
+  // C fragment: acc[.][0] (row g, col 2t), [1] (g, 2t+1), [2] (g+8, 2t), [3] (g+8, 2t+1)
+#pragma unroll
+  for (int r = 0; r < 2; r++)
+#pragma unroll
+    for (int cc = 0; cc < 2; cc++) {
+      const int n = 2 * t + cc;
+      if (n < R) {
+        const int o = 2 * r + cc;
+        long long l[7];
+#pragma unroll
+        for (int L = 0; L < 7; L++) l[L] = (long long)__float2int_rz(acc[L][o]);
+        const long long th = l[0] * 65536LL + l[1] * 256LL + l[2];
+        const long long tl = l[3] * 16777216LL + l[4] * 65536LL + l[5] * 256LL + l[6];
+        const int fe = c_ozf[NORD][P][n];
+        const int sc = em[r] + fe - 2046 - 62;
+        double out;
+        if (em[r] == 0x7FF) {
+          out = __longlong_as_double(0x7FF8000000000000LL);
+        } else if (sc >= -1022 && sc <= 900) {
+          // th 2^(32+sc) + tl 2^sc without an integer-to-double conversion: for |t| < 2^51 the
+          // integer sum of t and the bit pattern of 1.5 2^52 u is the double 1.5 2^52 u + t u, and
+          // subtracting 1.5 2^52 u leaves t u exactly.  One rounding, in the final addition.
+          const long long mh = ((long long)(sc + 32 + 52 + 1023) << 52) | (1LL << 51);
+          const long long ml = ((long long)(sc + 52 + 1023) << 52) | (1LL << 51);
+          const double hv = __longlong_as_double(mh + th) - __longlong_as_double(mh);
+          const double lv = __longlong_as_double(ml + tl) - __longlong_as_double(ml);
+          out = hv + lv;
+        } else if (sc < -1022) {
+          out = 0.0;  // below 2^-1022: negligible against any physical value
+        } else {
+          const double val = fma((double)th, 4294967296.0, (double)tl);
+          const int s1 = sc / 2, s2 = sc - s1;  // each <= 992: two exact power-of-two scalings
+          out = (val * __longlong_as_double((long long)(s1 + 1023) << 52)) *
+                __longlong_as_double((long long)(s2 + 1023) << 52);
+        }
+        Yd[(YROW0 + n) * 128 + col + 8 * r] = out;
+      }
+    }
+}
+
+// Both parities of one 32-cell tile: Y rows 0..NRe-1 from the even slots, NRe.. from the odd
+// slots.  Warp w of nw takes row tiles w, w + nw, ... of the 16 (8 per parity, 4 cells each).
+template <int N, int NUe, int NUo, int NRe, int NRo>
+__device__ __forceinline__ void oz_contract(const double *Xd, double *Yd, const int warp, const int nw,
+                                            const int lane) {
+  constexpr int KE = (NUe + 15) / 16, KO = (NUo + 15) / 16;
+  for (int u = warp; u < 16; u += nw) {
+    const int c0 = (u & 7) * 4;
+    if (u < 8) oz_tile<N, NUe, NRe, 0, 0, KE, 0>(Xd, Yd, c0, lane);
+    else oz_tile<N, NUo, NRo, NUe, NRe, KO, 1>(Xd, Yd, c0, lane);
+  }
+}
+
+// ---------------------------------------------------------------- host: operator digits
+// Digits and B fragments of the two parity blocks of S (even rows NRe x NUe, then odd rows
+// NRo x NUo, row-major) for the tensor-core contraction.
+static uint32_t oz_bf16_bits(int d) {
+  const float f = (float)d;  // |d| <= 255: exact, and exact in the upper 16 bits
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  return u >> 16;
+}
+
+static int oz_upload(int N, const std::vector<double> &S, int NUe, int NUo, int NRe, int NRo, std::string &err) {
+  if (!oz_used(N, true)) return 0;
+  int fexp[2][8] = {};
+  static uint2 frag[2][7][2][32];
+  std::memset(frag, 0, sizeof(frag));
+  for (int p = 0; p < 2; p++) {
+    const int K = p ? NUo : NUe, R = p ? NRo : NRe;
+    const size_t base = p ? (size_t)NRe * NUe : 0;
+    if (R > 8 || K > 32) { err = "tensor-core contraction: operator too large"; return -4; }
+    std::vector<int> dig((size_t)7 * 32 * 8, 0);  // [s][k][n]
+    for (int n = 0; n < R; n++) {
+      int F = 0;
+      for (int k = 0; k < K; k++) {
+        uint64_t b;
+        std::memcpy(&b, &S[base + (size_t)n * K + k], 8);
+        F = std::max(F, (int)((b >> 52) & 0x7FF));
+      }
+      if (F == 0x7FF) { err = "tensor-core contraction: non-finite operator entry"; return -4; }
+      fexp[p][n] = F;
+      for (int k = 0; k < K; k++) {
+        uint64_t b;
+        std::memcpy(&b, &S[base + (size_t)n * K + k], 8);
+        const int e = (int)((b >> 52) & 0x7FF);
+        const uint64_t M = e ? ((b & 0xFFFFFFFFFFFFFull) | (1ull << 52)) : 0;
+        const int sh = e - F + 3;
+        const uint64_t m = sh >= 0 ? (M << sh) : (sh > -64 ? (M >> -sh) : 0);
+        const int sg = (b >> 63) ? -1 : 1;
+        for (int s = 0; s < 7; s++) dig[((size_t)s * 32 + k) * 8 + n] = sg * (int)((m >> (8 * (6 - s))) & 255);
+      }
+    }
+    for (int s = 0; s < 7; s++)
+      for (int ks = 0; ks < 2; ks++)
+        for (int lane = 0; lane < 32; lane++) {
+          const int g = lane >> 2, t = lane & 3, k0 = 16 * ks + 2 * t;
+          auto D = [&](int k) { return k < 32 ? dig[((size_t)s * 32 + k) * 8 + g] : 0; };
+          frag[p][s][ks][lane].x = oz_bf16_bits(D(k0)) | (oz_bf16_bits(D(k0 + 1)) << 16);
+          frag[p][s][ks][lane].y = oz_bf16_bits(D(k0 + 8)) | (oz_bf16_bits(D(k0 + 9)) << 16);
+        }
+  }
+  cudaError_t ce = cudaMemcpyToSymbol(c_ozf, fexp, sizeof(fexp), (size_t)N * sizeof(fexp));
+  if (ce == cudaSuccess) ce = cudaMemcpyToSymbol(g_ozb, frag, sizeof(frag), (size_t)N * sizeof(frag));
+  if (ce != cudaSuccess) { err = std::string("constant upload: ") + cudaGetErrorString(ce); return -3; }
+  return 0;
+}

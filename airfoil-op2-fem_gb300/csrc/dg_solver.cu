@@ -123,6 +123,8 @@ __device__ __forceinline__ void st2(double *p, double a, double b) {
   *reinterpret_cast<double2 *>(p) = make_double2(a, b);
 }
 
+#include "dg_ozaki.cuh"
+
 // ---------------------------------------------------------------- face kernel
 // One face node (tid in [0, (nB + nE) * Nfp)): boundary face nodes come first.
 template <int N>
@@ -406,7 +408,7 @@ __global__ void __launch_bounds__(32 * np_of(N)) elem_kernel(const Inst d, const
 // differences give y_i - y_P(i).  The contraction shrinks to 0.55-0.62 of the dense one.
 // One tile of 32 cells starting at e0, thread (lane, node i) of a block with at least Np
 // node-warps (warps with i >= Np only take part in the barriers).
-template <int N, bool PDL = false>
+template <int N, bool PDL = false, bool TC = false>
 __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, const int e0, const int lane,
                                               const int i, double2 *X) {
   constexpr int Np = np_of(N), Nfp = N + 1, NK = nk_of(N);
@@ -483,7 +485,11 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
   }
   __syncthreads();
   double r0 = 0.0, r1 = 0.0, r2 = 0.0, r3 = 0.0;
-  if (!active) {
+  if constexpr (oz_used(N, TC)) {
+    // the contraction on the tensor cores (dg_ozaki.cuh), every warp of the block taking part
+    oz_contract<N, NUe, NUo, NRe, Sym<N>::NRo>(reinterpret_cast<const double *>(X), reinterpret_cast<double *>(Y),
+                                               i, (int)(blockDim.x * blockDim.y) >> 5, lane);
+  } else if (!active) {
   } else if (i < NRe) {
 #pragma unroll
     for (int k = 0; k < NUe; k++) {
@@ -505,7 +511,7 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
       r3 = fma(c, x23.y, r3);
     }
   }
-  if (active) {
+  if (active && !oz_used(N, TC)) {
     Y[(i * 32 + lane) * 2] = make_double2(r0, r1);
     Y[(i * 32 + lane) * 2 + 1] = make_double2(r2, r3);
   }
@@ -523,16 +529,27 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
       }
     }
   }
+  if constexpr (oz_used(N, TC)) {
+    // re-read this node's W rather than holding it through the contraction (registers); the
+    // node is written only below, by this thread
+    if (live) {
+      const double *wp = d.W + ((size_t)e * Np + i) * 4;
+      const double2 a = ld2(wp), b = ld2(wp + 2);
+      w[0] = a.x; w[1] = a.y; w[2] = b.x; w[3] = b.y;
+    }
+  }
   stage_combine<N>(d, stage, e, active, live, i, lane, w, r0, r1, r2, r3, X);
   // X and Y are rewritten by the next tile only after every warp is past this point
   __syncthreads();
 }
 
-template <int N>
-__global__ void __launch_bounds__(32 * np_of(N)) elem_kernel_sym(const Inst d, const int stage) {
+// MB: minimum resident blocks per SM the register allocation must allow (3 for the tensor-core
+// form: 64 registers; without the bound it takes ~95 and runs two blocks per SM, measured slower).
+template <int N, bool TC, int MB = 1>
+__global__ void __launch_bounds__(32 * np_of(N), MB) elem_kernel_sym(const Inst d, const int stage) {
   extern __shared__ double2 Xs[];  // [NK][32] x 4 doubles, then [Np][32] x 4 doubles
   pdl_trigger();  // the next face kernel may be scheduled (it waits for this grid's writes)
-  elem_tile_sym<N, true>(d, stage, blockIdx.x * 32, threadIdx.x, threadIdx.y, Xs);
+  elem_tile_sym<N, true, TC>(d, stage, blockIdx.x * 32, threadIdx.x, threadIdx.y, Xs);
 }
 
 // ---------------------------------------------------------------- per-step finalize
@@ -752,15 +769,19 @@ static void launch_face(const Inst &d, int stage, cudaStream_t s) {
   launch_pdl(face_kernel<N>, dim3((nf + bs - 1) / bs), dim3(bs), 0, s, d, stage);
 }
 
-// 1: even/odd element kernel (default), 0: dense element kernel.
-static int g_elem_variant = 1;
+// 2: even/odd with the contraction on the bf16 tensor cores (dg_ozaki.cuh; at N = 3, the even/odd
+// FP64 kernel at the other orders; default), 1: even/odd element kernel, 0: dense element kernel.
+static int g_elem_variant = 2;
 
 template <int N>
 static void launch_elem(const Inst &d, int stage, cudaStream_t s) {
   constexpr int Np = np_of(N), NK = nk_of(N);
   if (g_elem_variant) {
     const size_t smem = (size_t)(NK + Np) * 32 * 4 * sizeof(double);
-    launch_pdl(elem_kernel_sym<N>, dim3((d.K + 31) / 32), dim3(32, Np), smem, s, d, stage);
+    if (g_elem_variant == 2 && oz_used(N, true))
+      launch_pdl(elem_kernel_sym<N, true, 3>, dim3((d.K + 31) / 32), dim3(32, Np), smem, s, d, stage);
+    else
+      launch_pdl(elem_kernel_sym<N, false>, dim3((d.K + 31) / 32), dim3(32, Np), smem, s, d, stage);
   } else {
     const size_t smem = (size_t)NK * 32 * 4 * sizeof(double);
     launch_pdl(elem_kernel<N>, dim3((d.K + 31) / 32), dim3(32, Np), smem, s, d, stage);
@@ -779,7 +800,9 @@ static cudaError_t set_smem_attr() {
   cudaError_t e = cudaFuncSetAttribute(elem_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const size_t smem_sym = (size_t)(nk_of(N) + np_of(N)) * 32 * 4 * sizeof(double);
-  return cudaFuncSetAttribute(elem_kernel_sym<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_sym);
+  e = cudaFuncSetAttribute(elem_kernel_sym<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_sym);
+  if (e != cudaSuccess || !oz_used(N, true)) return e;
+  return cudaFuncSetAttribute(elem_kernel_sym<N, true, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_sym);
 }
 
 template <int N>
@@ -868,7 +891,7 @@ static int sym_tables(const Operators &o, const std::vector<double> &A, std::str
   if (ce == cudaSuccess) ce = cudaMemcpyToSymbol(c_pos, pos, sizeof(pos), (size_t)N * sizeof(pos));
   if (ce == cudaSuccess) ce = cudaMemcpyToSymbol(c_out, out, sizeof(out), (size_t)N * sizeof(out));
   if (ce != cudaSuccess) { err = std::string("constant upload: ") + cudaGetErrorString(ce); return -3; }
-  return 0;
+  return oz_upload(N, S, NUe, NUo, NRe, NRo, err);
 }
 
 // ---------------------------------------------------------------- operator upload
@@ -920,7 +943,8 @@ int load_order_constants(int N, std::string &err) {
   return 0;
 }
 
-void set_elem_variant(int v) { g_elem_variant = v ? 1 : 0; }
+void set_elem_variant(int v) { g_elem_variant = (v >= 0 && v <= 2) ? v : 2; }
+int elem_variant() { return g_elem_variant; }
 void set_pdl(int on) { g_pdl = on ? 1 : 0; }
 void set_face_block(int b) { g_face_block = (b >= 32 && b <= 256 && b % 32 == 0) ? b : 64; }
 

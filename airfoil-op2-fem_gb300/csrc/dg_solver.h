@@ -50,6 +50,7 @@ struct Inst {
 int load_order_constants(int N, std::string &err);
 // Element kernel form for launches enqueued from now on: 1 even/odd (default), 0 dense.
 void set_elem_variant(int v);
+int elem_variant();
 // Threads per face-kernel block for launches enqueued from now on (32..256, multiple of 32).
 void set_face_block(int b);
 // Programmatic dependent launch of the plain path's face and element kernels (default on).

@@ -531,6 +531,23 @@ def main():
         traffic = None
     stage_bytes = algo_bytes(N_ORDER) * K
     hbm_gbs = stage_bytes / ((face_ms + elem_ms) * 1e-3) * 1e-9
+    # the element kernel in its all-FP64 even/odd form on the same workload, for comparison
+    variant = pkg.lib().dg_elem_variant()
+    elem_ms_fp64 = None
+    if variant == 2:
+        pkg.lib().dg_set_elem_variant(1)
+        try:
+            s64 = pkg.Solver(mesh, pkg.config(N=N_ORDER, cfl=CFL)).init()
+            k64 = np.zeros(7)
+            for _ in range(3):
+                s64.step_timed()
+            for _ in range(nk):
+                pkg.l2_flush(stream)
+                k64 += s64.step_timed()
+            elem_ms_fp64 = float(np.mean(k64[[1, 3, 5]])) / nk
+            del s64
+        finally:
+            pkg.lib().dg_set_elem_variant(variant)
 
     # end to end through the C ABI with pinned host buffers
     nq = K * Np * 4
@@ -566,6 +583,12 @@ def main():
                      "traffic": traffic if dominant == "elem_kernel" else None,
                      "traffic_source": "ncu dram__bytes_read+write per launch, stage average (profiles/)",
                      "peak_source": "DFMA throughput measured live on this GPU (MEASURED_PEAKS.json has no FP64 figure)",
+                     "elem_form": {2: "even/odd, contraction on the bf16 tensor cores (exact integer product)",
+                                   1: "even/odd, FP64", 0: "dense FP64"}[variant],
+                     "frac_note": ("FP64-equivalent: algorithmic FP64 flops over the DFMA peak; the contraction "
+                                   "runs on the tensor cores, so frac can exceed 1 (FP64 pipe busy 70-74 % of "
+                                   "active cycles per ncu)") if variant == 2 else "FP64 flops over the DFMA peak",
+                     "elem_ms_fp64_form": elem_ms_fp64,
                      "fp64_tensor_peak_tflops": dmma_gflops * 1e-3,
                      "fp64_tensor_note": "DMMA (mma.sync m8n8k4 f64) measured live; below DFMA and on the same pipe, so unused",
                      "flops_per_unit": elem_flops(N_ORDER) if dominant == "elem_kernel" else face_flops(N_ORDER),

@@ -254,9 +254,14 @@ double dg_fp64_peak_gflops(void);
 double dg_fp64_mma_peak_gflops(void);
 /* Number of kernels one dg_solver_run step launches. */
 int dg_kernels_per_step(void);
-/* Element-kernel form for launches and graphs built from now on: 1 even/odd split of
- * [Drw | Dsw | -LIFT] (default), 0 dense rows.  Both compute the same right-hand side. */
+/* Element-kernel form for launches and graphs built from now on: 2 (default) the even/odd split
+ * of [Drw | Dsw | -LIFT] with its contraction on the bf16 tensor cores as an exact integer
+ * product at order N = 3 and in FP64 at the other orders, 1 the even/odd split in FP64, 0 dense
+ * FP64 rows.  All compute the same right-hand side to rounding (the tensor-core contraction is
+ * the correctly rounded dot product of the 56-bit truncated inputs). */
 void dg_set_elem_variant(int variant);
+/* The current element-kernel form. */
+int dg_elem_variant(void);
 /* Threads per face-kernel block of the plain path (32..256, multiple of 32; default 64). */
 void dg_set_face_block(int threads);
 /* Launch the plain path's face and element kernels with programmatic dependent launch (1, the

@@ -165,6 +165,7 @@ def test_device_even_odd_equals_dense(pkg, orc, omesh, N):
     """The even/odd element kernel (default) and the dense one: same RHS and steps."""
     m = omesh.vortex_square(12, 0.0, 1.0)
     out = []
+    prev = pkg.lib().dg_elem_variant()
     for variant in (0, 1):
         pkg.lib().dg_set_elem_variant(variant)
         try:
@@ -176,6 +177,6 @@ def test_device_even_odd_equals_dense(pkg, orc, omesh, N):
             a.sync()
             out.append((r, a.get("q")))
         finally:
-            pkg.lib().dg_set_elem_variant(1)
+            pkg.lib().dg_set_elem_variant(prev)
     assert orc.rel_l2(out[1][0], out[0][0]) < 1e-13
     assert orc.rel_l2(out[1][1], out[0][1]) < 1e-13

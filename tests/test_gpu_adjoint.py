@@ -183,6 +183,7 @@ def test_even_odd_adjoint_equals_dense(pkg, N):
     mesh, cfg, _ = setup(pkg, N=N)
     rng = np.random.default_rng(40 + N)
     out = []
+    prev = pkg.lib().dg_elem_variant()
     for variant in (0, 1):
         pkg.lib().dg_set_elem_variant(variant)
         try:
@@ -194,7 +195,7 @@ def test_even_odd_adjoint_equals_dense(pkg, N):
             obj.forward()
             out.append((vjp, ap) + obj.backward())
         finally:
-            pkg.lib().dg_set_elem_variant(1)
+            pkg.lib().dg_set_elem_variant(prev)
     a, b = out
     assert np.linalg.norm(a[0] - b[0]) <= 1e-13 * np.linalg.norm(a[0])
     assert abs(a[1] - b[1]) <= 1e-12 * abs(a[1])

@@ -198,11 +198,13 @@ def test_nonphysical_state_is_reported(pkg, omesh):
 
 @pytest.mark.parametrize("N", [1, 2, 3, 4, 5, 6])
 def test_even_odd_form_equals_dense_form(pkg, orc, omesh, N):
-    """The even/odd element kernel (default) and the dense one compute the same RHS and steps."""
+    """The element-kernel forms compute the same RHS and steps: dense FP64 rows (0), the even/odd
+    split in FP64 (1) and the even/odd split with the tensor-core contraction (2, the default;
+    FP64 at N != 3)."""
     m = omesh.naca_ogrid(32, 8, farfield="characteristic")
-    rng = np.random.default_rng(100 + N)
     out = []
-    for variant in (0, 1):
+    prev = pkg.lib().dg_elem_variant()
+    for variant in (0, 1, 2):
         pkg.lib().dg_set_elem_variant(variant)
         try:
             s = pkg.Solver(pkg.Mesh.from_tables(m), pkg.config(N=N, cfl=0.5)).init()
@@ -213,9 +215,58 @@ def test_even_odd_form_equals_dense_form(pkg, orc, omesh, N):
             s.sync()
             out.append((r, s.get("q")))
         finally:
-            pkg.lib().dg_set_elem_variant(1)
-    assert orc.rel_l2(out[1][0], out[0][0]) < 1e-13
-    assert orc.rel_l2(out[1][1], out[0][1]) < 1e-13
+            pkg.lib().dg_set_elem_variant(prev)
+    for k in (1, 2):
+        assert orc.rel_l2(out[k][0], out[0][0]) < 1e-13
+        assert orc.rel_l2(out[k][1], out[0][1]) < 1e-13
+    if N != 3:
+        assert np.array_equal(out[2][0], out[1][0])  # form 2 is form 1 away from N = 3
+
+
+def _rhs_forms(pkg, m, W, N=3):
+    out = []
+    prev = pkg.lib().dg_elem_variant()
+    for variant in (1, 2):
+        pkg.lib().dg_set_elem_variant(variant)
+        try:
+            s = pkg.Solver(pkg.Mesh.from_tables(m), pkg.config(N=N, cfl=0.5)).init()
+            out.append(s.rhs(W))
+        finally:
+            pkg.lib().dg_set_elem_variant(prev)
+    return out
+
+
+def test_tensor_core_contraction_wide_range(pkg, omesh):
+    """Cells whose states differ by up to 1e6 in scale (each cell's state scaled as a whole, so
+    it stays physical): the tensor-core contraction scales every column by its own largest
+    exponent, and agrees with the FP64 contraction to rounding."""
+    m = omesh.naca_ogrid(32, 8, farfield="characteristic")
+    s = pkg.Solver(pkg.Mesh.from_tables(m), pkg.config(N=3, cfl=0.5)).init()
+    q = s.get("q").reshape(-1, 40)
+    lam = 10.0 ** np.random.default_rng(7).uniform(-3, 3, q.shape[0])
+    W = (q * lam[:, None]).ravel()
+    r1, r2 = _rhs_forms(pkg, m, W)
+    assert np.all(np.isfinite(r2))
+    assert np.linalg.norm(r2 - r1) <= 1e-13 * np.linalg.norm(r1)
+    # entrywise: near the wall the staged fluxes are ~1e3-1e4 and cancel to an O(1) RHS, so
+    # both contractions carry ~1e-12 absolute rounding there
+    assert np.abs(r2 - r1).max() <= 1e-11 * np.abs(r1).max()
+
+
+def test_tensor_core_contraction_nonfinite(pkg, omesh):
+    """A non-finite value in a cell's staged column gives NaN there, as the FP64 contraction
+    does, and leaves the cells it does not reach finite."""
+    m = omesh.naca_ogrid(32, 8, farfield="characteristic")
+    s = pkg.Solver(pkg.Mesh.from_tables(m), pkg.config(N=3, cfl=0.5)).init()
+    q = s.get("q")
+    W = q * (1.0 + 0.05 * np.random.default_rng(3).standard_normal(q.size))
+    W[40 * 17 + 5] = np.nan
+    r1, r2 = _rhs_forms(pkg, m, W)
+    assert np.isnan(r2).any()
+    assert np.array_equal(np.isnan(r1.reshape(-1, 40)).any(1), np.isnan(r2.reshape(-1, 40)).any(1))
+    ok = ~np.isnan(r1)
+    assert np.linalg.norm(r2[ok] - r1[ok]) <= 1e-13 * np.linalg.norm(r1[ok])
+    assert np.abs(r2[ok] - r1[ok]).max() <= 1e-11 * np.abs(r1[ok]).max()
 
 
 @pytest.mark.parametrize("N", [3, 4])
