@@ -358,8 +358,13 @@ int dg_solver_step_host(dg_solver_t *h, const double *q_in, int nsteps, double *
     CKC(cudaMemcpyAsync(h->s.d.W, h->s.d.q, n, cudaMemcpyDeviceToDevice, h->s.stream));
   }
   std::string err;
-  if (h->s.step(nsteps, true, err)) return fail(DG_ERR_CUDA, err);
-  if (q_out) CKC(cudaMemcpyAsync(q_out, h->s.d.q, n, cudaMemcpyDeviceToHost, h->s.stream));
+  if (q_out && nsteps > 0) {
+    // the last step hands each range of cells to the copy engines as soon as it is final
+    if (h->s.step(nsteps - 1, true, err) || h->s.step_to_host(q_out, err)) return fail(DG_ERR_CUDA, err);
+  } else {
+    if (h->s.step(nsteps, true, err)) return fail(DG_ERR_CUDA, err);
+    if (q_out) CKC(cudaMemcpyAsync(q_out, h->s.d.q, n, cudaMemcpyDeviceToHost, h->s.stream));
+  }
   CKC(cudaStreamSynchronize(h->s.stream));
   return 0;
 }

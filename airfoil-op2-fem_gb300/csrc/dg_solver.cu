@@ -191,6 +191,18 @@ __global__ void __launch_bounds__(256) face_kernel(const Inst d, const int stage
   face_node<N>(d, stage, tid);
 }
 
+// double -> float by truncation of the bit pattern, with integer instructions only (the
+// conversion instruction occupies the FP64 pipe).  Relative error below 2^-23; magnitudes below
+// 2^-126 give +-0, above the float range (and inf, NaN) +-inf.  For the dt estimate only.
+__device__ __forceinline__ float f32_trunc(const double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const uint32_t hi = (uint32_t)(b >> 32), lo = (uint32_t)b;
+  const int e = (int)((hi >> 20) & 0x7FF) - (1023 - 127);
+  const uint32_t sign = hi & 0x80000000u;
+  const uint32_t mag = e <= 0 ? 0u : (e >= 255 ? 0x7F800000u : (((uint32_t)e << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29)));
+  return __uint_as_float(sign | mag);
+}
+
 // SSPRK3 stage combine of one node's right-hand side (r0..r3), and in the last stage the
 // calc_dt maximum.  Every thread of the block calls it: `active` is false for warps beyond the
 // Np node-warps of a wider block (they only take part in the barrier), `live` is false for
@@ -253,8 +265,9 @@ __device__ __forceinline__ void stage_combine(const Inst &d, const int stage, co
     // src/calc_dt.h: (N+1)^2 * 0.5 * fscale * (|v| + c) at the face points of this node, maximised
     // over the block.  A single-precision estimate finds the block's candidates first; only
     // those within 1e-4 of the block's estimated maximum are evaluated in FP64.  The FP32
-    // estimate is within ~1e-6 of the FP64 value, so the block's true maximum is always a
-    // candidate and the result equals the all-FP64 maximum.  (Measured cost of the whole
+    // estimate (from bit-truncated copies of the state, f32_trunc) is within ~1e-6 of the FP64
+    // value, so the block's true maximum is always a candidate and the result equals the
+    // all-FP64 maximum.  (Measured cost of the whole
     // reduction on the K=32768, N=3 benchmark: 6.2 us of an 86 us stage-2 launch.)
     __shared__ float s_wmax[32];
     __shared__ int s_ncand;
@@ -264,9 +277,9 @@ __device__ __forceinline__ void stage_combine(const Inst &d, const int stage, co
     if (live && fa >= 0) {
       const float *gf = reinterpret_cast<const float *>(ge + 14);  // fscale per face, single precision
       const float fsf = fb >= 0 ? fmaxf(gf[fa], gf[fb]) : gf[fa];
-      const float rho = (float)n0, ir = 1.0f / rho, u = (float)n1 * ir, v = (float)n2 * ir;
+      const float rho = f32_trunc(n0), ir = 1.0f / rho, u = f32_trunc(n1) * ir, v = f32_trunc(n2) * ir;
       const float v2 = u * u + v * v;
-      const float p = P.gm1f * ((float)n3 - 0.5f * rho * v2);
+      const float p = P.gm1f * (f32_trunc(n3) - 0.5f * rho * v2);
       const float cs = sqrtf(fabsf(P.gamf * p * ir));
       est = ((N + 1) * (N + 1) * 0.5f) * (sqrtf(v2) + cs) * fsf;
       if (!(est == est) || est > 3.0e38f) est = 3.0e38f;  // non-finite: always a candidate
@@ -545,11 +558,12 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
 
 // MB: minimum resident blocks per SM the register allocation must allow (3 for the tensor-core
 // form: 64 registers; without the bound it takes ~95 and runs two blocks per SM, measured slower).
+// tile0: first 32-cell tile of this launch (a launch may cover a range of the tiles).
 template <int N, bool TC, int MB = 1>
-__global__ void __launch_bounds__(32 * np_of(N), MB) elem_kernel_sym(const Inst d, const int stage) {
+__global__ void __launch_bounds__(32 * np_of(N), MB) elem_kernel_sym(const Inst d, const int stage, const int tile0) {
   extern __shared__ double2 Xs[];  // [NK][32] x 4 doubles, then [Np][32] x 4 doubles
   pdl_trigger();  // the next face kernel may be scheduled (it waits for this grid's writes)
-  elem_tile_sym<N, true, TC>(d, stage, blockIdx.x * 32, threadIdx.x, threadIdx.y, Xs);
+  elem_tile_sym<N, true, TC>(d, stage, (tile0 + (int)blockIdx.x) * 32, threadIdx.x, threadIdx.y, Xs);
 }
 
 // ---------------------------------------------------------------- per-step finalize
@@ -779,13 +793,24 @@ static void launch_elem(const Inst &d, int stage, cudaStream_t s) {
   if (g_elem_variant) {
     const size_t smem = (size_t)(NK + Np) * 32 * 4 * sizeof(double);
     if (g_elem_variant == 2 && oz_used(N, true))
-      launch_pdl(elem_kernel_sym<N, true, 3>, dim3((d.K + 31) / 32), dim3(32, Np), smem, s, d, stage);
+      launch_pdl(elem_kernel_sym<N, true, 3>, dim3((d.K + 31) / 32), dim3(32, Np), smem, s, d, stage, 0);
     else
-      launch_pdl(elem_kernel_sym<N, false>, dim3((d.K + 31) / 32), dim3(32, Np), smem, s, d, stage);
+      launch_pdl(elem_kernel_sym<N, false>, dim3((d.K + 31) / 32), dim3(32, Np), smem, s, d, stage, 0);
   } else {
     const size_t smem = (size_t)NK * 32 * 4 * sizeof(double);
     launch_pdl(elem_kernel<N>, dim3((d.K + 31) / 32), dim3(32, Np), smem, s, d, stage);
   }
+}
+
+// Element tiles [t0, t1) of one stage, in plain stream order on s (the even/odd forms only).
+template <int N>
+static void launch_elem_tiles(const Inst &d, int stage, int t0, int t1, cudaStream_t s) {
+  constexpr int Np = np_of(N), NK = nk_of(N);
+  const size_t smem = (size_t)(NK + Np) * 32 * 4 * sizeof(double);
+  if (g_elem_variant == 2 && oz_used(N, true))
+    elem_kernel_sym<N, true, 3><<<t1 - t0, dim3(32, Np), smem, s>>>(d, stage, t0);
+  else
+    elem_kernel_sym<N, false><<<t1 - t0, dim3(32, Np), smem, s>>>(d, stage, t0);
 }
 
 template <int N>
@@ -959,6 +984,12 @@ void set_face_block(int b) { g_face_block = (b >= 32 && b <= 256 && b % 32 == 0)
   } while (0)
 
 Solver::~Solver() {
+  for (int c = 0; c < kOutChunks; c++) {
+    if (out_streams[c]) cudaStreamDestroy(out_streams[c]);
+    if (out_kern[c]) cudaEventDestroy(out_kern[c]);
+    if (out_copy[c]) cudaEventDestroy(out_copy[c]);
+  }
+  if (out_fork) cudaEventDestroy(out_fork);
   if (graph_exec) cudaGraphExecDestroy(graph_exec);
   if (graph) cudaGraphDestroy(graph);
   for (void *p : allocs) cudaFree(p);
@@ -1114,6 +1145,49 @@ int Solver::build_graph(std::string &err) {
   cudaError_t ce = cudaStreamEndCapture(stream, &graph);
   if (ce != cudaSuccess) { err = std::string("graph capture: ") + cudaGetErrorString(ce); return -6; }
   CK(cudaGraphInstantiate(&graph_exec, graph, 0));
+  return 0;
+}
+
+int Solver::step_to_host(double *q_out, std::string &err) {
+  if (!g_elem_variant) {  // the dense form has no tile ranges: whole step, then one copy
+    enqueue_step(stream);
+    CK(cudaMemcpyAsync(q_out, d.q, q_count() * 8, cudaMemcpyDeviceToHost, stream));
+    return 0;
+  }
+  if (!out_fork) {
+    int lo = 0, hi = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));  // hi: the highest priority (numerically least)
+    for (int c = 0; c < kOutChunks; c++) {
+      const int prio = hi + (lo - hi) * c / (kOutChunks - 1);
+      CK(cudaStreamCreateWithPriority(&out_streams[c], cudaStreamNonBlocking, prio));
+      CK(cudaEventCreateWithFlags(&out_kern[c], cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&out_copy[c], cudaEventDisableTiming));
+    }
+    CK(cudaEventCreateWithFlags(&out_fork, cudaEventDisableTiming));
+  }
+  const int N = cfg.N, Np = (N + 1) * (N + 2) / 2, T = (K + 31) / 32;
+  DG_DISPATCH(N, (launch_stage<NN>(d, 0, stream), launch_stage<NN>(d, 1, stream), launch_face<NN>(d, 2, stream)));
+  CK(cudaEventRecord(out_fork, stream));
+  // Ranges on streams of falling priority: the block scheduler runs the first range's tiles
+  // first, so its q is final (and on its way to the host) while the later ranges compute.
+  for (int c = 0; c < kOutChunks; c++) {
+    const int t0 = (int)((long long)T * c / kOutChunks), t1 = (int)((long long)T * (c + 1) / kOutChunks);
+    cudaStream_t cs = out_streams[c];
+    CK(cudaStreamWaitEvent(cs, out_fork, 0));
+    if (t1 > t0) {
+      DG_DISPATCH(N, launch_elem_tiles<NN>(d, 2, t0, t1, cs));
+      CK(cudaGetLastError());
+    }
+    CK(cudaEventRecord(out_kern[c], cs));
+    const size_t e0 = (size_t)t0 * 32, e1 = std::min((size_t)t1 * 32, (size_t)K);
+    if (e1 > e0)
+      CK(cudaMemcpyAsync(q_out + e0 * Np * 4, d.q + e0 * Np * 4, (e1 - e0) * Np * 4 * 8, cudaMemcpyDeviceToHost, cs));
+    CK(cudaEventRecord(out_copy[c], cs));
+  }
+  for (int c = 0; c < kOutChunks; c++) CK(cudaStreamWaitEvent(stream, out_kern[c], 0));
+  finalize_kernel<<<1, 32, 0, stream>>>(d.st, d.dt_mode, d.dt_hist, d.dt_hist_len);
+  CK(cudaGetLastError());
+  for (int c = 0; c < kOutChunks; c++) CK(cudaStreamWaitEvent(stream, out_copy[c], 0));
   return 0;
 }
 

@@ -178,6 +178,40 @@ def test_step_host_pinned_buffers_equal_run(pkg, omesh, nsteps):
     assert np.array_equal(a.get("q"), b.get("q")) and a.time() == b.time()
 
 
+@pytest.mark.parametrize("variant", [0, 1, 2])
+@pytest.mark.parametrize("case", ["ogrid_n3", "ogrid_n4", "tiny_n3", "vortex_n3"])
+def test_step_host_ranges_equal_run(pkg, omesh, variant, case):
+    """The host-buffer call's last step runs its final element kernel as four ranges of cells
+    on separate streams, each copied back as soon as it is final: bitwise the graph step, for
+    every element-kernel form, with fewer tiles than ranges and with the time-dependent vortex
+    boundary."""
+    if case == "vortex_n3":
+        m = omesh.vortex_square(16)
+        cfg = pkg.config(N=3, app=pkg.APP_VORTEX, dt_mode=pkg.DT_FROZEN, cfl=0.5, vortex_x0=0.0,
+                         vortex_y0=0.0, vortex_beta=5.0)
+    else:
+        m = omesh.naca_ogrid(8, 4) if case == "tiny_n3" else omesh.naca_ogrid(64, 16)
+        cfg = pkg.config(N=4 if case == "ogrid_n4" else 3, cfl=0.5)
+    prev = pkg.lib().dg_elem_variant()
+    pkg.lib().dg_set_elem_variant(variant)
+    try:
+        a = pkg.Solver(pkg.Mesh.from_tables(m), cfg).init()
+        b = pkg.Solver(pkg.Mesh.from_tables(m), cfg).init()
+        q = a.get("q")
+        h_in, h_out = pkg.PinnedArray(q.size), pkg.PinnedArray(q.size)
+        h_in.array[:] = q
+        h_out.array[:] = np.nan
+        for _ in range(3):
+            a.step_host(h_in.array, 2, h_out.array)
+            h_in.array[:] = h_out.array
+        b.run(6)
+        b.sync()
+        assert np.array_equal(h_out.array, b.get("q"))
+        assert np.array_equal(a.get("q"), b.get("q")) and a.time() == b.time()
+    finally:
+        pkg.lib().dg_set_elem_variant(prev)
+
+
 def test_nonphysical_state_is_reported(pkg, omesh):
     """Host-side fault injection: a negative density makes the kernel's guard flag fire and
     the host call return DG_ERR_NONPHYSICAL; the context stays usable."""
