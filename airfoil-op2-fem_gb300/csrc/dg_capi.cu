@@ -353,17 +353,25 @@ int dg_solver_dt_history(dg_solver_t *h, double *out, int n) {
 int dg_solver_step_host(dg_solver_t *h, const double *q_in, int nsteps, double *q_out) {
   if (!h || nsteps < 0) return fail(DG_ERR_ARG, "bad arguments");
   const size_t n = h->s.q_count() * 8;
-  if (q_in) {
-    CKC(cudaMemcpyAsync(h->s.d.q, q_in, n, cudaMemcpyHostToDevice, h->s.stream));
-    CKC(cudaMemcpyAsync(h->s.d.W, h->s.d.q, n, cudaMemcpyDeviceToDevice, h->s.stream));
-  }
   std::string err;
-  if (q_out && nsteps > 0) {
-    // the last step hands each range of cells to the copy engines as soon as it is final
-    if (h->s.step(nsteps - 1, true, err) || h->s.step_to_host(q_out, err)) return fail(DG_ERR_CUDA, err);
-  } else {
-    if (h->s.step(nsteps, true, err)) return fail(DG_ERR_CUDA, err);
+  if (nsteps == 0) {
+    if (q_in) {
+      CKC(cudaMemcpyAsync(h->s.d.q, q_in, n, cudaMemcpyHostToDevice, h->s.stream));
+      CKC(cudaMemcpyAsync(h->s.d.W, h->s.d.q, n, cudaMemcpyDeviceToDevice, h->s.stream));
+    }
     if (q_out) CKC(cudaMemcpyAsync(q_out, h->s.d.q, n, cudaMemcpyDeviceToHost, h->s.stream));
+  } else {
+    // the first step takes the input range by range, the last hands out its result range by
+    // range (one step: both); the steps between are graph launches
+    int rc = 0;
+    if (nsteps == 1) {
+      rc = h->s.step_io(q_in, q_out, err);
+    } else {
+      rc = (q_in ? h->s.step_io(q_in, nullptr, err) : h->s.step(1, true, err));
+      if (!rc) rc = h->s.step(nsteps - 2, true, err);
+      if (!rc) rc = (q_out ? h->s.step_io(nullptr, q_out, err) : h->s.step(1, true, err));
+    }
+    if (rc) return fail(DG_ERR_CUDA, err);
   }
   CKC(cudaStreamSynchronize(h->s.stream));
   return 0;

@@ -985,11 +985,11 @@ void set_face_block(int b) { g_face_block = (b >= 32 && b <= 256 && b % 32 == 0)
 
 Solver::~Solver() {
   for (int c = 0; c < kOutChunks; c++) {
-    if (out_streams[c]) cudaStreamDestroy(out_streams[c]);
-    if (out_kern[c]) cudaEventDestroy(out_kern[c]);
-    if (out_copy[c]) cudaEventDestroy(out_copy[c]);
+    if (io_streams[c]) cudaStreamDestroy(io_streams[c]);
+    if (io_kern[c]) cudaEventDestroy(io_kern[c]);
+    if (io_copy[c]) cudaEventDestroy(io_copy[c]);
   }
-  if (out_fork) cudaEventDestroy(out_fork);
+  if (io_fork) cudaEventDestroy(io_fork);
   if (graph_exec) cudaGraphExecDestroy(graph_exec);
   if (graph) cudaGraphDestroy(graph);
   for (void *p : allocs) cudaFree(p);
@@ -1148,46 +1148,68 @@ int Solver::build_graph(std::string &err) {
   return 0;
 }
 
-int Solver::step_to_host(double *q_out, std::string &err) {
-  if (!g_elem_variant) {  // the dense form has no tile ranges: whole step, then one copy
+int Solver::step_io(const double *q_in, double *q_out, std::string &err) {
+  if (!g_elem_variant) {  // the dense form has no tile ranges: plain copies around a whole step
+    const size_t n = q_count() * 8;
+    if (q_in) {
+      CK(cudaMemcpyAsync(d.q, q_in, n, cudaMemcpyHostToDevice, stream));
+      CK(cudaMemcpyAsync(d.W, d.q, n, cudaMemcpyDeviceToDevice, stream));
+    }
     enqueue_step(stream);
-    CK(cudaMemcpyAsync(q_out, d.q, q_count() * 8, cudaMemcpyDeviceToHost, stream));
+    if (q_out) CK(cudaMemcpyAsync(q_out, d.q, n, cudaMemcpyDeviceToHost, stream));
     return 0;
   }
-  if (!out_fork) {
+  if (!io_fork) {
     int lo = 0, hi = 0;
     CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));  // hi: the highest priority (numerically least)
     for (int c = 0; c < kOutChunks; c++) {
       const int prio = hi + (lo - hi) * c / (kOutChunks - 1);
-      CK(cudaStreamCreateWithPriority(&out_streams[c], cudaStreamNonBlocking, prio));
-      CK(cudaEventCreateWithFlags(&out_kern[c], cudaEventDisableTiming));
-      CK(cudaEventCreateWithFlags(&out_copy[c], cudaEventDisableTiming));
+      CK(cudaStreamCreateWithPriority(&io_streams[c], cudaStreamNonBlocking, prio));
+      CK(cudaEventCreateWithFlags(&io_kern[c], cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&io_copy[c], cudaEventDisableTiming));
     }
-    CK(cudaEventCreateWithFlags(&out_fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&io_fork, cudaEventDisableTiming));
   }
   const int N = cfg.N, Np = (N + 1) * (N + 2) / 2, T = (K + 31) / 32;
-  DG_DISPATCH(N, (launch_stage<NN>(d, 0, stream), launch_stage<NN>(d, 1, stream), launch_face<NN>(d, 2, stream)));
-  CK(cudaEventRecord(out_fork, stream));
-  // Ranges on streams of falling priority: the block scheduler runs the first range's tiles
-  // first, so its q is final (and on its way to the host) while the later ranges compute.
+  const size_t cell_doubles = (size_t)Np * 4;
+  if (q_in) {
+    // one upload: split into ranges and overlapped with the first face kernel it saved ~4 us of
+    // 52, since host<->device copies slow the running kernels by about two thirds of their
+    // own time on this part
+    CK(cudaMemcpyAsync(d.q, q_in, q_count() * 8, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemcpyAsync(d.W, d.q, q_count() * 8, cudaMemcpyDeviceToDevice, stream));
+  }
+  DG_DISPATCH(N, launch_stage<NN>(d, 0, stream));
+  DG_DISPATCH(N, (launch_stage<NN>(d, 1, stream), launch_face<NN>(d, 2, stream)));
+  if (!q_out) {
+    DG_DISPATCH(N, launch_elem<NN>(d, 2, stream));
+    finalize_kernel<<<1, 32, 0, stream>>>(d.st, d.dt_mode, d.dt_hist, d.dt_hist_len);
+    CK(cudaGetLastError());
+    return 0;
+  }
+  CK(cudaEventRecord(io_fork, stream));
+  // The last element kernel as ranges of tiles on streams of falling priority: the block
+  // scheduler runs the first range's tiles first, so its q is final (and on its way to the host)
+  // while the later ranges compute.
   for (int c = 0; c < kOutChunks; c++) {
     const int t0 = (int)((long long)T * c / kOutChunks), t1 = (int)((long long)T * (c + 1) / kOutChunks);
-    cudaStream_t cs = out_streams[c];
-    CK(cudaStreamWaitEvent(cs, out_fork, 0));
+    cudaStream_t cs = io_streams[c];
+    CK(cudaStreamWaitEvent(cs, io_fork, 0));
     if (t1 > t0) {
       DG_DISPATCH(N, launch_elem_tiles<NN>(d, 2, t0, t1, cs));
       CK(cudaGetLastError());
     }
-    CK(cudaEventRecord(out_kern[c], cs));
+    CK(cudaEventRecord(io_kern[c], cs));
     const size_t e0 = (size_t)t0 * 32, e1 = std::min((size_t)t1 * 32, (size_t)K);
     if (e1 > e0)
-      CK(cudaMemcpyAsync(q_out + e0 * Np * 4, d.q + e0 * Np * 4, (e1 - e0) * Np * 4 * 8, cudaMemcpyDeviceToHost, cs));
-    CK(cudaEventRecord(out_copy[c], cs));
+      CK(cudaMemcpyAsync(q_out + e0 * cell_doubles, d.q + e0 * cell_doubles, (e1 - e0) * cell_doubles * 8,
+                         cudaMemcpyDeviceToHost, cs));
+    CK(cudaEventRecord(io_copy[c], cs));
   }
-  for (int c = 0; c < kOutChunks; c++) CK(cudaStreamWaitEvent(stream, out_kern[c], 0));
+  for (int c = 0; c < kOutChunks; c++) CK(cudaStreamWaitEvent(stream, io_kern[c], 0));
   finalize_kernel<<<1, 32, 0, stream>>>(d.st, d.dt_mode, d.dt_hist, d.dt_hist_len);
   CK(cudaGetLastError());
-  for (int c = 0; c < kOutChunks; c++) CK(cudaStreamWaitEvent(stream, out_copy[c], 0));
+  for (int c = 0; c < kOutChunks; c++) CK(cudaStreamWaitEvent(stream, io_copy[c], 0));
   return 0;
 }
 

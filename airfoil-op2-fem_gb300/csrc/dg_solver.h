@@ -76,13 +76,14 @@ struct Solver {
   void enqueue_step_events(cudaStream_t s, cudaEvent_t *ev);
   int build_graph(std::string &err);
   int step(int nsteps, bool use_graph, std::string &err);
-  // One step whose last element kernel runs as kOutChunks cell ranges on streams of falling
-  // priority, each range's new q copied to q_out (host) as soon as it is written; then the
-  // finalize kernel.  Returns when the work is enqueued (wait on `stream`).
-  int step_to_host(double *q_out, std::string &err);
+  // One step with host buffers at either end (either may be null): q_in is uploaded first; the
+  // last element kernel runs as kOutChunks ranges of tiles on streams of falling priority and
+  // each range's new q goes to q_out as soon as it is written.  Enqueues only (wait on
+  // `stream`); bitwise the same step as enqueue_step.
+  int step_io(const double *q_in, double *q_out, std::string &err);
   static constexpr int kOutChunks = 4;
-  cudaStream_t out_streams[kOutChunks] = {};
-  cudaEvent_t out_fork = nullptr, out_kern[kOutChunks] = {}, out_copy[kOutChunks] = {};
+  cudaStream_t io_streams[kOutChunks] = {};
+  cudaEvent_t io_fork = nullptr, io_kern[kOutChunks] = {}, io_copy[kOutChunks] = {};
   int rhs(double *out_dev, std::string &err);
   int l2_error(double err4[4], std::string &err);
   int state(StepState &s, std::string &err);
