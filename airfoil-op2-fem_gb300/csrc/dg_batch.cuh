@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(256) batch_face_kernel(const Inst *insts, cons
 }
 
 template <int N, bool TC>
-__global__ void __launch_bounds__(32 * np_of(N), oz_used(N, TC) ? 3 : 1) batch_elem_kernel(const Inst *insts, const int4 *etiles,
+__global__ void __launch_bounds__(32 * np_of(N), oz_used(N, TC) ? oz_min_blocks(N) : 1) batch_elem_kernel(const Inst *insts, const int4 *etiles,
                                                                                 const int first, const int stage) {
   extern __shared__ double2 Xg[];
   const int4 et = etiles[first + blockIdx.x];

@@ -26,16 +26,19 @@
 //
 // Units of work: parity x 8 groups of 4 cells (x 4 variables) = 16 m16n8k16 row tiles per
 // 32-cell tile; each needs 28 mma per k-step of 16 slots.  Non-finite inputs in a column give NaN.
-// Supported for N <= 3 (each parity has at most 8 operator rows: one n-tile); used at N = 3.
+// Each row tile takes the operator rows 8 at a time (one n-tile of mma).
 
-__constant__ int c_ozf[7][2][8];  // biased binary exponent F of every operator row (order, parity, row)
-__device__ uint2 g_ozb[7][2][7][2][32];  // B fragments: order, parity, digit s, k-step, lane
+__constant__ int c_ozf[7][2][16];  // biased binary exponent F of every operator row (order, parity, row)
+__device__ uint2 g_ozb[7][2][2][7][2][32];  // B fragments: order, parity, n-tile, digit s, k-step, lane
 
-// Orders that use it: N = 3 (measured on the K=32768 O-grid: step 367 -> 331 us).  At N = 1 and 2
-// the contraction is too small a share of the element kernel and the split costs more than it
-// saves (N = 1: 184 -> 192 us, N = 2: 236 -> 252 us); N >= 4 needs more than one n-tile.
-constexpr int kOzMinN = 3, kOzMaxN = 3;
-constexpr bool oz_used(int N, bool tc) { return tc && N >= kOzMinN && N <= kOzMaxN; }
+// Orders that use it: N = 3, 4, 5 (steps on the K=32768 O-grid: 365 -> 328, 564 -> 477,
+// 909 -> 720 us).  At N = 1 and 2 the contraction is too small a share of the element kernel and
+// the split costs more than it saves (N = 1: 184 -> 192 us, N = 2: 236 -> 252 us).  Orders up to
+// 5 fit the exactness bound (at most two k-steps of 16 slots); N = 6 needs three.
+constexpr int kOzMaxN = 5;
+constexpr bool oz_used(int N, bool tc) { return tc && (N == 3 || N == 4 || N == 5); }
+// Minimum resident blocks per SM for the element kernel's register allocation in this form.
+constexpr int oz_min_blocks(int N) { return N <= 3 ? 3 : (N == 4 ? 2 : 1); }
 
 __device__ __forceinline__ void mma_bf16_16816(float c[4], const uint32_t a[4], const uint2 b) {
   asm volatile(
@@ -61,15 +64,17 @@ __device__ __forceinline__ uint32_t oz_pack(const float f_lo, const float f_hi, 
 
 // One 16-row tile: cells c0..c0+3 x the four variables (row r: cell c0 + r / 4, variable r % 4, so
 // the eight row lanes of a fragment read eight consecutive doubles), slots SLOT0..SLOT0+K-1
-// (K <= 16 KST), times the R operator rows of this parity, written to Y rows YROW0 + n.
-template <int NORD, int K, int R, int SLOT0, int YROW0, int KST, int P>
+// (K <= 16 KST), times operator rows 8 NT .. 8 NT + 7 (of R) of parity P, written to Y rows
+// YROW0 + row.  The k-steps are taken one after the other (their values re-read from shared
+// memory) so that only one k-step's magnitudes are live next to the seven accumulators.
+template <int NORD, int K, int R, int SLOT0, int YROW0, int KST, int P, int NT>
 __device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *__restrict__ Yd, const int c0,
                                         const int lane) {
-  static_assert(R <= 8 && KST <= 2 && K <= 16 * KST, "one n-tile, at most two k-steps");
+  static_assert(KST <= 2 && K <= 16 * KST && R > 8 * NT && NT < 2, "two n-tiles, two k-steps at most");
   const int g = lane >> 2, t = lane & 3;
   const int col = c0 * 4 + g;  // (cell, variable) of row g; row g + 8 is col + 8
-  // staged values of rows (columns of X) c0+g and c0+g+8 at slots 16 ks + {2t, 2t+1, 2t+8, 2t+9}
-  uint32_t hi[KST][2][4], lo[KST][2][4];
+  const uint32_t *Xw = reinterpret_cast<const uint32_t *>(Xd);
+  // largest binary exponent of each of the two columns over all K slots (high words only)
   int em[2] = {0, 0};
 #pragma unroll
   for (int ks = 0; ks < KST; ks++)
@@ -78,57 +83,62 @@ __device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *_
 #pragma unroll
       for (int q = 0; q < 4; q++) {
         const int k = 16 * ks + 2 * t + (q & 1) + ((q >> 1) << 3);
-        const double x = k < K ? Xd[(SLOT0 + k) * 128 + col + 8 * r] : 0.0;
-        const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-        hi[ks][r][q] = (uint32_t)(b >> 32);
-        lo[ks][r][q] = (uint32_t)b;
-        em[r] = max(em[r], (int)((b >> 52) & 0x7FF));
+        if (k < K) em[r] = max(em[r], (int)((Xw[2 * ((SLOT0 + k) * 128 + col + 8 * r) + 1] >> 20) & 0x7FF));
       }
 #pragma unroll
   for (int r = 0; r < 2; r++) {
     em[r] = max(em[r], __shfl_xor_sync(0xffffffffu, em[r], 1));
     em[r] = max(em[r], __shfl_xor_sync(0xffffffffu, em[r], 2));
   }
-  // aligned magnitudes m = M 2^(e - E + 3) (M the 53-bit significand) and the sign pattern of
-  // every A-fragment register (pairs (g: q0 q1), (g+8: q0 q1), (g: q2 q3), (g+8: q2 q3))
-  uint32_t sgn[KST][4];
+  const uint2 *bfr = &g_ozb[NORD][P][NT][0][0][lane];
+  float acc[7][4];
+#pragma unroll
+  for (int l = 0; l < 7; l++) acc[l][0] = acc[l][1] = acc[l][2] = acc[l][3] = 0.0f;
 #pragma unroll
   for (int ks = 0; ks < KST; ks++) {
+    // this k-step's values at slots 16 ks + {2t, 2t+1, 2t+8, 2t+9}: aligned magnitudes
+    // m = M 2^(e - E + 3) (M the 53-bit significand) and the sign pattern of every A-fragment
+    // register (pairs (g: q0 q1), (g+8: q0 q1), (g: q2 q3), (g+8: q2 q3))
+    uint32_t hi[2][4], lo[2][4];
+#pragma unroll
+    for (int r = 0; r < 2; r++)
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const int k = 16 * ks + 2 * t + (q & 1) + ((q >> 1) << 3);
+        const double x = k < K ? Xd[(SLOT0 + k) * 128 + col + 8 * r] : 0.0;
+        const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+        hi[r][q] = (uint32_t)(b >> 32);
+        lo[r][q] = (uint32_t)b;
+      }
+    uint32_t sgn[4];
 #pragma unroll
     for (int x = 0; x < 4; x++) {
       const int r = x & 1, q0 = (x >> 1) * 2;
-      sgn[ks][x] = ((hi[ks][r][q0] >> 16) & 0x8000u) | (hi[ks][r][q0 + 1] & 0x80000000u);
+      sgn[x] = ((hi[r][q0] >> 16) & 0x8000u) | (hi[r][q0 + 1] & 0x80000000u);
     }
 #pragma unroll
     for (int r = 0; r < 2; r++)
 #pragma unroll
       for (int q = 0; q < 4; q++) {
-        const uint32_t h = hi[ks][r][q];
+        const uint32_t h = hi[r][q];
         const int e = (int)((h >> 20) & 0x7FF);
         const unsigned long long M =
-            e ? ((((unsigned long long)(h & 0xFFFFFu)) << 32) | lo[ks][r][q]) | (1ull << 52) : 0ull;
+            e ? ((((unsigned long long)(h & 0xFFFFFu)) << 32) | lo[r][q]) | (1ull << 52) : 0ull;
         const int sh = e - em[r] + 3;
         const unsigned long long m = sh >= 0 ? (M << sh) : (sh > -64 ? (M >> -sh) : 0ull);
-        hi[ks][r][q] = (uint32_t)(m >> 32);
-        lo[ks][r][q] = (uint32_t)m;
+        hi[r][q] = (uint32_t)(m >> 32);
+        lo[r][q] = (uint32_t)m;
       }
-  }
-  const uint2 *bfr = &g_ozb[NORD][P][0][0][lane];
-  float acc[7][4];
 #pragma unroll
-  for (int l = 0; l < 7; l++) acc[l][0] = acc[l][1] = acc[l][2] = acc[l][3] = 0.0f;
-#pragma unroll
-  for (int j = 0; j < 7; j++) {
-#pragma unroll
-    for (int ks = 0; ks < KST; ks++) {
+    for (int j = 0; j < 7; j++) {
       float f[2][4];
 #pragma unroll
       for (int r = 0; r < 2; r++)
 #pragma unroll
-        for (int q = 0; q < 4; q++) f[r][q] = oz_digit(hi[ks][r][q], lo[ks][r][q], j);
+        for (int q = 0; q < 4; q++) f[r][q] = oz_digit(hi[r][q], lo[r][q], j);
       // A fragment (row-major 16 x 16): rows g / g+8, slots 2t..2t+1 / 2t+8..2t+9
-      const uint32_t a[4] = {oz_pack(f[0][0], f[0][1], sgn[ks][0]), oz_pack(f[1][0], f[1][1], sgn[ks][1]),
-                             oz_pack(f[0][2], f[0][3], sgn[ks][2]), oz_pack(f[1][2], f[1][3], sgn[ks][3])};
+      const uint32_t a[4] = {oz_pack(f[0][0], f[0][1], sgn[0]), oz_pack(f[1][0], f[1][1], sgn[1]),
+                             oz_pack(f[0][2], f[0][3], sgn[2]), oz_pack(f[1][2], f[1][3], sgn[3])};
 #pragma unroll
       for (int s = 0; s + j < 7; s++) mma_bf16_16816(acc[j + s], a, __ldg(bfr + (s * 2 + ks) * 32));
     }
@@ -138,7 +148,7 @@ __device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *_
   for (int r = 0; r < 2; r++)
 #pragma unroll
     for (int cc = 0; cc < 2; cc++) {
-      const int n = 2 * t + cc;
+      const int n = 8 * NT + 2 * t + cc;
       if (n < R) {
         const int o = 2 * r + cc;
         long long l[7];
@@ -174,15 +184,27 @@ __device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *_
 }
 
 // Both parities of one 32-cell tile: Y rows 0..NRe-1 from the even slots, NRe.. from the odd
-// slots.  Warp w of nw takes row tiles w, w + nw, ... of the 16 (8 per parity, 4 cells each).
+// slots.  Work units: (parity, n-tile of 8 operator rows, group of 4 cells); warp w of nw takes
+// units w, w + nw, ...
 template <int N, int NUe, int NUo, int NRe, int NRo>
 __device__ __forceinline__ void oz_contract(const double *Xd, double *Yd, const int warp, const int nw,
                                             const int lane) {
-  constexpr int KE = (NUe + 15) / 16, KO = (NUo + 15) / 16;
-  for (int u = warp; u < 16; u += nw) {
-    const int c0 = (u & 7) * 4;
-    if (u < 8) oz_tile<N, NUe, NRe, 0, 0, KE, 0>(Xd, Yd, c0, lane);
-    else oz_tile<N, NUo, NRo, NUe, NRe, KO, 1>(Xd, Yd, c0, lane);
+  constexpr int KE = (NUe + 15) / 16, KO = (NUo + 15) / 16, NTE = (NRe + 7) / 8, NTO = (NRo + 7) / 8;
+  for (int u = warp; u < 8 * (NTE + NTO); u += nw) {
+    const int c0 = (u & 7) * 4, w = u >> 3;
+    if (w < NTE) {
+      if (w == 0) {
+        oz_tile<N, NUe, NRe, 0, 0, KE, 0, 0>(Xd, Yd, c0, lane);
+      } else {
+        if constexpr (NTE > 1) oz_tile<N, NUe, NRe, 0, 0, KE, 0, 1>(Xd, Yd, c0, lane);
+      }
+    } else {
+      if (w == NTE) {
+        oz_tile<N, NUo, NRo, NUe, NRe, KO, 1, 0>(Xd, Yd, c0, lane);
+      } else {
+        if constexpr (NTO > 1) oz_tile<N, NUo, NRo, NUe, NRe, KO, 1, 1>(Xd, Yd, c0, lane);
+      }
+    }
   }
 }
 
@@ -198,14 +220,14 @@ static uint32_t oz_bf16_bits(int d) {
 
 static int oz_upload(int N, const std::vector<double> &S, int NUe, int NUo, int NRe, int NRo, std::string &err) {
   if (!oz_used(N, true)) return 0;
-  int fexp[2][8] = {};
-  static uint2 frag[2][7][2][32];
+  int fexp[2][16] = {};
+  static uint2 frag[2][2][7][2][32];
   std::memset(frag, 0, sizeof(frag));
   for (int p = 0; p < 2; p++) {
     const int K = p ? NUo : NUe, R = p ? NRo : NRe;
     const size_t base = p ? (size_t)NRe * NUe : 0;
-    if (R > 8 || K > 32) { err = "tensor-core contraction: operator too large"; return -4; }
-    std::vector<int> dig((size_t)7 * 32 * 8, 0);  // [s][k][n]
+    if (R > 16 || K > 32) { err = "tensor-core contraction: operator too large"; return -4; }
+    std::vector<int> dig((size_t)7 * 32 * 16, 0);  // [s][k][n]
     for (int n = 0; n < R; n++) {
       int F = 0;
       for (int k = 0; k < K; k++) {
@@ -223,17 +245,18 @@ static int oz_upload(int N, const std::vector<double> &S, int NUe, int NUo, int 
         const int sh = e - F + 3;
         const uint64_t m = sh >= 0 ? (M << sh) : (sh > -64 ? (M >> -sh) : 0);
         const int sg = (b >> 63) ? -1 : 1;
-        for (int s = 0; s < 7; s++) dig[((size_t)s * 32 + k) * 8 + n] = sg * (int)((m >> (8 * (6 - s))) & 255);
+        for (int s = 0; s < 7; s++) dig[((size_t)s * 32 + k) * 16 + n] = sg * (int)((m >> (8 * (6 - s))) & 255);
       }
     }
-    for (int s = 0; s < 7; s++)
-      for (int ks = 0; ks < 2; ks++)
-        for (int lane = 0; lane < 32; lane++) {
-          const int g = lane >> 2, t = lane & 3, k0 = 16 * ks + 2 * t;
-          auto D = [&](int k) { return k < 32 ? dig[((size_t)s * 32 + k) * 8 + g] : 0; };
-          frag[p][s][ks][lane].x = oz_bf16_bits(D(k0)) | (oz_bf16_bits(D(k0 + 1)) << 16);
-          frag[p][s][ks][lane].y = oz_bf16_bits(D(k0 + 8)) | (oz_bf16_bits(D(k0 + 9)) << 16);
-        }
+    for (int nt = 0; nt < 2; nt++)
+      for (int s = 0; s < 7; s++)
+        for (int ks = 0; ks < 2; ks++)
+          for (int lane = 0; lane < 32; lane++) {
+            const int g = lane >> 2, t = lane & 3, k0 = 16 * ks + 2 * t;
+            auto D = [&](int k) { return k < 32 ? dig[((size_t)s * 32 + k) * 16 + 8 * nt + g] : 0; };
+            frag[p][nt][s][ks][lane].x = oz_bf16_bits(D(k0)) | (oz_bf16_bits(D(k0 + 1)) << 16);
+            frag[p][nt][s][ks][lane].y = oz_bf16_bits(D(k0 + 8)) | (oz_bf16_bits(D(k0 + 9)) << 16);
+          }
   }
   cudaError_t ce = cudaMemcpyToSymbol(c_ozf, fexp, sizeof(fexp), (size_t)N * sizeof(fexp));
   if (ce == cudaSuccess) ce = cudaMemcpyToSymbol(g_ozb, frag, sizeof(frag), (size_t)N * sizeof(frag));

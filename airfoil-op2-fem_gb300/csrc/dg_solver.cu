@@ -556,8 +556,9 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
   __syncthreads();
 }
 
-// MB: minimum resident blocks per SM the register allocation must allow (3 for the tensor-core
-// form: 64 registers; without the bound it takes ~95 and runs two blocks per SM, measured slower).
+// MB: minimum resident blocks per SM the register allocation must allow (oz_min_blocks for the
+// tensor-core form; at N = 3 without the bound it takes ~95 registers and runs two blocks per SM,
+// measured slower).
 // tile0: first 32-cell tile of this launch (a launch may cover a range of the tiles).
 template <int N, bool TC, int MB = 1>
 __global__ void __launch_bounds__(32 * np_of(N), MB) elem_kernel_sym(const Inst d, const int stage, const int tile0) {
@@ -783,8 +784,8 @@ static void launch_face(const Inst &d, int stage, cudaStream_t s) {
   launch_pdl(face_kernel<N>, dim3((nf + bs - 1) / bs), dim3(bs), 0, s, d, stage);
 }
 
-// 2: even/odd with the contraction on the bf16 tensor cores (dg_ozaki.cuh; at N = 3, the even/odd
-// FP64 kernel at the other orders; default), 1: even/odd element kernel, 0: dense element kernel.
+// 2: even/odd with the contraction on the bf16 tensor cores (dg_ozaki.cuh; at N = 3, 4, 5, the
+// even/odd FP64 kernel at the other orders; default), 1: even/odd element kernel, 0: dense.
 static int g_elem_variant = 2;
 
 template <int N>
@@ -792,10 +793,14 @@ static void launch_elem(const Inst &d, int stage, cudaStream_t s) {
   constexpr int Np = np_of(N), NK = nk_of(N);
   if (g_elem_variant) {
     const size_t smem = (size_t)(NK + Np) * 32 * 4 * sizeof(double);
-    if (g_elem_variant == 2 && oz_used(N, true))
-      launch_pdl(elem_kernel_sym<N, true, 3>, dim3((d.K + 31) / 32), dim3(32, Np), smem, s, d, stage, 0);
-    else
-      launch_pdl(elem_kernel_sym<N, false>, dim3((d.K + 31) / 32), dim3(32, Np), smem, s, d, stage, 0);
+    if constexpr (oz_used(N, true)) {
+      if (g_elem_variant == 2) {
+        launch_pdl(elem_kernel_sym<N, true, oz_min_blocks(N)>, dim3((d.K + 31) / 32), dim3(32, Np), smem, s, d,
+                   stage, 0);
+        return;
+      }
+    }
+    launch_pdl(elem_kernel_sym<N, false>, dim3((d.K + 31) / 32), dim3(32, Np), smem, s, d, stage, 0);
   } else {
     const size_t smem = (size_t)NK * 32 * 4 * sizeof(double);
     launch_pdl(elem_kernel<N>, dim3((d.K + 31) / 32), dim3(32, Np), smem, s, d, stage);
@@ -807,10 +812,13 @@ template <int N>
 static void launch_elem_tiles(const Inst &d, int stage, int t0, int t1, cudaStream_t s) {
   constexpr int Np = np_of(N), NK = nk_of(N);
   const size_t smem = (size_t)(NK + Np) * 32 * 4 * sizeof(double);
-  if (g_elem_variant == 2 && oz_used(N, true))
-    elem_kernel_sym<N, true, 3><<<t1 - t0, dim3(32, Np), smem, s>>>(d, stage, t0);
-  else
-    elem_kernel_sym<N, false><<<t1 - t0, dim3(32, Np), smem, s>>>(d, stage, t0);
+  if constexpr (oz_used(N, true)) {
+    if (g_elem_variant == 2) {
+      elem_kernel_sym<N, true, oz_min_blocks(N)><<<t1 - t0, dim3(32, Np), smem, s>>>(d, stage, t0);
+      return;
+    }
+  }
+  elem_kernel_sym<N, false><<<t1 - t0, dim3(32, Np), smem, s>>>(d, stage, t0);
 }
 
 template <int N>
@@ -826,8 +834,12 @@ static cudaError_t set_smem_attr() {
   if (e != cudaSuccess) return e;
   const size_t smem_sym = (size_t)(nk_of(N) + np_of(N)) * 32 * 4 * sizeof(double);
   e = cudaFuncSetAttribute(elem_kernel_sym<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_sym);
-  if (e != cudaSuccess || !oz_used(N, true)) return e;
-  return cudaFuncSetAttribute(elem_kernel_sym<N, true, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_sym);
+  if constexpr (oz_used(N, true)) {
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(elem_kernel_sym<N, true, oz_min_blocks(N)>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem_sym);
+  }
+  return e;
 }
 
 template <int N>

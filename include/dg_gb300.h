@@ -258,7 +258,7 @@ double dg_fp64_mma_peak_gflops(void);
 int dg_kernels_per_step(void);
 /* Element-kernel form for launches and graphs built from now on: 2 (default) the even/odd split
  * of [Drw | Dsw | -LIFT] with its contraction on the bf16 tensor cores as an exact integer
- * product at order N = 3 and in FP64 at the other orders, 1 the even/odd split in FP64, 0 dense
+ * product at orders N = 3, 4, 5 and in FP64 at the other orders, 1 the even/odd split in FP64, 0 dense
  * FP64 rows.  All compute the same right-hand side to rounding (the tensor-core contraction is
  * the correctly rounded dot product of the 56-bit truncated inputs). */
 void dg_set_elem_variant(int variant);

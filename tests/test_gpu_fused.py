@@ -234,7 +234,7 @@ def test_nonphysical_state_is_reported(pkg, omesh):
 def test_even_odd_form_equals_dense_form(pkg, orc, omesh, N):
     """The element-kernel forms compute the same RHS and steps: dense FP64 rows (0), the even/odd
     split in FP64 (1) and the even/odd split with the tensor-core contraction (2, the default;
-    FP64 at N != 3)."""
+    used at N = 3, 4, 5, FP64 at the other orders)."""
     m = omesh.naca_ogrid(32, 8, farfield="characteristic")
     out = []
     prev = pkg.lib().dg_elem_variant()
@@ -253,8 +253,8 @@ def test_even_odd_form_equals_dense_form(pkg, orc, omesh, N):
     for k in (1, 2):
         assert orc.rel_l2(out[k][0], out[0][0]) < 1e-13
         assert orc.rel_l2(out[k][1], out[0][1]) < 1e-13
-    if N != 3:
-        assert np.array_equal(out[2][0], out[1][0])  # form 2 is form 1 away from N = 3
+    if N not in (3, 4, 5):
+        assert np.array_equal(out[2][0], out[1][0])  # form 2 is form 1 at the other orders
 
 
 def _rhs_forms(pkg, m, W, N=3):
@@ -270,16 +270,17 @@ def _rhs_forms(pkg, m, W, N=3):
     return out
 
 
-def test_tensor_core_contraction_wide_range(pkg, omesh):
+@pytest.mark.parametrize("N", [3, 4, 5])
+def test_tensor_core_contraction_wide_range(pkg, omesh, N):
     """Cells whose states differ by up to 1e6 in scale (each cell's state scaled as a whole, so
     it stays physical): the tensor-core contraction scales every column by its own largest
     exponent, and agrees with the FP64 contraction to rounding."""
     m = omesh.naca_ogrid(32, 8, farfield="characteristic")
-    s = pkg.Solver(pkg.Mesh.from_tables(m), pkg.config(N=3, cfl=0.5)).init()
-    q = s.get("q").reshape(-1, 40)
+    s = pkg.Solver(pkg.Mesh.from_tables(m), pkg.config(N=N, cfl=0.5)).init()
+    q = s.get("q").reshape(m["cell2nodes"].shape[0], -1)
     lam = 10.0 ** np.random.default_rng(7).uniform(-3, 3, q.shape[0])
     W = (q * lam[:, None]).ravel()
-    r1, r2 = _rhs_forms(pkg, m, W)
+    r1, r2 = _rhs_forms(pkg, m, W, N)
     assert np.all(np.isfinite(r2))
     assert np.linalg.norm(r2 - r1) <= 1e-13 * np.linalg.norm(r1)
     # entrywise: near the wall the staged fluxes are ~1e3-1e4 and cancel to an O(1) RHS, so
