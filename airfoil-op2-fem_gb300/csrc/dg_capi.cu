@@ -626,6 +626,20 @@ double dg_fp64_mma_peak_gflops(void) {
 int dg_kernels_per_step(void) { return 7; }
 void dg_set_elem_variant(int variant) { dg::set_elem_variant(variant); }
 int dg_elem_variant(void) { return dg::elem_variant(); }
+
+int dg_tc_operator_digits(int N, int *dims, double *S, int *fexp, int *digits) {
+  if (!dims) return fail(DG_ERR_ARG, "bad arguments");
+  int d4[4], fe[2][16];
+  std::vector<double> Sv;
+  std::vector<int> dig;
+  std::string err;
+  if (dg::tc_operator_tables(N, d4, Sv, fe, dig, err)) return fail(DG_ERR_ARG, err);
+  for (int k = 0; k < 4; k++) dims[k] = d4[k];
+  if (S) std::copy(Sv.begin(), Sv.end(), S);
+  if (fexp) std::copy(&fe[0][0], &fe[0][0] + 32, fexp);
+  if (digits) std::copy(dig.begin(), dig.end(), digits);
+  return 0;
+}
 void dg_set_face_block(int threads) { dg::set_face_block(threads); }
 void dg_set_pdl(int on) { dg::set_pdl(on); }
 

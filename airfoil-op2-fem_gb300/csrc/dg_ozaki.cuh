@@ -218,16 +218,17 @@ static uint32_t oz_bf16_bits(int d) {
   return u >> 16;
 }
 
-static int oz_upload(int N, const std::vector<double> &S, int NUe, int NUo, int NRe, int NRo, std::string &err) {
-  if (!oz_used(N, true)) return 0;
-  int fexp[2][16] = {};
-  static uint2 frag[2][2][7][2][32];
-  std::memset(frag, 0, sizeof(frag));
+// Column exponents F (biased, per parity and operator row) and signed base-256 digits
+// dig[p][s][k][n] (|d| <= 255) of the two parity blocks: S[n][k] = sum_s dig 256^(6-s) 2^(F-1023-55)
+// up to the bits below 2^(F-1023-55) (cut).
+static int oz_digits(const std::vector<double> &S, int NUe, int NUo, int NRe, int NRo, int fexp[2][16],
+                     std::vector<int> &dig, std::string &err) {
+  dig.assign((size_t)2 * 7 * 32 * 16, 0);
   for (int p = 0; p < 2; p++) {
     const int K = p ? NUo : NUe, R = p ? NRo : NRe;
     const size_t base = p ? (size_t)NRe * NUe : 0;
     if (R > 16 || K > 32) { err = "tensor-core contraction: operator too large"; return -4; }
-    std::vector<int> dig((size_t)7 * 32 * 16, 0);  // [s][k][n]
+    for (int n = 0; n < 16; n++) fexp[p][n] = 0;
     for (int n = 0; n < R; n++) {
       int F = 0;
       for (int k = 0; k < K; k++) {
@@ -245,19 +246,31 @@ static int oz_upload(int N, const std::vector<double> &S, int NUe, int NUo, int 
         const int sh = e - F + 3;
         const uint64_t m = sh >= 0 ? (M << sh) : (sh > -64 ? (M >> -sh) : 0);
         const int sg = (b >> 63) ? -1 : 1;
-        for (int s = 0; s < 7; s++) dig[((size_t)s * 32 + k) * 16 + n] = sg * (int)((m >> (8 * (6 - s))) & 255);
+        for (int s = 0; s < 7; s++)
+          dig[(((size_t)p * 7 + s) * 32 + k) * 16 + n] = sg * (int)((m >> (8 * (6 - s))) & 255);
       }
     }
+  }
+  return 0;
+}
+
+static int oz_upload(int N, const std::vector<double> &S, int NUe, int NUo, int NRe, int NRo, std::string &err) {
+  if (!oz_used(N, true)) return 0;
+  int fexp[2][16] = {};
+  std::vector<int> dig;
+  if (int rc = oz_digits(S, NUe, NUo, NRe, NRo, fexp, dig, err)) return rc;
+  static uint2 frag[2][2][7][2][32];
+  std::memset(frag, 0, sizeof(frag));
+  for (int p = 0; p < 2; p++)
     for (int nt = 0; nt < 2; nt++)
       for (int s = 0; s < 7; s++)
         for (int ks = 0; ks < 2; ks++)
           for (int lane = 0; lane < 32; lane++) {
             const int g = lane >> 2, t = lane & 3, k0 = 16 * ks + 2 * t;
-            auto D = [&](int k) { return k < 32 ? dig[((size_t)s * 32 + k) * 16 + 8 * nt + g] : 0; };
+            auto D = [&](int k) { return dig[(((size_t)p * 7 + s) * 32 + k) * 16 + 8 * nt + g]; };
             frag[p][nt][s][ks][lane].x = oz_bf16_bits(D(k0)) | (oz_bf16_bits(D(k0 + 1)) << 16);
             frag[p][nt][s][ks][lane].y = oz_bf16_bits(D(k0 + 8)) | (oz_bf16_bits(D(k0 + 9)) << 16);
           }
-  }
   cudaError_t ce = cudaMemcpyToSymbol(c_ozf, fexp, sizeof(fexp), (size_t)N * sizeof(fexp));
   if (ce == cudaSuccess) ce = cudaMemcpyToSymbol(g_ozb, frag, sizeof(frag), (size_t)N * sizeof(frag));
   if (ce != cudaSuccess) { err = std::string("constant upload: ") + cudaGetErrorString(ce); return -3; }

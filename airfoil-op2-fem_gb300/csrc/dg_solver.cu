@@ -848,7 +848,13 @@ static void sym_dims(int &NUe, int &NUo, int &NRe, int &NRo) {
 }
 
 // Tables of the even/odd form (see elem_kernel_sym) from the dense rows A = [Drw | Dsw | -LIFT].
-static int sym_tables(const Operators &o, const std::vector<double> &A, std::string &err) {
+struct SymHost {
+  int NUe = 0, NUo = 0, NRe = 0, NRo = 0;
+  std::vector<double> S;  // even rows NRe x NUe, then odd rows NRo x NUo
+  int pos[77], out[28 * 3], rin[28 * 2];
+};
+
+static int sym_build(const Operators &o, const std::vector<double> &A, SymHost &t, std::string &err) {
   const int N = o.N, Np = o.Np, Nfp = o.Nfp, NK = 2 * Np + 3 * Nfp;
   std::vector<int> Pn(Np, -1), Pi(NK);
   for (int i = 0; i < Np; i++)
@@ -880,7 +886,7 @@ static int sym_tables(const Operators &o, const std::vector<double> &A, std::str
   int cNUe, cNUo, cNRe, cNRo;
   DG_DISPATCH(N, sym_dims<NN>(cNUe, cNUo, cNRe, cNRo));
   if (NUe != cNUe || NUo != cNUo || NRe != cNRe || NRo != cNRo) { err = "unexpected symmetry dimensions"; return -4; }
-  int pos[77], out[28 * 3];
+  int *pos = t.pos, *out = t.out, *rin = t.rin;
   for (int k = 0; k < 77; k++) pos[k] = 0;
   for (int k = 0; k < 28 * 3; k++) out[k] = 0;
   for (int p = 0; p < NPin; p++) {
@@ -888,7 +894,8 @@ static int sym_tables(const Operators &o, const std::vector<double> &A, std::str
     pos[inp[p].second] = NUe + p;
   }
   for (size_t j = 0; j < infix.size(); j++) pos[infix[j]] = NPin + (int)j;
-  std::vector<double> S((size_t)NRe * NUe + (size_t)NRo * NUo);
+  std::vector<double> &S = t.S;
+  S.assign((size_t)NRe * NUe + (size_t)NRo * NUo, 0.0);
   for (int r = 0; r < NRe; r++) {
     const int i = r < NPo ? outp[r].first : outfix[r - NPo];
     for (int k = 0; k < NUe; k++)
@@ -912,7 +919,6 @@ static int sym_tables(const Operators &o, const std::vector<double> &A, std::str
   }
   // rows -> nodes, for transposed products: even row r is the pair outp[r] (or a fixed node),
   // odd row NRe + q the pair outp[q]
-  int rin[28 * 2];
   for (int k = 0; k < 56; k++) rin[k] = -1;
   for (int r = 0; r < NRe; r++) {
     rin[2 * r] = r < NPo ? outp[r].first : outfix[r - NPo];
@@ -922,13 +928,50 @@ static int sym_tables(const Operators &o, const std::vector<double> &A, std::str
     rin[2 * (NRe + q)] = outp[q].first;
     rin[2 * (NRe + q) + 1] = outp[q].second;
   }
+  t.NUe = NUe; t.NUo = NUo; t.NRe = NRe; t.NRo = NRo;
+  return 0;
+}
+
+static int sym_tables(const Operators &o, const std::vector<double> &A, std::string &err) {
+  const int N = o.N;
+  SymHost t;
+  if (int rc = sym_build(o, A, t, err)) return rc;
   const void *syms[7] = {nullptr, c_S1, c_S2, c_S3, c_S4, c_S5, c_S6};
-  cudaError_t ce = cudaMemcpyToSymbol(syms[N], S.data(), S.size() * sizeof(double));
-  if (ce == cudaSuccess) ce = cudaMemcpyToSymbol(c_rin, rin, sizeof(rin), (size_t)N * sizeof(rin));
-  if (ce == cudaSuccess) ce = cudaMemcpyToSymbol(c_pos, pos, sizeof(pos), (size_t)N * sizeof(pos));
-  if (ce == cudaSuccess) ce = cudaMemcpyToSymbol(c_out, out, sizeof(out), (size_t)N * sizeof(out));
+  cudaError_t ce = cudaMemcpyToSymbol(syms[N], t.S.data(), t.S.size() * sizeof(double));
+  if (ce == cudaSuccess) ce = cudaMemcpyToSymbol(c_rin, t.rin, sizeof(t.rin), (size_t)N * sizeof(t.rin));
+  if (ce == cudaSuccess) ce = cudaMemcpyToSymbol(c_pos, t.pos, sizeof(t.pos), (size_t)N * sizeof(t.pos));
+  if (ce == cudaSuccess) ce = cudaMemcpyToSymbol(c_out, t.out, sizeof(t.out), (size_t)N * sizeof(t.out));
   if (ce != cudaSuccess) { err = std::string("constant upload: ") + cudaGetErrorString(ce); return -3; }
-  return oz_upload(N, S, NUe, NUo, NRe, NRo, err);
+  return oz_upload(N, t.S, t.NUe, t.NUo, t.NRe, t.NRo, err);
+}
+
+// Dense rows [Drw | Dsw | -LIFT] of order N.
+static void dense_rows(const Operators &o, std::vector<double> &A) {
+  const int Np = o.Np, Nfp = o.Nfp, NK = 2 * Np + 3 * Nfp;
+  A.assign((size_t)Np * NK, 0.0);
+  for (int i = 0; i < Np; i++) {
+    for (int k = 0; k < Np; k++) {
+      A[(size_t)i * NK + k] = o.Drw[(size_t)i * Np + k];
+      A[(size_t)i * NK + Np + k] = o.Dsw[(size_t)i * Np + k];
+    }
+    for (int k = 0; k < 3 * Nfp; k++) A[(size_t)i * NK + 2 * Np + k] = -o.LIFT[(size_t)i * 3 * Nfp + k];
+  }
+}
+
+// Host-only view of the tensor-core operator tables of order N (for tests): the parity
+// dimensions, the even/odd operator blocks S, the row exponents and the digits.
+int tc_operator_tables(int N, int dims[4], std::vector<double> &S, int fexp[2][16], std::vector<int> &dig,
+                       std::string &err) {
+  if (!oz_used(N, true)) { err = "no tensor-core contraction at this order"; return -1; }
+  Operators o;
+  if (build_operators(N, o)) { err = "operator construction failed"; return -2; }
+  std::vector<double> A;
+  dense_rows(o, A);
+  SymHost t;
+  if (int rc = sym_build(o, A, t, err)) return rc;
+  dims[0] = t.NUe; dims[1] = t.NUo; dims[2] = t.NRe; dims[3] = t.NRo;
+  S = t.S;
+  return oz_digits(t.S, t.NUe, t.NUo, t.NRe, t.NRo, fexp, dig, err);
 }
 
 // ---------------------------------------------------------------- operator upload
@@ -940,15 +983,9 @@ int load_order_constants(int N, std::string &err) {
   if (g_ops_loaded[N]) return 0;
   Operators o;
   if (build_operators(N, o)) { err = "operator construction failed"; return -2; }
-  const int Np = o.Np, Nfp = o.Nfp, NK = 2 * Np + 3 * Nfp;
-  std::vector<double> A((size_t)Np * NK);
-  for (int i = 0; i < Np; i++) {
-    for (int k = 0; k < Np; k++) {
-      A[(size_t)i * NK + k] = o.Drw[(size_t)i * Np + k];
-      A[(size_t)i * NK + Np + k] = o.Dsw[(size_t)i * Np + k];
-    }
-    for (int k = 0; k < 3 * Nfp; k++) A[(size_t)i * NK + 2 * Np + k] = -o.LIFT[(size_t)i * 3 * Nfp + k];
-  }
+  const int Np = o.Np, Nfp = o.Nfp;
+  std::vector<double> A;
+  dense_rows(o, A);
   const void *syms[7] = {nullptr, c_A1, c_A2, c_A3, c_A4, c_A5, c_A6};
   cudaError_t ce = cudaMemcpyToSymbol(syms[N], A.data(), A.size() * sizeof(double));
   if (ce == cudaSuccess) {
