@@ -311,10 +311,11 @@ __global__ void __launch_bounds__(32 * np_of(N)) adj_elem_kernel(const Inst d, c
 // butterfly, S: the even and odd blocks, R: output recombination), so A^T = B^T S^T R^T: the
 // node adjoints are combined pairwise into even and odd rows (R^T), the blocks are applied
 // transposed (about half the multiply-adds of the dense columns) and each original column is
-// read back as a sum or difference of an even and an odd column (B^T).
-template <int N>
-__global__ void __launch_bounds__(32 * np_of(N)) adj_elem_kernel_sym(const Inst d, const double *mu, double *wbar,
-                                                                      double *fluxbar) {
+// read back as a sum or difference of an even and an odd column (B^T).  TC: S^T on the tensor
+// cores as the exact integer product of dg_ozaki.cuh (element-kernel form 2, at N = 3).
+template <int N, bool TC>
+__global__ void __launch_bounds__(32 * np_of(N), oz_used_t(N, TC) ? 3 : 1)
+    adj_elem_kernel_sym(const Inst d, const double *mu, double *wbar, double *fluxbar) {
   constexpr int Np = np_of(N), Nfp = N + 1, NK = nk_of(N);
   constexpr int NUe = Sym<N>::NUe, NUo = Sym<N>::NUo, NRe = Sym<N>::NRe;
   extern __shared__ double2 sm[];
@@ -350,6 +351,10 @@ __global__ void __launch_bounds__(32 * np_of(N)) adj_elem_kernel_sym(const Inst 
   }
   __syncthreads();
   // S^T: column k of the even block (k < NUe) or of the odd block
+  if constexpr (oz_used_t(N, TC)) {
+    oz_contract_t<N, NUe, NUo, NRe, Sym<N>::NRo>(reinterpret_cast<const double *>(MS), reinterpret_cast<double *>(XS),
+                                                 i, Np, lane);
+  } else
   for (int k = i; k < NK; k += Np) {
     double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
     if (k < NUe) {
@@ -795,9 +800,10 @@ struct Adjoint {
       DG_DISPATCH(cfg.N, {
         const size_t sm = (size_t)(np_of(NN) + nk_of(NN)) * 32 * 4 * sizeof(double);
         ce = cudaFuncSetAttribute(adj_elem_kernel<NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        if (ce == cudaSuccess)
-          ce = cudaFuncSetAttribute(adj_elem_kernel_sym<NN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)((size_t)(2 * np_of(NN) + nk_of(NN)) * 32 * 4 * sizeof(double)));
+        for (auto k : {adj_elem_kernel_sym<NN, false>, adj_elem_kernel_sym<NN, true>})
+          if (ce == cudaSuccess)
+            ce = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)((size_t)(2 * np_of(NN) + nk_of(NN)) * 32 * 4 * sizeof(double)));
       });
     }
     if (ce != cudaSuccess) { err = cudaGetErrorString(ce); return -100; }
@@ -916,7 +922,10 @@ struct Adjoint {
     DG_DISPATCH(cfg.N, {
       if (g_elem_variant) {
         const size_t sm = (size_t)(2 * np_of(NN) + nk_of(NN)) * 32 * 4 * sizeof(double);
-        adj_elem_kernel_sym<NN><<<(d.K + 31) / 32, dim3(32, np_of(NN)), sm, st>>>(d, v, wbar, fluxbar);
+        if (g_elem_variant == 2 && oz_used_t(NN, true))
+          adj_elem_kernel_sym<NN, true><<<(d.K + 31) / 32, dim3(32, np_of(NN)), sm, st>>>(d, v, wbar, fluxbar);
+        else
+          adj_elem_kernel_sym<NN, false><<<(d.K + 31) / 32, dim3(32, np_of(NN)), sm, st>>>(d, v, wbar, fluxbar);
       } else {
         const size_t sm = (size_t)(np_of(NN) + nk_of(NN)) * 32 * 4 * sizeof(double);
         adj_elem_kernel<NN><<<(d.K + 31) / 32, dim3(32, np_of(NN)), sm, st>>>(d, v, wbar, fluxbar);

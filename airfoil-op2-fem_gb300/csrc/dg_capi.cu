@@ -629,14 +629,14 @@ int dg_elem_variant(void) { return dg::elem_variant(); }
 
 int dg_tc_operator_digits(int N, int *dims, double *S, int *fexp, int *digits) {
   if (!dims) return fail(DG_ERR_ARG, "bad arguments");
-  int d4[4], fe[2][16];
+  int d4[4], fe[2][32];
   std::vector<double> Sv;
   std::vector<int> dig;
   std::string err;
   if (dg::tc_operator_tables(N, d4, Sv, fe, dig, err)) return fail(DG_ERR_ARG, err);
   for (int k = 0; k < 4; k++) dims[k] = d4[k];
   if (S) std::copy(Sv.begin(), Sv.end(), S);
-  if (fexp) std::copy(&fe[0][0], &fe[0][0] + 32, fexp);
+  if (fexp) std::copy(&fe[0][0], &fe[0][0] + 64, fexp);
   if (digits) std::copy(dig.begin(), dig.end(), digits);
   return 0;
 }

@@ -28,8 +28,11 @@
 // 32-cell tile; each needs 28 mma per k-step of 16 slots.  Non-finite inputs in a column give NaN.
 // Each row tile takes the operator rows 8 at a time (one n-tile of mma).
 
-__constant__ int c_ozf[7][2][16];  // biased binary exponent F of every operator row (order, parity, row)
-__device__ uint2 g_ozb[7][2][2][7][2][32];  // B fragments: order, parity, n-tile, digit s, k-step, lane
+// Tables of the operator blocks S_p (T = 0: rows of S_p are the outputs, the element kernel)
+// and of their transposes (T = 1: columns of S_p are the outputs, the adjoint element kernel).
+constexpr int kOzRows = 32;  // outputs per parity: up to 4 n-tiles of 8
+__constant__ int c_ozf[2][7][2][kOzRows];  // biased binary exponent F of every output row: T, order, parity, row
+__device__ uint2 g_ozb[2][7][2][4][7][2][32];  // B fragments: T, order, parity, n-tile, digit s, k-step, lane
 
 // Orders that use it: N = 3, 4, 5 (steps on the K=32768 O-grid: 365 -> 328, 564 -> 477,
 // 909 -> 720 us).  At N = 1 and 2 the contraction is too small a share of the element kernel and
@@ -37,6 +40,9 @@ __device__ uint2 g_ozb[7][2][2][7][2][32];  // B fragments: order, parity, n-til
 // 5 fit the exactness bound (at most two k-steps of 16 slots); N = 6 needs three.
 constexpr int kOzMaxN = 5;
 constexpr bool oz_used(int N, bool tc) { return tc && (N == 3 || N == 4 || N == 5); }
+// The adjoint element kernel's transposed contraction: N = 3 (the transposed blocks of N = 4
+// need six n-tiles of outputs).
+constexpr bool oz_used_t(int N, bool tc) { return tc && N == 3; }
 // Minimum resident blocks per SM for the element kernel's register allocation in this form.
 constexpr int oz_min_blocks(int N) { return N <= 3 ? 3 : (N == 4 ? 2 : 1); }
 
@@ -67,10 +73,10 @@ __device__ __forceinline__ uint32_t oz_pack(const float f_lo, const float f_hi, 
 // (K <= 16 KST), times operator rows 8 NT .. 8 NT + 7 (of R) of parity P, written to Y rows
 // YROW0 + row.  The k-steps are taken one after the other (their values re-read from shared
 // memory) so that only one k-step's magnitudes are live next to the seven accumulators.
-template <int NORD, int K, int R, int SLOT0, int YROW0, int KST, int P, int NT>
+template <int T, int NORD, int K, int R, int SLOT0, int YROW0, int KST, int P, int NT>
 __device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *__restrict__ Yd, const int c0,
                                         const int lane) {
-  static_assert(KST <= 2 && K <= 16 * KST && R > 8 * NT && NT < 2, "two n-tiles, two k-steps at most");
+  static_assert(KST <= 2 && K <= 16 * KST && R > 8 * NT && NT < 4, "four n-tiles, two k-steps at most");
   const int g = lane >> 2, t = lane & 3;
   const int col = c0 * 4 + g;  // (cell, variable) of row g; row g + 8 is col + 8
   const uint32_t *Xw = reinterpret_cast<const uint32_t *>(Xd);
@@ -90,7 +96,7 @@ __device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *_
     em[r] = max(em[r], __shfl_xor_sync(0xffffffffu, em[r], 1));
     em[r] = max(em[r], __shfl_xor_sync(0xffffffffu, em[r], 2));
   }
-  const uint2 *bfr = &g_ozb[NORD][P][NT][0][0][lane];
+  const uint2 *bfr = &g_ozb[T][NORD][P][NT][0][0][lane];
   float acc[7][4];
 #pragma unroll
   for (int l = 0; l < 7; l++) acc[l][0] = acc[l][1] = acc[l][2] = acc[l][3] = 0.0f;
@@ -156,7 +162,7 @@ __device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *_
         for (int L = 0; L < 7; L++) l[L] = (long long)__float2int_rz(acc[L][o]);
         const long long th = l[0] * 65536LL + l[1] * 256LL + l[2];
         const long long tl = l[3] * 16777216LL + l[4] * 65536LL + l[5] * 256LL + l[6];
-        const int fe = c_ozf[NORD][P][n];
+        const int fe = c_ozf[T][NORD][P][n];
         const int sc = em[r] + fe - 2046 - 62;
         double out;
         if (em[r] == 0x7FF) {
@@ -183,29 +189,45 @@ __device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *_
     }
 }
 
-// Both parities of one 32-cell tile: Y rows 0..NRe-1 from the even slots, NRe.. from the odd
-// slots.  Work units: (parity, n-tile of 8 operator rows, group of 4 cells); warp w of nw takes
-// units w, w + nw, ...
+// Parity 0: K0 staged slots from slot 0 to R0 outputs from row 0; parity 1: K1 slots from SLOT1
+// to R1 outputs from YROW1.  Work units: (parity, n-tile of 8 outputs, group of 4 cells); warp w
+// of nw takes units w, w + nw, ...
+template <int N, int T, int K0, int R0, int K1, int R1, int SLOT1, int YROW1, int NT>
+__device__ __forceinline__ void oz_unit(const double *Xd, double *Yd, const int w, const int c0, const int lane) {
+  constexpr int NT0 = (R0 + 7) / 8;
+  if constexpr (NT < 4) {
+    if (w == NT) {
+      if constexpr (NT < NT0) oz_tile<T, N, K0, R0, 0, 0, (K0 + 15) / 16, 0, NT>(Xd, Yd, c0, lane);
+      else if constexpr (NT - NT0 < (R1 + 7) / 8)
+        oz_tile<T, N, K1, R1, SLOT1, YROW1, (K1 + 15) / 16, 1, NT - NT0>(Xd, Yd, c0, lane);
+      return;
+    }
+    oz_unit<N, T, K0, R0, K1, R1, SLOT1, YROW1, NT + 1>(Xd, Yd, w, c0, lane);
+  }
+}
+
+template <int N, int T, int K0, int R0, int K1, int R1, int SLOT1, int YROW1>
+__device__ __forceinline__ void oz_product(const double *Xd, double *Yd, const int warp, const int nw,
+                                           const int lane) {
+  constexpr int NTT = (R0 + 7) / 8 + (R1 + 7) / 8;
+  static_assert(NTT <= 4, "at most 4 n-tiles");
+  for (int u = warp; u < 8 * NTT; u += nw) oz_unit<N, T, K0, R0, K1, R1, SLOT1, YROW1, 0>(Xd, Yd, u >> 3, (u & 7) * 4, lane);
+}
+
+// The element kernel's contraction: Y rows 0..NRe-1 = S_e (even slots), Y rows NRe.. = S_o (odd
+// slots).
 template <int N, int NUe, int NUo, int NRe, int NRo>
 __device__ __forceinline__ void oz_contract(const double *Xd, double *Yd, const int warp, const int nw,
                                             const int lane) {
-  constexpr int KE = (NUe + 15) / 16, KO = (NUo + 15) / 16, NTE = (NRe + 7) / 8, NTO = (NRo + 7) / 8;
-  for (int u = warp; u < 8 * (NTE + NTO); u += nw) {
-    const int c0 = (u & 7) * 4, w = u >> 3;
-    if (w < NTE) {
-      if (w == 0) {
-        oz_tile<N, NUe, NRe, 0, 0, KE, 0, 0>(Xd, Yd, c0, lane);
-      } else {
-        if constexpr (NTE > 1) oz_tile<N, NUe, NRe, 0, 0, KE, 0, 1>(Xd, Yd, c0, lane);
-      }
-    } else {
-      if (w == NTE) {
-        oz_tile<N, NUo, NRo, NUe, NRe, KO, 1, 0>(Xd, Yd, c0, lane);
-      } else {
-        if constexpr (NTO > 1) oz_tile<N, NUo, NRo, NUe, NRe, KO, 1, 1>(Xd, Yd, c0, lane);
-      }
-    }
-  }
+  oz_product<N, 0, NUe, NRe, NUo, NRo, NUe, NRe>(Xd, Yd, warp, nw, lane);
+}
+
+// The adjoint element kernel's transposed contraction: columns 0..NUe-1 = S_e^T (even rows of the
+// staged node adjoints), columns NUe.. = S_o^T (odd rows).
+template <int N, int NUe, int NUo, int NRe, int NRo>
+__device__ __forceinline__ void oz_contract_t(const double *Xd, double *Yd, const int warp, const int nw,
+                                              const int lane) {
+  oz_product<N, 1, NRe, NUe, NRo, NUo, NRe, NUe>(Xd, Yd, warp, nw, lane);
 }
 
 // ---------------------------------------------------------------- host: operator digits
@@ -221,14 +243,14 @@ static uint32_t oz_bf16_bits(int d) {
 // Column exponents F (biased, per parity and operator row) and signed base-256 digits
 // dig[p][s][k][n] (|d| <= 255) of the two parity blocks: S[n][k] = sum_s dig 256^(6-s) 2^(F-1023-55)
 // up to the bits below 2^(F-1023-55) (cut).
-static int oz_digits(const std::vector<double> &S, int NUe, int NUo, int NRe, int NRo, int fexp[2][16],
+static int oz_digits(const std::vector<double> &S, int NUe, int NUo, int NRe, int NRo, int fexp[2][kOzRows],
                      std::vector<int> &dig, std::string &err) {
-  dig.assign((size_t)2 * 7 * 32 * 16, 0);
+  dig.assign((size_t)2 * 7 * 32 * kOzRows, 0);
   for (int p = 0; p < 2; p++) {
     const int K = p ? NUo : NUe, R = p ? NRo : NRe;
     const size_t base = p ? (size_t)NRe * NUe : 0;
-    if (R > 16 || K > 32) { err = "tensor-core contraction: operator too large"; return -4; }
-    for (int n = 0; n < 16; n++) fexp[p][n] = 0;
+    if (R > kOzRows || K > 32) { err = "tensor-core contraction: operator too large"; return -4; }
+    for (int n = 0; n < kOzRows; n++) fexp[p][n] = 0;
     for (int n = 0; n < R; n++) {
       int F = 0;
       for (int k = 0; k < K; k++) {
@@ -247,7 +269,7 @@ static int oz_digits(const std::vector<double> &S, int NUe, int NUo, int NRe, in
         const uint64_t m = sh >= 0 ? (M << sh) : (sh > -64 ? (M >> -sh) : 0);
         const int sg = (b >> 63) ? -1 : 1;
         for (int s = 0; s < 7; s++)
-          dig[(((size_t)p * 7 + s) * 32 + k) * 16 + n] = sg * (int)((m >> (8 * (6 - s))) & 255);
+          dig[(((size_t)p * 7 + s) * 32 + k) * kOzRows + n] = sg * (int)((m >> (8 * (6 - s))) & 255);
       }
     }
   }
@@ -256,23 +278,43 @@ static int oz_digits(const std::vector<double> &S, int NUe, int NUo, int NRe, in
 
 static int oz_upload(int N, const std::vector<double> &S, int NUe, int NUo, int NRe, int NRo, std::string &err) {
   if (!oz_used(N, true)) return 0;
-  int fexp[2][16] = {};
-  std::vector<int> dig;
-  if (int rc = oz_digits(S, NUe, NUo, NRe, NRo, fexp, dig, err)) return rc;
-  static uint2 frag[2][2][7][2][32];
+  static int fexp[2][2][kOzRows];
+  static uint2 frag[2][2][4][7][2][32];
+  std::memset(fexp, 0, sizeof(fexp));
   std::memset(frag, 0, sizeof(frag));
-  for (int p = 0; p < 2; p++)
-    for (int nt = 0; nt < 2; nt++)
-      for (int s = 0; s < 7; s++)
-        for (int ks = 0; ks < 2; ks++)
-          for (int lane = 0; lane < 32; lane++) {
-            const int g = lane >> 2, t = lane & 3, k0 = 16 * ks + 2 * t;
-            auto D = [&](int k) { return dig[(((size_t)p * 7 + s) * 32 + k) * 16 + 8 * nt + g]; };
-            frag[p][nt][s][ks][lane].x = oz_bf16_bits(D(k0)) | (oz_bf16_bits(D(k0 + 1)) << 16);
-            frag[p][nt][s][ks][lane].y = oz_bf16_bits(D(k0 + 8)) | (oz_bf16_bits(D(k0 + 9)) << 16);
-          }
-  cudaError_t ce = cudaMemcpyToSymbol(c_ozf, fexp, sizeof(fexp), (size_t)N * sizeof(fexp));
-  if (ce == cudaSuccess) ce = cudaMemcpyToSymbol(g_ozb, frag, sizeof(frag), (size_t)N * sizeof(frag));
+  for (int T = 0; T < 2; T++) {
+    if (T == 1 && !oz_used_t(N, true)) break;
+    // T = 1: the transposed blocks, S_e^T (NUe x NRe) then S_o^T (NUo x NRo)
+    std::vector<double> ST;
+    if (T == 1) {
+      ST.resize(S.size());
+      for (int r = 0; r < NRe; r++)
+        for (int k = 0; k < NUe; k++) ST[(size_t)k * NRe + r] = S[(size_t)r * NUe + k];
+      const size_t so = (size_t)NRe * NUe;
+      for (int r = 0; r < NRo; r++)
+        for (int k = 0; k < NUo; k++) ST[so + (size_t)k * NRo + r] = S[so + (size_t)r * NUo + k];
+    }
+    std::vector<int> dig;
+    const int rc = T == 0 ? oz_digits(S, NUe, NUo, NRe, NRo, fexp[0], dig, err)
+                          : oz_digits(ST, NRe, NRo, NUe, NUo, fexp[1], dig, err);
+    if (rc) return rc;
+    for (int p = 0; p < 2; p++)
+      for (int nt = 0; nt < 4; nt++)
+        for (int s = 0; s < 7; s++)
+          for (int ks = 0; ks < 2; ks++)
+            for (int lane = 0; lane < 32; lane++) {
+              const int g = lane >> 2, t = lane & 3, k0 = 16 * ks + 2 * t;
+              auto D = [&](int k) { return dig[(((size_t)p * 7 + s) * 32 + k) * kOzRows + 8 * nt + g]; };
+              frag[T][p][nt][s][ks][lane].x = oz_bf16_bits(D(k0)) | (oz_bf16_bits(D(k0 + 1)) << 16);
+              frag[T][p][nt][s][ks][lane].y = oz_bf16_bits(D(k0 + 8)) | (oz_bf16_bits(D(k0 + 9)) << 16);
+            }
+  }
+  cudaError_t ce = cudaSuccess;
+  for (int T = 0; T < 2 && ce == cudaSuccess; T++) {
+    ce = cudaMemcpyToSymbol(c_ozf, fexp[T], sizeof(fexp[T]), ((size_t)T * 7 + N) * sizeof(fexp[T]));
+    if (ce == cudaSuccess)
+      ce = cudaMemcpyToSymbol(g_ozb, frag[T], sizeof(frag[T]), ((size_t)T * 7 + N) * sizeof(frag[T]));
+  }
   if (ce != cudaSuccess) { err = std::string("constant upload: ") + cudaGetErrorString(ce); return -3; }
   return 0;
 }

@@ -960,7 +960,7 @@ static void dense_rows(const Operators &o, std::vector<double> &A) {
 
 // Host-only view of the tensor-core operator tables of order N (for tests): the parity
 // dimensions, the even/odd operator blocks S, the row exponents and the digits.
-int tc_operator_tables(int N, int dims[4], std::vector<double> &S, int fexp[2][16], std::vector<int> &dig,
+int tc_operator_tables(int N, int dims[4], std::vector<double> &S, int fexp[2][kOzRows], std::vector<int> &dig,
                        std::string &err) {
   if (!oz_used(N, true)) { err = "no tensor-core contraction at this order"; return -1; }
   Operators o;

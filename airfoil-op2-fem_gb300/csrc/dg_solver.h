@@ -51,9 +51,10 @@ int load_order_constants(int N, std::string &err);
 // Element kernel form for launches enqueued from now on: 1 even/odd (default), 0 dense.
 void set_elem_variant(int v);
 int elem_variant();
-// Host-only: parity dimensions {NUe, NUo, NRe, NRo}, even/odd operator blocks, row exponents and
-// signed base-256 digits [parity][digit][slot][row] of the tensor-core contraction of order N.
-int tc_operator_tables(int N, int dims[4], std::vector<double> &S, int fexp[2][16], std::vector<int> &dig,
+// Host-only: parity dimensions {NUe, NUo, NRe, NRo}, even/odd operator blocks, row exponents
+// [parity][32] and signed base-256 digits [parity][digit][slot 32][row 32] of the tensor-core
+// contraction of order N.
+int tc_operator_tables(int N, int dims[4], std::vector<double> &S, int fexp[2][32], std::vector<int> &dig,
                        std::string &err);
 // Threads per face-kernel block for launches enqueued from now on (32..256, multiple of 32).
 void set_face_block(int b);

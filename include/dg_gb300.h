@@ -266,8 +266,8 @@ void dg_set_elem_variant(int variant);
 int dg_elem_variant(void);
 /* Host-only (no GPU needed): the tables of the tensor-core contraction of order N (3..5).
  * dims[4] receives NUe, NUo, NRe, NRo; S (NRe*NUe + NRo*NUo doubles, may be NULL) the even then
- * odd operator blocks row-major; fexp (2 x 16 ints, may be NULL) each row's biased binary
- * exponent F; digits (2 x 7 x 32 x 16 ints, may be NULL) [parity][digit s][slot k][row n], with
+ * odd operator blocks row-major; fexp (2 x 32 ints, may be NULL) each row's biased binary
+ * exponent F; digits (2 x 7 x 32 x 32 ints, may be NULL) [parity][digit s][slot k][row n], with
  * S[n][k] = sum_s digit * 256^(6-s) * 2^(F-1023-55) up to the cut bits below 2^(F-1023-55). */
 int dg_tc_operator_digits(int N, int *dims, double *S, int *fexp, int *digits);
 /* Threads per face-kernel block of the plain path (32..256, multiple of 32; default 64). */

@@ -16,10 +16,10 @@ def tables(pkg, N):
     assert lib.dg_tc_operator_digits(N, dims.ctypes.data, None, None, None) == 0
     NUe, NUo, NRe, NRo = (int(x) for x in dims)
     S = np.zeros(NRe * NUe + NRo * NUo)
-    fexp = np.zeros(32, np.int32)
-    dig = np.zeros(2 * 7 * 32 * 16, np.int32)
+    fexp = np.zeros(64, np.int32)
+    dig = np.zeros(2 * 7 * 32 * 32, np.int32)
     assert lib.dg_tc_operator_digits(N, dims.ctypes.data, S.ctypes.data, fexp.ctypes.data, dig.ctypes.data) == 0
-    return (NUe, NUo, NRe, NRo), S, fexp.reshape(2, 16), dig.reshape(2, 7, 32, 16)
+    return (NUe, NUo, NRe, NRo), S, fexp.reshape(2, 32), dig.reshape(2, 7, 32, 32)
 
 
 @pytest.mark.parametrize("N", [3, 4, 5])
