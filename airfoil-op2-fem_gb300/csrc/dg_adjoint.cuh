@@ -922,7 +922,7 @@ struct Adjoint {
     DG_DISPATCH(cfg.N, {
       if (g_elem_variant) {
         const size_t sm = (size_t)(2 * np_of(NN) + nk_of(NN)) * 32 * 4 * sizeof(double);
-        if (g_elem_variant == 2 && oz_used_t(NN, true))
+        if (g_elem_variant >= 2 && oz_used_t(NN, true))
           adj_elem_kernel_sym<NN, true><<<(d.K + 31) / 32, dim3(32, np_of(NN)), sm, st>>>(d, v, wbar, fluxbar);
         else
           adj_elem_kernel_sym<NN, false><<<(d.K + 31) / 32, dim3(32, np_of(NN)), sm, st>>>(d, v, wbar, fluxbar);

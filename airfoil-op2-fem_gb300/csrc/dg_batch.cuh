@@ -66,8 +66,9 @@ __device__ __forceinline__ bool grid_barrier(GridBarrier *b, const unsigned nblo
   }
 
 // ftiles: {instance, first face node, count, order}; etiles: {instance, first cell, 0, order}.
-// TC: the element contraction on the tensor cores (element-kernel form 2), as the plain path.
-template <int BS, int MINB, bool TC>
+// TC: the element contraction's form as in elem_tile_sym (0 FP64, 1 even/odd blocks on the tensor
+// cores, 2 dense rows on the tensor cores), the one the plain path uses.
+template <int BS, int MINB, int TC>
 __global__ void __launch_bounds__(BS, MINB) batch_stage_kernel(const Inst *insts, const int4 *ftiles, const int nft,
                                                                 const int4 *etiles, const int net, const int stage,
                                                                 GridBarrier *bar) {
@@ -94,8 +95,8 @@ __global__ void __launch_bounds__(256) batch_face_kernel(const Inst *insts, cons
   DG_DISPATCH_RT(ft.w, face_node<NN>(insts[ft.x], stage, ft.y + threadIdx.x));
 }
 
-template <int N, bool TC>
-__global__ void __launch_bounds__(32 * np_of(N), oz_used(N, TC) ? oz_min_blocks(N) : 1) batch_elem_kernel(const Inst *insts, const int4 *etiles,
+template <int N, int TC>
+__global__ void __launch_bounds__(32 * np_of(N), elem_min_blocks(N, TC)) batch_elem_kernel(const Inst *insts, const int4 *etiles,
                                                                                 const int first, const int stage) {
   extern __shared__ double2 Xg[];
   const int4 et = etiles[first + blockIdx.x];
@@ -122,7 +123,7 @@ struct BatchVariant {
   const void *fn;
 };
 
-template <int BS, int MINB, bool TC>
+template <int BS, int MINB, int TC>
 static BatchVariant batch_variant() {
   return BatchVariant{BS, MINB, (const void *)batch_stage_kernel<BS, MINB, TC>};
 }
@@ -130,9 +131,11 @@ static BatchVariant batch_variant() {
 // The persistent kernels of the current element-kernel form (the batch computes exactly what the
 // plain solvers compute).
 static std::vector<BatchVariant> batch_variants() {
+  if (g_elem_variant == 3)
+    return {batch_variant<512, 1, 2>(), batch_variant<512, 2, 2>(), batch_variant<1024, 1, 2>()};
   if (g_elem_variant == 2)
-    return {batch_variant<512, 1, true>(), batch_variant<512, 2, true>(), batch_variant<1024, 1, true>()};
-  return {batch_variant<512, 1, false>(), batch_variant<512, 2, false>(), batch_variant<1024, 1, false>()};
+    return {batch_variant<512, 1, 1>(), batch_variant<512, 2, 1>(), batch_variant<1024, 1, 1>()};
+  return {batch_variant<512, 1, 0>(), batch_variant<512, 2, 0>(), batch_variant<1024, 1, 0>()};
 }
 
 // Variant id of the grouped launches (not a persistent kernel).
@@ -247,10 +250,14 @@ struct Batch {
       for (int n = 1; n <= 6; n++) {
         const size_t sm = (size_t)(nk_of(n) + np_of(n)) * 32 * 4 * sizeof(double);
         cudaError_t ce = cudaSuccess;
-        DG_DISPATCH(n, ce = cudaFuncSetAttribute(batch_elem_kernel<NN, false>,
+        DG_DISPATCH(n, ce = cudaFuncSetAttribute(batch_elem_kernel<NN, 0>,
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         if (ce == cudaSuccess) {
-          DG_DISPATCH(n, ce = cudaFuncSetAttribute(batch_elem_kernel<NN, true>,
+          DG_DISPATCH(n, ce = cudaFuncSetAttribute(batch_elem_kernel<NN, 1>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        }
+        if (ce == cudaSuccess) {
+          DG_DISPATCH(n, ce = cudaFuncSetAttribute(batch_elem_kernel<NN, 2>,
                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         }
         if (ce != cudaSuccess) { err = cudaGetErrorString(ce); return -100; }
@@ -310,12 +317,15 @@ struct Batch {
     for (int n = 6; n >= 1; n--) {
       if (!ord_count[n]) continue;
       const size_t sm = (size_t)(nk_of(n) + np_of(n)) * 32 * 4 * sizeof(double);
-      if (g_elem_variant == 2) {
-        DG_DISPATCH(n, (batch_elem_kernel<NN, true><<<ord_count[n], 32 * np_of(NN), sm, s>>>(d_insts, d_etiles,
-                                                                                             ord_first[n], stage)));
+      if (g_elem_variant == 3) {
+        DG_DISPATCH(n, (batch_elem_kernel<NN, 2><<<ord_count[n], 32 * np_of(NN), sm, s>>>(d_insts, d_etiles,
+                                                                                          ord_first[n], stage)));
+      } else if (g_elem_variant == 2) {
+        DG_DISPATCH(n, (batch_elem_kernel<NN, 1><<<ord_count[n], 32 * np_of(NN), sm, s>>>(d_insts, d_etiles,
+                                                                                          ord_first[n], stage)));
       } else {
-        DG_DISPATCH(n, (batch_elem_kernel<NN, false><<<ord_count[n], 32 * np_of(NN), sm, s>>>(d_insts, d_etiles,
-                                                                                              ord_first[n], stage)));
+        DG_DISPATCH(n, (batch_elem_kernel<NN, 0><<<ord_count[n], 32 * np_of(NN), sm, s>>>(d_insts, d_etiles,
+                                                                                          ord_first[n], stage)));
       }
     }
     return cudaGetLastError();

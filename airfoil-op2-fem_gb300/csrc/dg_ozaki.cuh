@@ -17,10 +17,10 @@
 //    (L = 0..6; the levels L >= 7 lie below 2^-56 of the leading term and are dropped).  A level
 //    sums at most 7 pairs x 32 slots x 255^2 < 2^24, so every accumulation is an exact integer
 //    (checked on the GPU: bit-exact against 64-bit integer sums up to 1.46e7).
-//  * the seven level sums are joined as integers, T = sum_L lev_L 256^(6-L), split in two 64-bit
-//    parts of < 2^49 each, turned into doubles scaled by 2^(E+F-62) exactly (bit-pattern
-//    addition, no int-to-double conversion: those take several FP64 issue slots each on this
-//    part) and added with one rounding.  The result is the correctly rounded dot product of the
+//  * the seven level sums are joined as integers, T = sum_L lev_L 256^(6-L) (two 64-bit parts of
+//    < 2^49 each), and T 2^(E+F-62) is rounded to the nearest double with integer instructions
+//    only (oz_round; no FP64 instruction and no int-to-double conversion, which takes several
+//    FP64 issue slots on this part).  The result is the correctly rounded dot product of the
 //    56-bit truncations:
 //    its error is below 2^-55 max|x| sum|s|, under the FP64 dot product's own error bound.
 //
@@ -28,11 +28,13 @@
 // 32-cell tile; each needs 28 mma per k-step of 16 slots.  Non-finite inputs in a column give NaN.
 // Each row tile takes the operator rows 8 at a time (one n-tile of mma).
 
-// Tables of the operator blocks S_p (T = 0: rows of S_p are the outputs, the element kernel)
-// and of their transposes (T = 1: columns of S_p are the outputs, the adjoint element kernel).
+// Tables of the operator blocks S_p (T = 0: rows of S_p are the outputs, the element kernel),
+// of their transposes (T = 1: columns of S_p are the outputs, the adjoint element kernel) and of
+// the dense rows A = [Drw | Dsw | -LIFT] (T = 2, parity 0 only: the element kernel's dense form).
 constexpr int kOzRows = 32;  // outputs per parity: up to 4 n-tiles of 8
-__constant__ int c_ozf[2][7][2][kOzRows];  // biased binary exponent F of every output row: T, order, parity, row
-__device__ uint2 g_ozb[2][7][2][4][7][2][32];  // B fragments: T, order, parity, n-tile, digit s, k-step, lane
+constexpr int kOzTables = 3;
+__constant__ int c_ozf[kOzTables][7][2][kOzRows];  // biased binary exponent F of every output row: T, order, parity, row
+__device__ uint2 g_ozb[kOzTables][7][2][4][7][2][32];  // B fragments: T, order, parity, n-tile, digit s, k-step, lane
 
 // Orders that use it: N = 3, 4, 5 (steps on the K=32768 O-grid: 365 -> 328, 564 -> 477,
 // 909 -> 720 us).  At N = 1 and 2 the contraction is too small a share of the element kernel and
@@ -45,6 +47,18 @@ constexpr bool oz_used(int N, bool tc) { return tc && (N == 3 || N == 4 || N == 
 constexpr bool oz_used_t(int N, bool tc) { return tc && N == 3; }
 // Minimum resident blocks per SM for the element kernel's register allocation in this form.
 constexpr int oz_min_blocks(int N) { return N <= 3 ? 3 : (N == 4 ? 2 : 1); }
+// The dense form (element-kernel form 3 at N = 1, 2): the NK = 2 Np + 3 Nfp staged slots of every
+// column go through the dense rows A directly, without the even/odd butterfly and the
+// recombination of the outputs, at twice the mma count of the even/odd blocks.  On the K=32768
+// O-grid: steps 187 -> 175 us (N = 1) and 241 -> 222 us (N = 2).  At N = 3 (NK = 32, still within
+// two k-steps) it measured slower than the even/odd blocks on the tensor cores (341 vs 327 us:
+// each warp's share of the contraction doubles, and spills rise), so N = 3 keeps those.
+constexpr bool ozd_used(int N, int mode) { return mode == 2 && N >= 1 && N <= 2; }
+// Minimum resident blocks per SM of an element kernel of form TC (0 FP64, 1 even/odd blocks on the
+// tensor cores, 2 dense rows on the tensor cores) at order N.
+constexpr int elem_min_blocks(int N, int TC) {
+  return (ozd_used(N, TC) || oz_used(N, TC != 0)) ? oz_min_blocks(N) : 1;
+}
 
 __device__ __forceinline__ void mma_bf16_16816(float c[4], const uint32_t a[4], const uint2 b) {
   asm volatile(
@@ -66,6 +80,41 @@ __device__ __forceinline__ float oz_digit(const uint32_t hi, const uint32_t lo, 
 // pattern of the pair (bit 15: low, bit 31: high) applied.
 __device__ __forceinline__ uint32_t oz_pack(const float f_lo, const float f_hi, const uint32_t sign) {
   return __byte_perm(__float_as_uint(f_lo), __float_as_uint(f_hi), 0x7632u) ^ sign;
+}
+
+// (th 2^32 + tl) 2^sc rounded to the nearest double (ties to even), with integer instructions only:
+// on this part an FP64 add holds the FP64 pipe for 16 clocks per warp, an integer instruction
+// for 1/2.  With level sums below 2^24, |th| < 2^41 and |tl| < 2^49, so |T| < 2^74; for
+// -1022 <= sc <= 900 the result is a normal double (its biased exponent is sc + 1022 plus the
+// bit length of T, at most 1997), so no subnormal or overflow case arises.  The result equals
+// RN(th 2^(32+sc) + tl 2^sc), the sum of the two exact parts rounded once.
+__device__ __forceinline__ double oz_round(const long long th, const long long tl, const int sc) {
+  const __int128 T = (__int128)th * 4294967296LL + (__int128)tl;
+  const unsigned long long sign = T < 0 ? 0x8000000000000000ull : 0ull;
+  const unsigned __int128 mag = (unsigned __int128)(T < 0 ? -T : T);
+  const unsigned long long hi = (unsigned long long)(mag >> 64), lo = (unsigned long long)mag;
+  if ((hi | lo) == 0ull) return 0.0;
+  const int nb = hi ? 128 - __clzll((long long)hi) : 64 - __clzll((long long)lo);  // bit length
+  unsigned long long q;  // significand, 2^52 <= q < 2^53
+  int e2;                // value = q 2^(e2 + sc)
+  if (nb <= 53) {
+    q = lo << (53 - nb);
+    e2 = nb - 53;
+  } else {
+    const int sh = nb - 53;
+    const unsigned __int128 qq = mag >> sh;
+    const unsigned __int128 rem = mag - (qq << sh);
+    const unsigned __int128 half = (unsigned __int128)1 << (sh - 1);
+    q = (unsigned long long)qq;
+    if (rem > half || (rem == half && (q & 1ull))) q++;
+    e2 = sh;
+    if (q >> 53) {  // rounded up to 2^53
+      q >>= 1;
+      e2++;
+    }
+  }
+  const unsigned long long be = (unsigned long long)(e2 + sc + 52 + 1023);
+  return __longlong_as_double((long long)(sign | (be << 52) | (q & 0xFFFFFFFFFFFFFull)));
 }
 
 // One 16-row tile: cells c0..c0+3 x the four variables (row r: cell c0 + r / 4, variable r % 4, so
@@ -168,14 +217,7 @@ __device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *_
         if (em[r] == 0x7FF) {
           out = __longlong_as_double(0x7FF8000000000000LL);
         } else if (sc >= -1022 && sc <= 900) {
-          // th 2^(32+sc) + tl 2^sc without an integer-to-double conversion: for |t| < 2^51 the
-          // integer sum of t and the bit pattern of 1.5 2^52 u is the double 1.5 2^52 u + t u, and
-          // subtracting 1.5 2^52 u leaves t u exactly.  One rounding, in the final addition.
-          const long long mh = ((long long)(sc + 32 + 52 + 1023) << 52) | (1LL << 51);
-          const long long ml = ((long long)(sc + 52 + 1023) << 52) | (1LL << 51);
-          const double hv = __longlong_as_double(mh + th) - __longlong_as_double(mh);
-          const double lv = __longlong_as_double(ml + tl) - __longlong_as_double(ml);
-          out = hv + lv;
+          out = oz_round(th, tl, sc);
         } else if (sc < -1022) {
           out = 0.0;  // below 2^-1022: negligible against any physical value
         } else {
@@ -220,6 +262,14 @@ template <int N, int NUe, int NUo, int NRe, int NRo>
 __device__ __forceinline__ void oz_contract(const double *Xd, double *Yd, const int warp, const int nw,
                                             const int lane) {
   oz_product<N, 0, NUe, NRe, NUo, NRo, NUe, NRe>(Xd, Yd, warp, nw, lane);
+}
+
+// The dense form: Y rows 0..NP-1 (one per node) = A (NP x NK) applied to the NK slots in their
+// natural order (Fr, Fs, face points).
+template <int N, int NK, int NP>
+__device__ __forceinline__ void oz_contract_dense(const double *Xd, double *Yd, const int warp, const int nw,
+                                                  const int lane) {
+  oz_product<N, 2, NK, NP, 0, 0, NK, NP>(Xd, Yd, warp, nw, lane);
 }
 
 // The adjoint element kernel's transposed contraction: columns 0..NUe-1 = S_e^T (even rows of the
@@ -276,14 +326,18 @@ static int oz_digits(const std::vector<double> &S, int NUe, int NUo, int NRe, in
   return 0;
 }
 
-static int oz_upload(int N, const std::vector<double> &S, int NUe, int NUo, int NRe, int NRo, std::string &err) {
-  if (!oz_used(N, true)) return 0;
-  static int fexp[2][2][kOzRows];
-  static uint2 frag[2][2][4][7][2][32];
+// A: the dense rows (Np x NK, row-major) for the dense form's table (T = 2).
+static int oz_upload(int N, const std::vector<double> &S, int NUe, int NUo, int NRe, int NRo,
+                     const std::vector<double> &A, int Np, int NK, std::string &err) {
+  if (!oz_used(N, true) && !ozd_used(N, 2)) return 0;
+  static int fexp[kOzTables][2][kOzRows];
+  static uint2 frag[kOzTables][2][4][7][2][32];
   std::memset(fexp, 0, sizeof(fexp));
   std::memset(frag, 0, sizeof(frag));
-  for (int T = 0; T < 2; T++) {
-    if (T == 1 && !oz_used_t(N, true)) break;
+  for (int T = 0; T < kOzTables; T++) {
+    if (T == 0 && !oz_used(N, true)) continue;
+    if (T == 1 && !oz_used_t(N, true)) continue;
+    if (T == 2 && !ozd_used(N, 2)) continue;
     // T = 1: the transposed blocks, S_e^T (NUe x NRe) then S_o^T (NUo x NRo)
     std::vector<double> ST;
     if (T == 1) {
@@ -296,7 +350,8 @@ static int oz_upload(int N, const std::vector<double> &S, int NUe, int NUo, int 
     }
     std::vector<int> dig;
     const int rc = T == 0 ? oz_digits(S, NUe, NUo, NRe, NRo, fexp[0], dig, err)
-                          : oz_digits(ST, NRe, NRo, NUe, NUo, fexp[1], dig, err);
+                 : T == 1 ? oz_digits(ST, NRe, NRo, NUe, NUo, fexp[1], dig, err)
+                          : oz_digits(A, NK, 0, Np, 0, fexp[2], dig, err);
     if (rc) return rc;
     for (int p = 0; p < 2; p++)
       for (int nt = 0; nt < 4; nt++)
@@ -310,7 +365,7 @@ static int oz_upload(int N, const std::vector<double> &S, int NUe, int NUo, int 
             }
   }
   cudaError_t ce = cudaSuccess;
-  for (int T = 0; T < 2 && ce == cudaSuccess; T++) {
+  for (int T = 0; T < kOzTables && ce == cudaSuccess; T++) {
     ce = cudaMemcpyToSymbol(c_ozf, fexp[T], sizeof(fexp[T]), ((size_t)T * 7 + N) * sizeof(fexp[T]));
     if (ce == cudaSuccess)
       ce = cudaMemcpyToSymbol(g_ozb, frag[T], sizeof(frag[T]), ((size_t)T * 7 + N) * sizeof(frag[T]));

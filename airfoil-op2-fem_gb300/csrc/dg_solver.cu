@@ -421,12 +421,17 @@ __global__ void __launch_bounds__(32 * np_of(N)) elem_kernel(const Inst d, const
 // differences give y_i - y_P(i).  The contraction shrinks to 0.55-0.62 of the dense one.
 // One tile of 32 cells starting at e0, thread (lane, node i) of a block with at least Np
 // node-warps (warps with i >= Np only take part in the barriers).
-template <int N, bool PDL = false, bool TC = false>
+// TC: 0 the even/odd contraction in FP64, 1 the even/odd blocks on the tensor cores (N = 3-5),
+// 2 the dense rows on the tensor cores (N <= 3, no butterfly; the even/odd blocks on the tensor
+// cores at N = 4, 5).
+template <int N, bool PDL = false, int TC = 0>
 __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, const int e0, const int lane,
                                               const int i, double2 *X) {
   constexpr int Np = np_of(N), Nfp = N + 1, NK = nk_of(N);
   constexpr int NUe = Sym<N>::NUe, NUo = Sym<N>::NUo, NRe = Sym<N>::NRe;
   constexpr int NPin = NUo;  // input pairs
+  constexpr bool DENSE = ozd_used(N, TC);           // dense rows, slots in natural order
+  constexpr bool SYMTC = !DENSE && oz_used(N, TC != 0);  // even/odd blocks on the tensor cores
   double2 *Y = X + NK * 32 * 2;
   const int nthr = 32 * Np, tid = i * 32 + lane;
   const bool active = i < Np;
@@ -462,7 +467,7 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
       fs3 = V * ep;
     }
     if (active) {
-      const int pr = c_pos[N][i], ps = c_pos[N][Np + i];
+      const int pr = DENSE ? i : c_pos[N][i], ps = DENSE ? Np + i : c_pos[N][Np + i];
       X[(pr * 32 + lane) * 2] = make_double2(fr0, fr1);
       X[(pr * 32 + lane) * 2 + 1] = make_double2(fr2, fr3);
       X[(ps * 32 + lane) * 2] = make_double2(fs0, fs1);
@@ -481,24 +486,30 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
       a = ld2(fp);
       b = ld2(fp + 2);
     }
-    const int pf = c_pos[N][2 * Np + f];
+    const int pf = DENSE ? 2 * Np + f : c_pos[N][2 * Np + f];
     X[(pf * 32 + el) * 2] = a;
     X[(pf * 32 + el) * 2 + 1] = b;
   }
   __syncthreads();
-  // butterfly over the input pairs: slot p <- x_a + x_b, slot NUe + p <- x_a - x_b
-  for (int j = active ? tid : NPin * 32; j < NPin * 32; j += nthr) {
-    const int p = j >> 5, el = j & 31;
-    double2 *xa = X + (p * 32 + el) * 2, *xb = X + ((NUe + p) * 32 + el) * 2;
-    const double2 a0 = xa[0], a1 = xa[1], b0 = xb[0], b1 = xb[1];
-    xa[0] = make_double2(a0.x + b0.x, a0.y + b0.y);
-    xa[1] = make_double2(a1.x + b1.x, a1.y + b1.y);
-    xb[0] = make_double2(a0.x - b0.x, a0.y - b0.y);
-    xb[1] = make_double2(a1.x - b1.x, a1.y - b1.y);
+  if constexpr (!DENSE) {
+    // butterfly over the input pairs: slot p <- x_a + x_b, slot NUe + p <- x_a - x_b
+    for (int j = active ? tid : NPin * 32; j < NPin * 32; j += nthr) {
+      const int p = j >> 5, el = j & 31;
+      double2 *xa = X + (p * 32 + el) * 2, *xb = X + ((NUe + p) * 32 + el) * 2;
+      const double2 a0 = xa[0], a1 = xa[1], b0 = xb[0], b1 = xb[1];
+      xa[0] = make_double2(a0.x + b0.x, a0.y + b0.y);
+      xa[1] = make_double2(a1.x + b1.x, a1.y + b1.y);
+      xb[0] = make_double2(a0.x - b0.x, a0.y - b0.y);
+      xb[1] = make_double2(a1.x - b1.x, a1.y - b1.y);
+    }
+    __syncthreads();
   }
-  __syncthreads();
   double r0 = 0.0, r1 = 0.0, r2 = 0.0, r3 = 0.0;
-  if constexpr (oz_used(N, TC)) {
+  if constexpr (DENSE) {
+    // the dense rows on the tensor cores: Y row i is node i's right-hand side
+    oz_contract_dense<N, NK, Np>(reinterpret_cast<const double *>(X), reinterpret_cast<double *>(Y), i,
+                                 (int)(blockDim.x * blockDim.y) >> 5, lane);
+  } else if constexpr (SYMTC) {
     // the contraction on the tensor cores (dg_ozaki.cuh), every warp of the block taking part
     oz_contract<N, NUe, NUo, NRe, Sym<N>::NRo>(reinterpret_cast<const double *>(X), reinterpret_cast<double *>(Y),
                                                i, (int)(blockDim.x * blockDim.y) >> 5, lane);
@@ -524,12 +535,15 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
       r3 = fma(c, x23.y, r3);
     }
   }
-  if (active && !oz_used(N, TC)) {
+  if (active && !DENSE && !SYMTC) {
     Y[(i * 32 + lane) * 2] = make_double2(r0, r1);
     Y[(i * 32 + lane) * 2 + 1] = make_double2(r2, r3);
   }
   __syncthreads();
-  if (active) {
+  if (DENSE && active) {
+    const double2 y01 = Y[(i * 32 + lane) * 2], y23 = Y[(i * 32 + lane) * 2 + 1];
+    r0 = y01.x; r1 = y01.y; r2 = y23.x; r3 = y23.y;
+  } else if (active) {
     const int re = c_out[N][3 * i], ro = c_out[N][3 * i + 1], sg = c_out[N][3 * i + 2];
     const double2 e01 = Y[(re * 32 + lane) * 2], e23 = Y[(re * 32 + lane) * 2 + 1];
     r0 = e01.x; r1 = e01.y; r2 = e23.x; r3 = e23.y;
@@ -542,7 +556,7 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
       }
     }
   }
-  if constexpr (oz_used(N, TC)) {
+  if constexpr (DENSE || SYMTC) {
     // re-read this node's W rather than holding it through the contraction (registers); the
     // node is written only below, by this thread
     if (live) {
@@ -560,7 +574,7 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
 // tensor-core form; at N = 3 without the bound it takes ~95 registers and runs two blocks per SM,
 // measured slower).
 // tile0: first 32-cell tile of this launch (a launch may cover a range of the tiles).
-template <int N, bool TC, int MB = 1>
+template <int N, int TC, int MB = 1>
 __global__ void __launch_bounds__(32 * np_of(N), MB) elem_kernel_sym(const Inst d, const int stage, const int tile0) {
   extern __shared__ double2 Xs[];  // [NK][32] x 4 doubles, then [Np][32] x 4 doubles
   pdl_trigger();  // the next face kernel may be scheduled (it waits for this grid's writes)
@@ -784,17 +798,26 @@ static void launch_face(const Inst &d, int stage, cudaStream_t s) {
   launch_pdl(face_kernel<N>, dim3((nf + bs - 1) / bs), dim3(bs), 0, s, d, stage);
 }
 
-// 2: even/odd with the contraction on the bf16 tensor cores (dg_ozaki.cuh; at N = 3, 4, 5, the
-// even/odd FP64 kernel at the other orders; default), 1: even/odd element kernel, 0: dense.
-static int g_elem_variant = 2;
+// 3: dense rows on the bf16 tensor cores at N = 1, 2 (dg_ozaki.cuh), form 2 at the other orders
+// (default);
+// 2: even/odd with the contraction on the bf16 tensor cores (at N = 3, 4, 5, the even/odd FP64
+// kernel at the other orders), 1: even/odd element kernel, 0: dense FP64.
+static int g_elem_variant = 3;
 
 template <int N>
 static void launch_elem(const Inst &d, int stage, cudaStream_t s) {
   constexpr int Np = np_of(N), NK = nk_of(N);
   if (g_elem_variant) {
     const size_t smem = (size_t)(NK + Np) * 32 * 4 * sizeof(double);
+    if constexpr (ozd_used(N, 2)) {
+      if (g_elem_variant == 3) {
+        launch_pdl(elem_kernel_sym<N, 2, oz_min_blocks(N)>, dim3((d.K + 31) / 32), dim3(32, Np), smem, s, d,
+                   stage, 0);
+        return;
+      }
+    }
     if constexpr (oz_used(N, true)) {
-      if (g_elem_variant == 2) {
+      if (g_elem_variant >= 2) {
         launch_pdl(elem_kernel_sym<N, true, oz_min_blocks(N)>, dim3((d.K + 31) / 32), dim3(32, Np), smem, s, d,
                    stage, 0);
         return;
@@ -812,8 +835,14 @@ template <int N>
 static void launch_elem_tiles(const Inst &d, int stage, int t0, int t1, cudaStream_t s) {
   constexpr int Np = np_of(N), NK = nk_of(N);
   const size_t smem = (size_t)(NK + Np) * 32 * 4 * sizeof(double);
+  if constexpr (ozd_used(N, 2)) {
+    if (g_elem_variant == 3) {
+      elem_kernel_sym<N, 2, oz_min_blocks(N)><<<t1 - t0, dim3(32, Np), smem, s>>>(d, stage, t0);
+      return;
+    }
+  }
   if constexpr (oz_used(N, true)) {
-    if (g_elem_variant == 2) {
+    if (g_elem_variant >= 2) {
       elem_kernel_sym<N, true, oz_min_blocks(N)><<<t1 - t0, dim3(32, Np), smem, s>>>(d, stage, t0);
       return;
     }
@@ -837,6 +866,11 @@ static cudaError_t set_smem_attr() {
   if constexpr (oz_used(N, true)) {
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(elem_kernel_sym<N, true, oz_min_blocks(N)>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem_sym);
+  }
+  if constexpr (ozd_used(N, 2)) {
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(elem_kernel_sym<N, 2, oz_min_blocks(N)>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)smem_sym);
   }
   return e;
@@ -942,7 +976,7 @@ static int sym_tables(const Operators &o, const std::vector<double> &A, std::str
   if (ce == cudaSuccess) ce = cudaMemcpyToSymbol(c_pos, t.pos, sizeof(t.pos), (size_t)N * sizeof(t.pos));
   if (ce == cudaSuccess) ce = cudaMemcpyToSymbol(c_out, t.out, sizeof(t.out), (size_t)N * sizeof(t.out));
   if (ce != cudaSuccess) { err = std::string("constant upload: ") + cudaGetErrorString(ce); return -3; }
-  return oz_upload(N, t.S, t.NUe, t.NUo, t.NRe, t.NRo, err);
+  return oz_upload(N, t.S, t.NUe, t.NUo, t.NRe, t.NRo, A, o.Np, 2 * o.Np + 3 * o.Nfp, err);
 }
 
 // Dense rows [Drw | Dsw | -LIFT] of order N.
@@ -1017,7 +1051,7 @@ int load_order_constants(int N, std::string &err) {
   return 0;
 }
 
-void set_elem_variant(int v) { g_elem_variant = (v >= 0 && v <= 2) ? v : 2; }
+void set_elem_variant(int v) { g_elem_variant = (v >= 0 && v <= 3) ? v : 3; }
 int elem_variant() { return g_elem_variant; }
 void set_pdl(int on) { g_pdl = on ? 1 : 0; }
 void set_face_block(int b) { g_face_block = (b >= 32 && b <= 256 && b % 32 == 0) ? b : 64; }

@@ -534,7 +534,7 @@ def main():
     # the element kernel in its all-FP64 even/odd form on the same workload, for comparison
     variant = pkg.lib().dg_elem_variant()
     elem_ms_fp64 = None
-    if variant == 2:
+    if variant >= 2:
         pkg.lib().dg_set_elem_variant(1)
         try:
             s64 = pkg.Solver(mesh, pkg.config(N=N_ORDER, cfl=CFL)).init()
@@ -583,11 +583,12 @@ def main():
                      "traffic": traffic if dominant == "elem_kernel" else None,
                      "traffic_source": "ncu dram__bytes_read+write per launch, stage average (profiles/)",
                      "peak_source": "DFMA throughput measured live on this GPU (MEASURED_PEAKS.json has no FP64 figure)",
-                     "elem_form": {2: "even/odd, contraction on the bf16 tensor cores (exact integer product)",
+                     "elem_form": {3: "even/odd, contraction on the bf16 tensor cores (exact integer product)",
+                                   2: "even/odd, contraction on the bf16 tensor cores (exact integer product)",
                                    1: "even/odd, FP64", 0: "dense FP64"}[variant],
                      "frac_note": ("FP64-equivalent: algorithmic FP64 flops over the DFMA peak; the contraction "
                                    "runs on the tensor cores, so frac can exceed 1 (FP64 pipe busy 70-74 % of "
-                                   "active cycles per ncu)") if variant == 2 else "FP64 flops over the DFMA peak",
+                                   "active cycles per ncu)") if variant >= 2 else "FP64 flops over the DFMA peak",
                      "elem_ms_fp64_form": elem_ms_fp64,
                      "fp64_tensor_peak_tflops": dmma_gflops * 1e-3,
                      "fp64_tensor_note": "DMMA (mma.sync m8n8k4 f64) measured live; below DFMA and on the same pipe, so unused",

@@ -256,11 +256,12 @@ double dg_fp64_peak_gflops(void);
 double dg_fp64_mma_peak_gflops(void);
 /* Number of kernels one dg_solver_run step launches. */
 int dg_kernels_per_step(void);
-/* Element-kernel form for launches and graphs built from now on: 2 (default) the even/odd split
- * of [Drw | Dsw | -LIFT] with its contraction on the bf16 tensor cores as an exact integer
- * product at orders N = 3, 4, 5 and in FP64 at the other orders, 1 the even/odd split in FP64, 0 dense
- * FP64 rows.  All compute the same right-hand side to rounding (the tensor-core contraction is
- * the correctly rounded dot product of the 56-bit truncated inputs). */
+/* Element-kernel form for launches and graphs built from now on: 3 (default) the dense rows
+ * [Drw | Dsw | -LIFT] on the bf16 tensor cores as an exact integer product at orders N = 1, 2 and
+ * form 2 at the other orders; 2 the even/odd split of those rows with its contraction on the
+ * tensor cores at orders N = 3, 4, 5 and in FP64 at the other orders; 1 the even/odd split in
+ * FP64; 0 dense FP64 rows.  All compute the same right-hand side to rounding (the tensor-core
+ * contraction is the correctly rounded dot product of the 56-bit truncated inputs). */
 void dg_set_elem_variant(int variant);
 /* The current element-kernel form. */
 int dg_elem_variant(void);

@@ -178,8 +178,8 @@ def test_step_host_pinned_buffers_equal_run(pkg, omesh, nsteps):
     assert np.array_equal(a.get("q"), b.get("q")) and a.time() == b.time()
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2])
-@pytest.mark.parametrize("case", ["ogrid_n3", "ogrid_n4", "tiny_n3", "vortex_n3"])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+@pytest.mark.parametrize("case", ["ogrid_n2", "ogrid_n3", "ogrid_n4", "tiny_n3", "vortex_n3"])
 def test_step_host_ranges_equal_run(pkg, omesh, variant, case):
     """The host-buffer call's last step runs its final element kernel as four ranges of cells
     on separate streams, each copied back as soon as it is final: bitwise the graph step, for
@@ -191,7 +191,7 @@ def test_step_host_ranges_equal_run(pkg, omesh, variant, case):
                          vortex_y0=0.0, vortex_beta=5.0)
     else:
         m = omesh.naca_ogrid(8, 4) if case == "tiny_n3" else omesh.naca_ogrid(64, 16)
-        cfg = pkg.config(N=4 if case == "ogrid_n4" else 3, cfl=0.5)
+        cfg = pkg.config(N={"ogrid_n4": 4, "ogrid_n2": 2}.get(case, 3), cfl=0.5)
     prev = pkg.lib().dg_elem_variant()
     pkg.lib().dg_set_elem_variant(variant)
     try:
@@ -233,12 +233,14 @@ def test_nonphysical_state_is_reported(pkg, omesh):
 @pytest.mark.parametrize("N", [1, 2, 3, 4, 5, 6])
 def test_even_odd_form_equals_dense_form(pkg, orc, omesh, N):
     """The element-kernel forms compute the same RHS and steps: dense FP64 rows (0), the even/odd
-    split in FP64 (1) and the even/odd split with the tensor-core contraction (2, the default;
-    used at N = 3, 4, 5, FP64 at the other orders)."""
+    split in FP64 (1), the even/odd split with the tensor-core contraction (2; used at N = 3, 4,
+    5, FP64 at the other orders) and form 3 (the default: the dense rows on the tensor cores at
+    N = 1, 2, form 2 at the other orders)."""
     m = omesh.naca_ogrid(32, 8, farfield="characteristic")
     out = []
     prev = pkg.lib().dg_elem_variant()
-    for variant in (0, 1, 2):
+    assert prev == 3
+    for variant in (0, 1, 2, 3):
         pkg.lib().dg_set_elem_variant(variant)
         try:
             s = pkg.Solver(pkg.Mesh.from_tables(m), pkg.config(N=N, cfl=0.5)).init()
@@ -250,17 +252,22 @@ def test_even_odd_form_equals_dense_form(pkg, orc, omesh, N):
             out.append((r, s.get("q")))
         finally:
             pkg.lib().dg_set_elem_variant(prev)
-    for k in (1, 2):
+    for k in (1, 2, 3):
         assert orc.rel_l2(out[k][0], out[0][0]) < 1e-13
         assert orc.rel_l2(out[k][1], out[0][1]) < 1e-13
     if N not in (3, 4, 5):
         assert np.array_equal(out[2][0], out[1][0])  # form 2 is form 1 at the other orders
+    if N >= 3:
+        assert np.array_equal(out[3][0], out[2][0])  # form 3 is form 2 from N = 3 on
+        assert np.array_equal(out[3][1], out[2][1])
+    else:
+        assert not np.array_equal(out[3][0], out[1][0])  # the dense tensor-core rows ran
 
 
-def _rhs_forms(pkg, m, W, N=3):
+def _rhs_forms(pkg, m, W, N=3, tc_variant=2):
     out = []
     prev = pkg.lib().dg_elem_variant()
-    for variant in (1, 2):
+    for variant in (1, tc_variant):
         pkg.lib().dg_set_elem_variant(variant)
         try:
             s = pkg.Solver(pkg.Mesh.from_tables(m), pkg.config(N=N, cfl=0.5)).init()
@@ -270,7 +277,7 @@ def _rhs_forms(pkg, m, W, N=3):
     return out
 
 
-@pytest.mark.parametrize("N", [3, 4, 5])
+@pytest.mark.parametrize("N", [1, 2, 3, 4, 5])
 def test_tensor_core_contraction_wide_range(pkg, omesh, N):
     """Cells whose states differ by up to 1e6 in scale (each cell's state scaled as a whole, so
     it stays physical): the tensor-core contraction scales every column by its own largest
@@ -280,7 +287,7 @@ def test_tensor_core_contraction_wide_range(pkg, omesh, N):
     q = s.get("q").reshape(m["cell2nodes"].shape[0], -1)
     lam = 10.0 ** np.random.default_rng(7).uniform(-3, 3, q.shape[0])
     W = (q * lam[:, None]).ravel()
-    r1, r2 = _rhs_forms(pkg, m, W, N)
+    r1, r2 = _rhs_forms(pkg, m, W, N, tc_variant=3 if N <= 2 else 2)
     assert np.all(np.isfinite(r2))
     assert np.linalg.norm(r2 - r1) <= 1e-13 * np.linalg.norm(r1)
     # entrywise: near the wall the staged fluxes are ~1e3-1e4 and cancel to an O(1) RHS, so
@@ -288,17 +295,20 @@ def test_tensor_core_contraction_wide_range(pkg, omesh, N):
     assert np.abs(r2 - r1).max() <= 1e-11 * np.abs(r1).max()
 
 
-def test_tensor_core_contraction_nonfinite(pkg, omesh):
+@pytest.mark.parametrize("N", [2, 3])
+def test_tensor_core_contraction_nonfinite(pkg, omesh, N):
     """A non-finite value in a cell's staged column gives NaN there, as the FP64 contraction
-    does, and leaves the cells it does not reach finite."""
+    does, and leaves the cells it does not reach finite (the dense rows at N = 2, the even/odd
+    blocks at N = 3)."""
     m = omesh.naca_ogrid(32, 8, farfield="characteristic")
-    s = pkg.Solver(pkg.Mesh.from_tables(m), pkg.config(N=3, cfl=0.5)).init()
+    s = pkg.Solver(pkg.Mesh.from_tables(m), pkg.config(N=N, cfl=0.5)).init()
     q = s.get("q")
+    nc = 2 * (N + 1) * (N + 2)  # doubles per cell
     W = q * (1.0 + 0.05 * np.random.default_rng(3).standard_normal(q.size))
-    W[40 * 17 + 5] = np.nan
-    r1, r2 = _rhs_forms(pkg, m, W)
+    W[nc * 17 + 5] = np.nan
+    r1, r2 = _rhs_forms(pkg, m, W, N, tc_variant=3 if N <= 2 else 2)
     assert np.isnan(r2).any()
-    assert np.array_equal(np.isnan(r1.reshape(-1, 40)).any(1), np.isnan(r2.reshape(-1, 40)).any(1))
+    assert np.array_equal(np.isnan(r1.reshape(-1, nc)).any(1), np.isnan(r2.reshape(-1, nc)).any(1))
     ok = ~np.isnan(r1)
     assert np.linalg.norm(r2[ok] - r1[ok]) <= 1e-13 * np.linalg.norm(r1[ok])
     assert np.abs(r2[ok] - r1[ok]).max() <= 1e-11 * np.abs(r1[ok]).max()
