@@ -36,11 +36,13 @@ __constant__ double c_wq[7][8];    // face quadrature weights per order
 __constant__ int c_fpt[7][28 * 2]; // face points k with FMASK[k] == node (up to two; -1 none)
 
 // ---------------------------------------------------------------- reverse of roe_flux2
-// Adds to qmb, qpb the adjoints of qm, qp given fb, the adjoint of roe_flux2's output f2.
+// Adds to qmb, qpb the adjoints of qm, qp given fb, the adjoint of roe_flux2's output f2.  The
+// forward sweep writes the Roe averages with the weights sqrt(rho_L), sqrt(rho_R) (roe_flux2 divides
+// them through by sqrt(rho_L)): the same function, whose reverse sweep is shorter in this form.
 __device__ __forceinline__ void roe_flux2_adj(const double qm[4], const double qp[4], const double nx,
                                               const double ny, const Phys &P, const double fb[4], double qmb[4],
                                               double qpb[4]) {
-  // forward sweep (as roe_flux2)
+  // forward sweep
   const double mL = fma(nx, qm[1], ny * qm[2]);
   const double tL = fma(nx, qm[2], -ny * qm[1]);
   const double mR = fma(nx, qp[1], ny * qp[2]);

@@ -51,21 +51,27 @@ __device__ __forceinline__ void roe_flux2(const double qm[4], const double qp[4]
   const double tL = fma(nx, qm[2], -ny * qm[1]);
   const double mR = fma(nx, qp[1], ny * qp[2]);
   const double tR = fma(nx, qp[2], -ny * qp[1]);
-  const double rsL = rsqrt(qm[0]), rsR = rsqrt(qp[0]);
-  const double sL = qm[0] * rsL, sR = qp[0] * rsR;     // sqrt(rho)
-  const double irL = rsL * rsL, irR = rsR * rsR;       // 1/rho
+  // One reciprocal square root serves both sides: with r = 1/sqrt(rho_L rho_R),
+  // 1/rho_L = rho_R r^2, 1/rho_R = rho_L r^2, sqrt(rho_R / rho_L) = rho_R r and the Roe density
+  // sqrt(rho_L rho_R) = rho_L rho_R r.
+  const double PLR = qm[0] * qp[0];
+  const double r = rsqrt(PLR);
+  const double r2 = r * r;
+  const double irL = qp[0] * r2, irR = qm[0] * r2;   // 1/rho
   const double uL = mL * irL, vL = tL * irL;
   const double uR = mR * irR, vR = tR * irR;
   const double pL = P.gm1 * fma(-0.5, fma(mL, uL, tL * vL), qm[3]);
   const double pR = P.gm1 * fma(-0.5, fma(mR, uR, tR * vR), qp[3]);
   const double EpL = qm[3] + pL, EpR = qp[3] + pR;
   const double HL = EpL * irL, HR = EpR * irR;
-  // Roe averages
-  const double rho = sL * sR;
-  const double isum = rcp(sL + sR);
-  const double u = fma(sL, uL, sR * uR) * isum;
-  const double v = fma(sL, vL, sR * vR) * isum;
-  const double H = fma(sL, HL, sR * HR) * isum;
+  // Roe averages (sqrt(rho_L) x_L + sqrt(rho_R) x_R) / (sqrt(rho_L) + sqrt(rho_R)), divided through
+  // by sqrt(rho_L): (x_L + R x_R) / (1 + R), R = sqrt(rho_R / rho_L)
+  const double rho = PLR * r;
+  const double R = qp[0] * r;
+  const double isum = rcp(1.0 + R);
+  const double u = fma(R, uR, uL) * isum;
+  const double v = fma(R, vR, vL) * isum;
+  const double H = fma(R, HR, HL) * isum;
   const double q2 = fma(u, u, v * v);
   const double c2 = P.gm1 * fma(-0.5, q2, H);
   const double rc = rsqrt(c2);

@@ -117,19 +117,39 @@ __device__ __forceinline__ double oz_round(const long long th, const long long t
   return __longlong_as_double((long long)(sign | (be << 52) | (q & 0xFFFFFFFFFFFFFull)));
 }
 
+// Bit pattern of a double -> its magnitude aligned to the biased column exponent em as an integer,
+// M 2^(e - em + SH) (M the 53-bit significand), with the double's sign; 0 below 2^-63 of the
+// column's leading bit.
+template <int SH>
+__device__ __forceinline__ long long oz_align(const unsigned long long b, const int em) {
+  const int e = (int)((b >> 52) & 0x7FF);
+  const unsigned long long M = e ? ((b & 0xFFFFFFFFFFFFFull) | (1ull << 52)) : 0ull;
+  const int sh = e - em + SH;
+  const unsigned long long m = sh >= 0 ? (M << sh) : (sh > -64 ? (M >> -sh) : 0ull);
+  return (b >> 63) ? -(long long)m : (long long)m;
+}
+
 // One 16-row tile: cells c0..c0+3 x the four variables (row r: cell c0 + r / 4, variable r % 4, so
 // the eight row lanes of a fragment read eight consecutive doubles), slots SLOT0..SLOT0+K-1
 // (K <= 16 KST), times operator rows 8 NT .. 8 NT + 7 (of R) of parity P, written to Y rows
 // YROW0 + row.  The k-steps are taken one after the other (their values re-read from shared
 // memory) so that only one k-step's magnitudes are live next to the seven accumulators.
-template <int T, int NORD, int K, int R, int SLOT0, int YROW0, int KST, int P, int NT>
+// BF (the even/odd butterfly, done here in integers instead of on the staged doubles): 0 the
+// slot values as they are; 1 slot k plus slot PAIR0 + k for k < NPAIR, slot k alone above;
+// 2 slot k minus slot PAIR0 + k.  Both values are aligned to the largest exponent of all the
+// values read (as 55-bit integers, so that the exact sum or difference fits 56 bits), which makes
+// the butterfly exact and leaves no FP64 instruction in it.
+template <int T, int NORD, int K, int R, int SLOT0, int YROW0, int KST, int P, int NT, int BF = 0, int PAIR0 = 0,
+          int NPAIR = 0>
 __device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *__restrict__ Yd, const int c0,
                                         const int lane) {
   static_assert(KST <= 2 && K <= 16 * KST && R > 8 * NT && NT < 4, "four n-tiles, two k-steps at most");
+  static_assert(BF == 0 || (SLOT0 == 0 && (BF == 1 ? NPAIR <= K : NPAIR == K)), "butterfly operands");
+  constexpr int SH = BF ? 2 : 3;  // alignment of a value below 2^56 (2^55 for butterfly operands)
   const int g = lane >> 2, t = lane & 3;
   const int col = c0 * 4 + g;  // (cell, variable) of row g; row g + 8 is col + 8
   const uint32_t *Xw = reinterpret_cast<const uint32_t *>(Xd);
-  // largest binary exponent of each of the two columns over all K slots (high words only)
+  // largest binary exponent of each of the two columns over all values read (high words only)
   int em[2] = {0, 0};
 #pragma unroll
   for (int ks = 0; ks < KST; ks++)
@@ -139,6 +159,7 @@ __device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *_
       for (int q = 0; q < 4; q++) {
         const int k = 16 * ks + 2 * t + (q & 1) + ((q >> 1) << 3);
         if (k < K) em[r] = max(em[r], (int)((Xw[2 * ((SLOT0 + k) * 128 + col + 8 * r) + 1] >> 20) & 0x7FF));
+        if (BF && k < NPAIR) em[r] = max(em[r], (int)((Xw[2 * ((PAIR0 + k) * 128 + col + 8 * r) + 1] >> 20) & 0x7FF));
       }
 #pragma unroll
   for (int r = 0; r < 2; r++) {
@@ -152,35 +173,30 @@ __device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *_
 #pragma unroll
   for (int ks = 0; ks < KST; ks++) {
     // this k-step's values at slots 16 ks + {2t, 2t+1, 2t+8, 2t+9}: aligned magnitudes
-    // m = M 2^(e - E + 3) (M the 53-bit significand) and the sign pattern of every A-fragment
-    // register (pairs (g: q0 q1), (g+8: q0 q1), (g: q2 q3), (g+8: q2 q3))
-    uint32_t hi[2][4], lo[2][4];
+    // m = M 2^(e - E + SH) (M the 53-bit significand; for BF the exact integer sum or difference
+    // of two such values) and the sign pattern of every A-fragment register (pairs (g: q0 q1),
+    // (g+8: q0 q1), (g: q2 q3), (g+8: q2 q3))
+    // sgn[r + 2 (q >> 1)]: bit 15 the sign of value (r, q) for even q, bit 31 for odd q
+    uint32_t hi[2][4], lo[2][4], sgn[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
     for (int r = 0; r < 2; r++)
 #pragma unroll
       for (int q = 0; q < 4; q++) {
         const int k = 16 * ks + 2 * t + (q & 1) + ((q >> 1) << 3);
         const double x = k < K ? Xd[(SLOT0 + k) * 128 + col + 8 * r] : 0.0;
-        const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-        hi[r][q] = (uint32_t)(b >> 32);
-        lo[r][q] = (uint32_t)b;
-      }
-    uint32_t sgn[4];
-#pragma unroll
-    for (int x = 0; x < 4; x++) {
-      const int r = x & 1, q0 = (x >> 1) * 2;
-      sgn[x] = ((hi[r][q0] >> 16) & 0x8000u) | (hi[r][q0 + 1] & 0x80000000u);
-    }
-#pragma unroll
-    for (int r = 0; r < 2; r++)
-#pragma unroll
-      for (int q = 0; q < 4; q++) {
-        const uint32_t h = hi[r][q];
-        const int e = (int)((h >> 20) & 0x7FF);
-        const unsigned long long M =
-            e ? ((((unsigned long long)(h & 0xFFFFFu)) << 32) | lo[r][q]) | (1ull << 52) : 0ull;
-        const int sh = e - em[r] + 3;
-        const unsigned long long m = sh >= 0 ? (M << sh) : (sh > -64 ? (M >> -sh) : 0ull);
+        unsigned long long b = (unsigned long long)__double_as_longlong(x);
+        if constexpr (BF != 0) {
+          const double y = k < NPAIR ? Xd[(PAIR0 + k) * 128 + col + 8 * r] : 0.0;
+          const long long ma = oz_align<SH>(b, em[r]);
+          const long long mb = oz_align<SH>((unsigned long long)__double_as_longlong(y), em[r]);
+          const long long v = BF == 1 ? ma + mb : ma - mb;
+          b = (unsigned long long)v;
+        }
+        const uint32_t sbit = (uint32_t)(b >> 32) & 0x80000000u;
+        sgn[r + 2 * (q >> 1)] |= (q & 1) ? sbit : (sbit >> 16);
+        unsigned long long m;
+        if constexpr (BF != 0) m = (b >> 63) ? (unsigned long long)(-(long long)b) : b;
+        else m = (unsigned long long)oz_align<SH>(b & 0x7FFFFFFFFFFFFFFFull, em[r]);
         hi[r][q] = (uint32_t)(m >> 32);
         lo[r][q] = (uint32_t)m;
       }
@@ -212,7 +228,7 @@ __device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *_
         const long long th = l[0] * 65536LL + l[1] * 256LL + l[2];
         const long long tl = l[3] * 16777216LL + l[4] * 65536LL + l[5] * 256LL + l[6];
         const int fe = c_ozf[T][NORD][P][n];
-        const int sc = em[r] + fe - 2046 - 62;
+        const int sc = em[r] + fe - 2046 - 62 + (3 - SH);
         double out;
         if (em[r] == 0x7FF) {
           out = __longlong_as_double(0x7FF8000000000000LL);
@@ -233,35 +249,49 @@ __device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *_
 
 // Parity 0: K0 staged slots from slot 0 to R0 outputs from row 0; parity 1: K1 slots from SLOT1
 // to R1 outputs from YROW1.  Work units: (parity, n-tile of 8 outputs, group of 4 cells); warp w
-// of nw takes units w, w + nw, ...
-template <int N, int T, int K0, int R0, int K1, int R1, int SLOT1, int YROW1, int NT>
+// of nw takes units w, w + nw, ...  IBF: the slots hold the even/odd pairs unsplit (slot k and
+// slot K0 + k for k < K1, the K0 - K1 unpaired slots below K0) and the butterfly is done in the
+// operands (oz_tile's BF): parity 0 takes the sums, parity 1 the differences.
+template <int N, int T, int K0, int R0, int K1, int R1, int SLOT1, int YROW1, int NT, bool IBF>
 __device__ __forceinline__ void oz_unit(const double *Xd, double *Yd, const int w, const int c0, const int lane) {
   constexpr int NT0 = (R0 + 7) / 8;
   if constexpr (NT < 4) {
     if (w == NT) {
-      if constexpr (NT < NT0) oz_tile<T, N, K0, R0, 0, 0, (K0 + 15) / 16, 0, NT>(Xd, Yd, c0, lane);
-      else if constexpr (NT - NT0 < (R1 + 7) / 8)
-        oz_tile<T, N, K1, R1, SLOT1, YROW1, (K1 + 15) / 16, 1, NT - NT0>(Xd, Yd, c0, lane);
+      if constexpr (NT < NT0) {
+        if constexpr (IBF) oz_tile<T, N, K0, R0, 0, 0, (K0 + 15) / 16, 0, NT, 1, K0, K1>(Xd, Yd, c0, lane);
+        else oz_tile<T, N, K0, R0, 0, 0, (K0 + 15) / 16, 0, NT>(Xd, Yd, c0, lane);
+      } else if constexpr (NT - NT0 < (R1 + 7) / 8) {
+        if constexpr (IBF) oz_tile<T, N, K1, R1, 0, YROW1, (K1 + 15) / 16, 1, NT - NT0, 2, K0, K1>(Xd, Yd, c0, lane);
+        else oz_tile<T, N, K1, R1, SLOT1, YROW1, (K1 + 15) / 16, 1, NT - NT0>(Xd, Yd, c0, lane);
+      }
       return;
     }
-    oz_unit<N, T, K0, R0, K1, R1, SLOT1, YROW1, NT + 1>(Xd, Yd, w, c0, lane);
+    oz_unit<N, T, K0, R0, K1, R1, SLOT1, YROW1, NT + 1, IBF>(Xd, Yd, w, c0, lane);
   }
 }
 
-template <int N, int T, int K0, int R0, int K1, int R1, int SLOT1, int YROW1>
+template <int N, int T, int K0, int R0, int K1, int R1, int SLOT1, int YROW1, bool IBF = false>
 __device__ __forceinline__ void oz_product(const double *Xd, double *Yd, const int warp, const int nw,
                                            const int lane) {
   constexpr int NTT = (R0 + 7) / 8 + (R1 + 7) / 8;
   static_assert(NTT <= 4, "at most 4 n-tiles");
-  for (int u = warp; u < 8 * NTT; u += nw) oz_unit<N, T, K0, R0, K1, R1, SLOT1, YROW1, 0>(Xd, Yd, u >> 3, (u & 7) * 4, lane);
+  for (int u = warp; u < 8 * NTT; u += nw)
+    oz_unit<N, T, K0, R0, K1, R1, SLOT1, YROW1, 0, IBF>(Xd, Yd, u >> 3, (u & 7) * 4, lane);
 }
 
-// The element kernel's contraction: Y rows 0..NRe-1 = S_e (even slots), Y rows NRe.. = S_o (odd
-// slots).
-template <int N, int NUe, int NUo, int NRe, int NRo>
+// Whether the element kernel leaves the even/odd butterfly to the contraction's operands (IBF):
+// at N = 3, where each parity has one n-tile of outputs, it saves the 128 FP64 adds per cell of
+// the butterfly (step 326 -> 322 us on the K=32768 O-grid); at N = 4, 5 every n-tile would redo
+// the doubled operand alignment, measured slower (501 -> 520 us, 765 -> 812 us).
+constexpr bool oz_ibf(int N) { return N == 3; }
+
+// The element kernel's contraction: Y rows 0..NRe-1 = S_e, Y rows NRe.. = S_o.  With IBF the
+// staged slots hold the pairs unsplit and the operands are x_a + x_b (and the unpaired slots) for
+// S_e, x_a - x_b for S_o; otherwise the slots hold the sums and differences already.
+template <int N, int NUe, int NUo, int NRe, int NRo, bool IBF>
 __device__ __forceinline__ void oz_contract(const double *Xd, double *Yd, const int warp, const int nw,
                                             const int lane) {
-  oz_product<N, 0, NUe, NRe, NUo, NRo, NUe, NRe>(Xd, Yd, warp, nw, lane);
+  oz_product<N, 0, NUe, NRe, NUo, NRo, NUe, NRe, IBF>(Xd, Yd, warp, nw, lane);
 }
 
 // The dense form: Y rows 0..NP-1 (one per node) = A (NP x NK) applied to the NK slots in their

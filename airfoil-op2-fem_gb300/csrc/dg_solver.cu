@@ -432,6 +432,7 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
   constexpr int NPin = NUo;  // input pairs
   constexpr bool DENSE = ozd_used(N, TC);           // dense rows, slots in natural order
   constexpr bool SYMTC = !DENSE && oz_used(N, TC != 0);  // even/odd blocks on the tensor cores
+  constexpr bool IBF = SYMTC && oz_ibf(N);  // the butterfly done in the contraction's operands
   double2 *Y = X + NK * 32 * 2;
   const int nthr = 32 * Np, tid = i * 32 + lane;
   const bool active = i < Np;
@@ -491,8 +492,9 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
     X[(pf * 32 + el) * 2 + 1] = b;
   }
   __syncthreads();
-  if constexpr (!DENSE) {
-    // butterfly over the input pairs: slot p <- x_a + x_b, slot NUe + p <- x_a - x_b
+  if constexpr (!DENSE && !IBF) {
+    // butterfly over the input pairs: slot p <- x_a + x_b, slot NUe + p <- x_a - x_b (with IBF
+    // the tensor-core contraction does it exactly in its operands instead)
     for (int j = active ? tid : NPin * 32; j < NPin * 32; j += nthr) {
       const int p = j >> 5, el = j & 31;
       double2 *xa = X + (p * 32 + el) * 2, *xb = X + ((NUe + p) * 32 + el) * 2;
@@ -511,7 +513,7 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
                                  (int)(blockDim.x * blockDim.y) >> 5, lane);
   } else if constexpr (SYMTC) {
     // the contraction on the tensor cores (dg_ozaki.cuh), every warp of the block taking part
-    oz_contract<N, NUe, NUo, NRe, Sym<N>::NRo>(reinterpret_cast<const double *>(X), reinterpret_cast<double *>(Y),
+    oz_contract<N, NUe, NUo, NRe, Sym<N>::NRo, IBF>(reinterpret_cast<const double *>(X), reinterpret_cast<double *>(Y),
                                                i, (int)(blockDim.x * blockDim.y) >> 5, lane);
   } else if (!active) {
   } else if (i < NRe) {

@@ -22,6 +22,7 @@ struct Dual {
 };
 
 __device__ __forceinline__ Dual operator+(Dual a, Dual b) { return {a.v + b.v, a.d + b.d}; }
+__device__ __forceinline__ Dual operator+(double a, Dual b) { return {a + b.v, b.d}; }
 __device__ __forceinline__ Dual operator-(Dual a, Dual b) { return {a.v - b.v, a.d - b.d}; }
 __device__ __forceinline__ Dual operator-(Dual a) { return {-a.v, -a.d}; }
 __device__ __forceinline__ Dual operator*(Dual a, Dual b) { return {a.v * b.v, fma(a.d, b.v, a.v * b.d)}; }
@@ -51,20 +52,22 @@ __device__ __forceinline__ void roe_flux2_t(const T qm[4], const T qp[4], double
   const T tL = fma(nx, qm[2], -ny * qm[1]);
   const T mR = fma(nx, qp[1], ny * qp[2]);
   const T tR = fma(nx, qp[2], -ny * qp[1]);
-  const T rsL = rsqrt(qm[0]), rsR = rsqrt(qp[0]);
-  const T sL = qm[0] * rsL, sR = qp[0] * rsR;
-  const T irL = rsL * rsL, irR = rsR * rsR;
+  const T PLR = qm[0] * qp[0];
+  const T r = rsqrt(PLR);
+  const T r2 = r * r;
+  const T irL = qp[0] * r2, irR = qm[0] * r2;
   const T uL = mL * irL, vL = tL * irL;
   const T uR = mR * irR, vR = tR * irR;
   const T pL = P.gm1 * fma(-0.5, fma(mL, uL, tL * vL), qm[3]);
   const T pR = P.gm1 * fma(-0.5, fma(mR, uR, tR * vR), qp[3]);
   const T EpL = qm[3] + pL, EpR = qp[3] + pR;
   const T HL = EpL * irL, HR = EpR * irR;
-  const T rho = sL * sR;
-  const T isum = rcp(sL + sR);
-  const T u = fma(sL, uL, sR * uR) * isum;
-  const T v = fma(sL, vL, sR * vR) * isum;
-  const T H = fma(sL, HL, sR * HR) * isum;
+  const T rho = PLR * r;
+  const T R = qp[0] * r;
+  const T isum = rcp(1.0 + R);
+  const T u = fma(R, uR, uL) * isum;
+  const T v = fma(R, vR, vL) * isum;
+  const T H = fma(R, HR, HL) * isum;
   const T q2 = fma(u, u, v * v);
   const T c2 = P.gm1 * fma(-0.5, q2, H);
   const T rc = rsqrt(c2);
