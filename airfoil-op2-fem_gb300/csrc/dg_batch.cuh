@@ -248,7 +248,7 @@ struct Batch {
     if (variant == kGroupedVariant) {
       if (ft < 32 || ft > 256 || ft % 32) { err = "grouped face tiles are 32..256 nodes, a multiple of 32"; return -1; }
       for (int n = 1; n <= 6; n++) {
-        const size_t sm = (size_t)(nk_of(n) + np_of(n)) * 32 * 4 * sizeof(double);
+        const size_t sm = elem_sym_smem(n);
         cudaError_t ce = cudaSuccess;
         DG_DISPATCH(n, ce = cudaFuncSetAttribute(batch_elem_kernel<NN, 0>,
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
@@ -273,7 +273,7 @@ struct Batch {
     if (variant < 0 || variant >= (int)vs.size()) { err = "bad variant"; return -1; }
     const BatchVariant &v = vs[variant];
     if (v.bs < 32 * maxNp) { err = "block too small for the batch's highest order"; return -1; }
-    const size_t smem = (size_t)(nk_of(maxN) + maxNp) * 32 * 4 * sizeof(double);
+    const size_t smem = (size_t)(nk_of(maxN) + maxNp) * kElemSlot * sizeof(double);
     cudaError_t ce = cudaFuncSetAttribute(v.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int per_sm = 0, dev = 0, sms = 0;
     if (ce == cudaSuccess) ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v.fn, v.bs, smem);
@@ -316,7 +316,7 @@ struct Batch {
     batch_face_kernel<<<nft, sh.face_tile, 0, s>>>(d_insts, d_ftiles, stage);
     for (int n = 6; n >= 1; n--) {
       if (!ord_count[n]) continue;
-      const size_t sm = (size_t)(nk_of(n) + np_of(n)) * 32 * 4 * sizeof(double);
+      const size_t sm = elem_sym_smem(n);
       if (g_elem_variant == 3) {
         DG_DISPATCH(n, (batch_elem_kernel<NN, 2><<<ord_count[n], 32 * np_of(NN), sm, s>>>(d_insts, d_etiles,
                                                                                           ord_first[n], stage)));

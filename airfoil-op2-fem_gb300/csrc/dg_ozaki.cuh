@@ -134,13 +134,15 @@ __device__ __forceinline__ long long oz_align(const unsigned long long b, const 
 // (K <= 16 KST), times operator rows 8 NT .. 8 NT + 7 (of R) of parity P, written to Y rows
 // YROW0 + row.  The k-steps are taken one after the other (their values re-read from shared
 // memory) so that only one k-step's magnitudes are live next to the seven accumulators.
+// XST: doubles from one slot (or output row) to the next in Xd and Yd (128 = 32 cells x 4
+// variables, plus any padding).
 // BF (the even/odd butterfly, done here in integers instead of on the staged doubles): 0 the
 // slot values as they are; 1 slot k plus slot PAIR0 + k for k < NPAIR, slot k alone above;
 // 2 slot k minus slot PAIR0 + k.  Both values are aligned to the largest exponent of all the
 // values read (as 55-bit integers, so that the exact sum or difference fits 56 bits), which makes
 // the butterfly exact and leaves no FP64 instruction in it.
 template <int T, int NORD, int K, int R, int SLOT0, int YROW0, int KST, int P, int NT, int BF = 0, int PAIR0 = 0,
-          int NPAIR = 0>
+          int NPAIR = 0, int XST = 128>
 __device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *__restrict__ Yd, const int c0,
                                         const int lane) {
   static_assert(KST <= 2 && K <= 16 * KST && R > 8 * NT && NT < 4, "four n-tiles, two k-steps at most");
@@ -158,8 +160,8 @@ __device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *_
 #pragma unroll
       for (int q = 0; q < 4; q++) {
         const int k = 16 * ks + 2 * t + (q & 1) + ((q >> 1) << 3);
-        if (k < K) em[r] = max(em[r], (int)((Xw[2 * ((SLOT0 + k) * 128 + col + 8 * r) + 1] >> 20) & 0x7FF));
-        if (BF && k < NPAIR) em[r] = max(em[r], (int)((Xw[2 * ((PAIR0 + k) * 128 + col + 8 * r) + 1] >> 20) & 0x7FF));
+        if (k < K) em[r] = max(em[r], (int)((Xw[2 * ((SLOT0 + k) * XST + col + 8 * r) + 1] >> 20) & 0x7FF));
+        if (BF && k < NPAIR) em[r] = max(em[r], (int)((Xw[2 * ((PAIR0 + k) * XST + col + 8 * r) + 1] >> 20) & 0x7FF));
       }
 #pragma unroll
   for (int r = 0; r < 2; r++) {
@@ -183,10 +185,10 @@ __device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *_
 #pragma unroll
       for (int q = 0; q < 4; q++) {
         const int k = 16 * ks + 2 * t + (q & 1) + ((q >> 1) << 3);
-        const double x = k < K ? Xd[(SLOT0 + k) * 128 + col + 8 * r] : 0.0;
+        const double x = k < K ? Xd[(SLOT0 + k) * XST + col + 8 * r] : 0.0;
         unsigned long long b = (unsigned long long)__double_as_longlong(x);
         if constexpr (BF != 0) {
-          const double y = k < NPAIR ? Xd[(PAIR0 + k) * 128 + col + 8 * r] : 0.0;
+          const double y = k < NPAIR ? Xd[(PAIR0 + k) * XST + col + 8 * r] : 0.0;
           const long long ma = oz_align<SH>(b, em[r]);
           const long long mb = oz_align<SH>((unsigned long long)__double_as_longlong(y), em[r]);
           const long long v = BF == 1 ? ma + mb : ma - mb;
@@ -242,7 +244,7 @@ __device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *_
           out = (val * __longlong_as_double((long long)(s1 + 1023) << 52)) *
                 __longlong_as_double((long long)(s2 + 1023) << 52);
         }
-        Yd[(YROW0 + n) * 128 + col + 8 * r] = out;
+        Yd[(YROW0 + n) * XST + col + 8 * r] = out;
       }
     }
 }
@@ -252,32 +254,39 @@ __device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *_
 // of nw takes units w, w + nw, ...  IBF: the slots hold the even/odd pairs unsplit (slot k and
 // slot K0 + k for k < K1, the K0 - K1 unpaired slots below K0) and the butterfly is done in the
 // operands (oz_tile's BF): parity 0 takes the sums, parity 1 the differences.
-template <int N, int T, int K0, int R0, int K1, int R1, int SLOT1, int YROW1, int NT, bool IBF>
+template <int N, int T, int K0, int R0, int K1, int R1, int SLOT1, int YROW1, int NT, bool IBF, int XST>
 __device__ __forceinline__ void oz_unit(const double *Xd, double *Yd, const int w, const int c0, const int lane) {
   constexpr int NT0 = (R0 + 7) / 8;
   if constexpr (NT < 4) {
     if (w == NT) {
       if constexpr (NT < NT0) {
-        if constexpr (IBF) oz_tile<T, N, K0, R0, 0, 0, (K0 + 15) / 16, 0, NT, 1, K0, K1>(Xd, Yd, c0, lane);
-        else oz_tile<T, N, K0, R0, 0, 0, (K0 + 15) / 16, 0, NT>(Xd, Yd, c0, lane);
+        if constexpr (IBF) oz_tile<T, N, K0, R0, 0, 0, (K0 + 15) / 16, 0, NT, 1, K0, K1, XST>(Xd, Yd, c0, lane);
+        else oz_tile<T, N, K0, R0, 0, 0, (K0 + 15) / 16, 0, NT, 0, 0, 0, XST>(Xd, Yd, c0, lane);
       } else if constexpr (NT - NT0 < (R1 + 7) / 8) {
-        if constexpr (IBF) oz_tile<T, N, K1, R1, 0, YROW1, (K1 + 15) / 16, 1, NT - NT0, 2, K0, K1>(Xd, Yd, c0, lane);
-        else oz_tile<T, N, K1, R1, SLOT1, YROW1, (K1 + 15) / 16, 1, NT - NT0>(Xd, Yd, c0, lane);
+        if constexpr (IBF)
+          oz_tile<T, N, K1, R1, 0, YROW1, (K1 + 15) / 16, 1, NT - NT0, 2, K0, K1, XST>(Xd, Yd, c0, lane);
+        else oz_tile<T, N, K1, R1, SLOT1, YROW1, (K1 + 15) / 16, 1, NT - NT0, 0, 0, 0, XST>(Xd, Yd, c0, lane);
       }
       return;
     }
-    oz_unit<N, T, K0, R0, K1, R1, SLOT1, YROW1, NT + 1, IBF>(Xd, Yd, w, c0, lane);
+    oz_unit<N, T, K0, R0, K1, R1, SLOT1, YROW1, NT + 1, IBF, XST>(Xd, Yd, w, c0, lane);
   }
 }
 
-template <int N, int T, int K0, int R0, int K1, int R1, int SLOT1, int YROW1, bool IBF = false>
+template <int N, int T, int K0, int R0, int K1, int R1, int SLOT1, int YROW1, bool IBF = false, int XST = 128>
 __device__ __forceinline__ void oz_product(const double *Xd, double *Yd, const int warp, const int nw,
                                            const int lane) {
   constexpr int NTT = (R0 + 7) / 8 + (R1 + 7) / 8;
   static_assert(NTT <= 4, "at most 4 n-tiles");
   for (int u = warp; u < 8 * NTT; u += nw)
-    oz_unit<N, T, K0, R0, K1, R1, SLOT1, YROW1, 0, IBF>(Xd, Yd, u >> 3, (u & 7) * 4, lane);
+    oz_unit<N, T, K0, R0, K1, R1, SLOT1, YROW1, 0, IBF, XST>(Xd, Yd, u >> 3, (u & 7) * 4, lane);
 }
+
+// Doubles per staged slot (and per output row) in the element kernel's shared memory: 32 cells x 4
+// variables plus 4 doubles of padding.  With 128 the four k-rows a fragment load touches (lanes
+// t = 0..3, rows 2t + ...) start on the same bank, so every half-warp's 64-bit load met a 4-way
+// bank conflict; a row offset of 132 doubles (8 banks) spreads them over all 32 banks.
+constexpr int kElemSlot = 132;
 
 // Whether the element kernel leaves the even/odd butterfly to the contraction's operands (IBF):
 // at N = 3, where each parity has one n-tile of outputs, it saves the 128 FP64 adds per cell of
@@ -291,7 +300,7 @@ constexpr bool oz_ibf(int N) { return N == 3; }
 template <int N, int NUe, int NUo, int NRe, int NRo, bool IBF>
 __device__ __forceinline__ void oz_contract(const double *Xd, double *Yd, const int warp, const int nw,
                                             const int lane) {
-  oz_product<N, 0, NUe, NRe, NUo, NRo, NUe, NRe, IBF>(Xd, Yd, warp, nw, lane);
+  oz_product<N, 0, NUe, NRe, NUo, NRo, NUe, NRe, IBF, kElemSlot>(Xd, Yd, warp, nw, lane);
 }
 
 // The dense form: Y rows 0..NP-1 (one per node) = A (NP x NK) applied to the NK slots in their
@@ -299,7 +308,7 @@ __device__ __forceinline__ void oz_contract(const double *Xd, double *Yd, const 
 template <int N, int NK, int NP>
 __device__ __forceinline__ void oz_contract_dense(const double *Xd, double *Yd, const int warp, const int nw,
                                                   const int lane) {
-  oz_product<N, 2, NK, NP, 0, 0, NK, NP>(Xd, Yd, warp, nw, lane);
+  oz_product<N, 2, NK, NP, 0, 0, NK, NP, false, kElemSlot>(Xd, Yd, warp, nw, lane);
 }
 
 // The adjoint element kernel's transposed contraction: columns 0..NUe-1 = S_e^T (even rows of the

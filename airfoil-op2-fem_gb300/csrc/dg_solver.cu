@@ -430,10 +430,11 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
   constexpr int Np = np_of(N), Nfp = N + 1, NK = nk_of(N);
   constexpr int NUe = Sym<N>::NUe, NUo = Sym<N>::NUo, NRe = Sym<N>::NRe;
   constexpr int NPin = NUo;  // input pairs
+  constexpr int kS2 = kElemSlot / 2;  // double2 per staged slot
   constexpr bool DENSE = ozd_used(N, TC);           // dense rows, slots in natural order
   constexpr bool SYMTC = !DENSE && oz_used(N, TC != 0);  // even/odd blocks on the tensor cores
   constexpr bool IBF = SYMTC && oz_ibf(N);  // the butterfly done in the contraction's operands
-  double2 *Y = X + NK * 32 * 2;
+  double2 *Y = X + NK * kS2;
   const int nthr = 32 * Np, tid = i * 32 + lane;
   const bool active = i < Np;
   const int e = e0 + lane;
@@ -469,10 +470,10 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
     }
     if (active) {
       const int pr = DENSE ? i : c_pos[N][i], ps = DENSE ? Np + i : c_pos[N][Np + i];
-      X[(pr * 32 + lane) * 2] = make_double2(fr0, fr1);
-      X[(pr * 32 + lane) * 2 + 1] = make_double2(fr2, fr3);
-      X[(ps * 32 + lane) * 2] = make_double2(fs0, fs1);
-      X[(ps * 32 + lane) * 2 + 1] = make_double2(fs2, fs3);
+      X[pr * kS2 + lane * 2] = make_double2(fr0, fr1);
+      X[pr * kS2 + lane * 2 + 1] = make_double2(fr2, fr3);
+      X[ps * kS2 + lane * 2] = make_double2(fs0, fs1);
+      X[ps * kS2 + lane * 2 + 1] = make_double2(fs2, fs3);
     }
   }
   // Everything above reads only W and the metrics (written before the face kernel ran); the face
@@ -488,8 +489,8 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
       b = ld2(fp + 2);
     }
     const int pf = DENSE ? 2 * Np + f : c_pos[N][2 * Np + f];
-    X[(pf * 32 + el) * 2] = a;
-    X[(pf * 32 + el) * 2 + 1] = b;
+    X[pf * kS2 + el * 2] = a;
+    X[pf * kS2 + el * 2 + 1] = b;
   }
   __syncthreads();
   if constexpr (!DENSE && !IBF) {
@@ -497,7 +498,7 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
     // the tensor-core contraction does it exactly in its operands instead)
     for (int j = active ? tid : NPin * 32; j < NPin * 32; j += nthr) {
       const int p = j >> 5, el = j & 31;
-      double2 *xa = X + (p * 32 + el) * 2, *xb = X + ((NUe + p) * 32 + el) * 2;
+      double2 *xa = X + p * kS2 + el * 2, *xb = X + (NUe + p) * kS2 + el * 2;
       const double2 a0 = xa[0], a1 = xa[1], b0 = xb[0], b1 = xb[1];
       xa[0] = make_double2(a0.x + b0.x, a0.y + b0.y);
       xa[1] = make_double2(a1.x + b1.x, a1.y + b1.y);
@@ -520,7 +521,7 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
 #pragma unroll
     for (int k = 0; k < NUe; k++) {
       const double c = opS<N>(i * NUe + k);
-      const double2 x01 = X[(k * 32 + lane) * 2], x23 = X[(k * 32 + lane) * 2 + 1];
+      const double2 x01 = X[k * kS2 + lane * 2], x23 = X[k * kS2 + lane * 2 + 1];
       r0 = fma(c, x01.x, r0);
       r1 = fma(c, x01.y, r1);
       r2 = fma(c, x23.x, r2);
@@ -530,7 +531,7 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
 #pragma unroll
     for (int k = 0; k < NUo; k++) {
       const double c = opS<N>(NRe * NUe + (i - NRe) * NUo + k);
-      const double2 x01 = X[((NUe + k) * 32 + lane) * 2], x23 = X[((NUe + k) * 32 + lane) * 2 + 1];
+      const double2 x01 = X[(NUe + k) * kS2 + lane * 2], x23 = X[(NUe + k) * kS2 + lane * 2 + 1];
       r0 = fma(c, x01.x, r0);
       r1 = fma(c, x01.y, r1);
       r2 = fma(c, x23.x, r2);
@@ -538,19 +539,19 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
     }
   }
   if (active && !DENSE && !SYMTC) {
-    Y[(i * 32 + lane) * 2] = make_double2(r0, r1);
-    Y[(i * 32 + lane) * 2 + 1] = make_double2(r2, r3);
+    Y[i * kS2 + lane * 2] = make_double2(r0, r1);
+    Y[i * kS2 + lane * 2 + 1] = make_double2(r2, r3);
   }
   __syncthreads();
   if (DENSE && active) {
-    const double2 y01 = Y[(i * 32 + lane) * 2], y23 = Y[(i * 32 + lane) * 2 + 1];
+    const double2 y01 = Y[i * kS2 + lane * 2], y23 = Y[i * kS2 + lane * 2 + 1];
     r0 = y01.x; r1 = y01.y; r2 = y23.x; r3 = y23.y;
   } else if (active) {
     const int re = c_out[N][3 * i], ro = c_out[N][3 * i + 1], sg = c_out[N][3 * i + 2];
-    const double2 e01 = Y[(re * 32 + lane) * 2], e23 = Y[(re * 32 + lane) * 2 + 1];
+    const double2 e01 = Y[re * kS2 + lane * 2], e23 = Y[re * kS2 + lane * 2 + 1];
     r0 = e01.x; r1 = e01.y; r2 = e23.x; r3 = e23.y;
     if (ro >= 0) {
-      const double2 o01 = Y[(ro * 32 + lane) * 2], o23 = Y[(ro * 32 + lane) * 2 + 1];
+      const double2 o01 = Y[ro * kS2 + lane * 2], o23 = Y[ro * kS2 + lane * 2 + 1];
       if (sg > 0) {
         r0 += o01.x; r1 += o01.y; r2 += o23.x; r3 += o23.y;
       } else {
@@ -571,6 +572,9 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
   // X and Y are rewritten by the next tile only after every warp is past this point
   __syncthreads();
 }
+
+// Dynamic shared memory of the even/odd element kernels: NK staged slots and Np output rows.
+constexpr size_t elem_sym_smem(int N) { return (size_t)(nk_of(N) + np_of(N)) * kElemSlot * sizeof(double); }
 
 // MB: minimum resident blocks per SM the register allocation must allow (oz_min_blocks for the
 // tensor-core form; at N = 3 without the bound it takes ~95 registers and runs two blocks per SM,
@@ -810,7 +814,7 @@ template <int N>
 static void launch_elem(const Inst &d, int stage, cudaStream_t s) {
   constexpr int Np = np_of(N), NK = nk_of(N);
   if (g_elem_variant) {
-    const size_t smem = (size_t)(NK + Np) * 32 * 4 * sizeof(double);
+    const size_t smem = elem_sym_smem(N);
     if constexpr (ozd_used(N, 2)) {
       if (g_elem_variant == 3) {
         launch_pdl(elem_kernel_sym<N, 2, oz_min_blocks(N)>, dim3((d.K + 31) / 32), dim3(32, Np), smem, s, d,
@@ -835,8 +839,8 @@ static void launch_elem(const Inst &d, int stage, cudaStream_t s) {
 // Element tiles [t0, t1) of one stage, in plain stream order on s (the even/odd forms only).
 template <int N>
 static void launch_elem_tiles(const Inst &d, int stage, int t0, int t1, cudaStream_t s) {
-  constexpr int Np = np_of(N), NK = nk_of(N);
-  const size_t smem = (size_t)(NK + Np) * 32 * 4 * sizeof(double);
+  constexpr int Np = np_of(N);
+  const size_t smem = elem_sym_smem(N);
   if constexpr (ozd_used(N, 2)) {
     if (g_elem_variant == 3) {
       elem_kernel_sym<N, 2, oz_min_blocks(N)><<<t1 - t0, dim3(32, Np), smem, s>>>(d, stage, t0);
@@ -863,7 +867,7 @@ static cudaError_t set_smem_attr() {
   const size_t smem = (size_t)nk_of(N) * 32 * 4 * sizeof(double);
   cudaError_t e = cudaFuncSetAttribute(elem_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  const size_t smem_sym = (size_t)(nk_of(N) + np_of(N)) * 32 * 4 * sizeof(double);
+  const size_t smem_sym = elem_sym_smem(N);
   e = cudaFuncSetAttribute(elem_kernel_sym<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_sym);
   if constexpr (oz_used(N, true)) {
     if (e == cudaSuccess)
