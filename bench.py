@@ -583,11 +583,11 @@ def main():
                      "traffic": traffic if dominant == "elem_kernel" else None,
                      "traffic_source": "ncu dram__bytes_read+write per launch, stage average (profiles/)",
                      "peak_source": "DFMA throughput measured live on this GPU (MEASURED_PEAKS.json has no FP64 figure)",
-                     "elem_form": {3: "even/odd, contraction on the bf16 tensor cores (exact integer product)",
+                     "elem_form": {3: "even/odd, contraction and butterfly on the bf16 tensor cores (exact integer product)",
                                    2: "even/odd, contraction on the bf16 tensor cores (exact integer product)",
                                    1: "even/odd, FP64", 0: "dense FP64"}[variant],
                      "frac_note": ("FP64-equivalent: algorithmic FP64 flops over the DFMA peak; the contraction "
-                                   "runs on the tensor cores, so frac can exceed 1 (FP64 pipe busy 70-74 % of "
+                                   "runs on the tensor cores, so frac can exceed 1 (FP64 pipe busy 45-50 % of "
                                    "active cycles per ncu)") if variant >= 2 else "FP64 flops over the DFMA peak",
                      "elem_ms_fp64_form": elem_ms_fp64,
                      "fp64_tensor_peak_tflops": dmma_gflops * 1e-3,
