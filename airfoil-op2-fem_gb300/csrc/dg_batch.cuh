@@ -273,7 +273,7 @@ struct Batch {
     if (variant < 0 || variant >= (int)vs.size()) { err = "bad variant"; return -1; }
     const BatchVariant &v = vs[variant];
     if (v.bs < 32 * maxNp) { err = "block too small for the batch's highest order"; return -1; }
-    const size_t smem = (size_t)(nk_of(maxN) + maxNp) * kElemSlot * sizeof(double);
+    const size_t smem = elem_sym_smem(maxN);
     cudaError_t ce = cudaFuncSetAttribute(v.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int per_sm = 0, dev = 0, sms = 0;
     if (ce == cudaSuccess) ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v.fn, v.bs, smem);

@@ -136,37 +136,38 @@ __device__ __forceinline__ long long oz_align(const unsigned long long b, const 
 // memory) so that only one k-step's magnitudes are live next to the seven accumulators.
 // XST: doubles from one slot (or output row) to the next in Xd and Yd (128 = 32 cells x 4
 // variables, plus any padding).
-// BF (the even/odd butterfly, done here in integers instead of on the staged doubles): 0 the
-// slot values as they are; 1 slot k plus slot PAIR0 + k for k < NPAIR, slot k alone above;
-// 2 slot k minus slot PAIR0 + k.  Both values are aligned to the largest exponent of all the
-// values read (as 55-bit integers, so that the exact sum or difference fits 56 bits), which makes
-// the butterfly exact and leaves no FP64 instruction in it.
-template <int T, int NORD, int K, int R, int SLOT0, int YROW0, int KST, int P, int NT, int BF = 0, int PAIR0 = 0,
-          int NPAIR = 0, int XST = 128>
+// PRE: the slots hold operands already aligned by oz_prep (sign in bit 63, magnitude below 2^56,
+// aligned to 2^(E-54)) and Ems[col] their column exponent E; otherwise the slots hold doubles,
+// aligned here to 2^(E-55).
+template <int T, int NORD, int K, int R, int SLOT0, int YROW0, int KST, int P, int NT, bool PRE = false,
+          int XST = 128>
 __device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *__restrict__ Yd, const int c0,
-                                        const int lane) {
+                                        const int lane, const int *__restrict__ Ems = nullptr) {
   static_assert(KST <= 2 && K <= 16 * KST && R > 8 * NT && NT < 4, "four n-tiles, two k-steps at most");
-  static_assert(BF == 0 || (SLOT0 == 0 && (BF == 1 ? NPAIR <= K : NPAIR == K)), "butterfly operands");
-  constexpr int SH = BF ? 2 : 3;  // alignment of a value below 2^56 (2^55 for butterfly operands)
+  constexpr int SH = PRE ? 2 : 3;  // the alignment shift (oz_align)
   const int g = lane >> 2, t = lane & 3;
   const int col = c0 * 4 + g;  // (cell, variable) of row g; row g + 8 is col + 8
   const uint32_t *Xw = reinterpret_cast<const uint32_t *>(Xd);
   // largest binary exponent of each of the two columns over all values read (high words only)
   int em[2] = {0, 0};
+  if constexpr (PRE) {
+    em[0] = Ems[col];
+    em[1] = Ems[col + 8];
+  } else {
 #pragma unroll
-  for (int ks = 0; ks < KST; ks++)
+    for (int ks = 0; ks < KST; ks++)
 #pragma unroll
-    for (int r = 0; r < 2; r++)
+      for (int r = 0; r < 2; r++)
 #pragma unroll
-      for (int q = 0; q < 4; q++) {
-        const int k = 16 * ks + 2 * t + (q & 1) + ((q >> 1) << 3);
-        if (k < K) em[r] = max(em[r], (int)((Xw[2 * ((SLOT0 + k) * XST + col + 8 * r) + 1] >> 20) & 0x7FF));
-        if (BF && k < NPAIR) em[r] = max(em[r], (int)((Xw[2 * ((PAIR0 + k) * XST + col + 8 * r) + 1] >> 20) & 0x7FF));
-      }
+        for (int q = 0; q < 4; q++) {
+          const int k = 16 * ks + 2 * t + (q & 1) + ((q >> 1) << 3);
+          if (k < K) em[r] = max(em[r], (int)((Xw[2 * ((SLOT0 + k) * XST + col + 8 * r) + 1] >> 20) & 0x7FF));
+        }
 #pragma unroll
-  for (int r = 0; r < 2; r++) {
-    em[r] = max(em[r], __shfl_xor_sync(0xffffffffu, em[r], 1));
-    em[r] = max(em[r], __shfl_xor_sync(0xffffffffu, em[r], 2));
+    for (int r = 0; r < 2; r++) {
+      em[r] = max(em[r], __shfl_xor_sync(0xffffffffu, em[r], 1));
+      em[r] = max(em[r], __shfl_xor_sync(0xffffffffu, em[r], 2));
+    }
   }
   const uint2 *bfr = &g_ozb[T][NORD][P][NT][0][0][lane];
   float acc[7][4];
@@ -175,9 +176,9 @@ __device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *_
 #pragma unroll
   for (int ks = 0; ks < KST; ks++) {
     // this k-step's values at slots 16 ks + {2t, 2t+1, 2t+8, 2t+9}: aligned magnitudes
-    // m = M 2^(e - E + SH) (M the 53-bit significand; for BF the exact integer sum or difference
-    // of two such values) and the sign pattern of every A-fragment register (pairs (g: q0 q1),
-    // (g+8: q0 q1), (g: q2 q3), (g+8: q2 q3))
+    // m = M 2^(e - E + SH) (M the 53-bit significand; with PRE oz_prep's integers) and the sign
+    // pattern of every A-fragment register (pairs (g: q0 q1), (g+8: q0 q1), (g: q2 q3),
+    // (g+8: q2 q3))
     // sgn[r + 2 (q >> 1)]: bit 15 the sign of value (r, q) for even q, bit 31 for odd q
     uint32_t hi[2][4], lo[2][4], sgn[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
@@ -186,18 +187,11 @@ __device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *_
       for (int q = 0; q < 4; q++) {
         const int k = 16 * ks + 2 * t + (q & 1) + ((q >> 1) << 3);
         const double x = k < K ? Xd[(SLOT0 + k) * XST + col + 8 * r] : 0.0;
-        unsigned long long b = (unsigned long long)__double_as_longlong(x);
-        if constexpr (BF != 0) {
-          const double y = k < NPAIR ? Xd[(PAIR0 + k) * XST + col + 8 * r] : 0.0;
-          const long long ma = oz_align<SH>(b, em[r]);
-          const long long mb = oz_align<SH>((unsigned long long)__double_as_longlong(y), em[r]);
-          const long long v = BF == 1 ? ma + mb : ma - mb;
-          b = (unsigned long long)v;
-        }
+        const unsigned long long b = (unsigned long long)__double_as_longlong(x);
         const uint32_t sbit = (uint32_t)(b >> 32) & 0x80000000u;
         sgn[r + 2 * (q >> 1)] |= (q & 1) ? sbit : (sbit >> 16);
         unsigned long long m;
-        if constexpr (BF != 0) m = (b >> 63) ? (unsigned long long)(-(long long)b) : b;
+        if constexpr (PRE) m = b & 0x00FFFFFFFFFFFFFFull;
         else m = (unsigned long long)oz_align<SH>(b & 0x7FFFFFFFFFFFFFFFull, em[r]);
         hi[r][q] = (uint32_t)(m >> 32);
         lo[r][q] = (uint32_t)m;
@@ -251,35 +245,68 @@ __device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *_
 
 // Parity 0: K0 staged slots from slot 0 to R0 outputs from row 0; parity 1: K1 slots from SLOT1
 // to R1 outputs from YROW1.  Work units: (parity, n-tile of 8 outputs, group of 4 cells); warp w
-// of nw takes units w, w + nw, ...  IBF: the slots hold the even/odd pairs unsplit (slot k and
-// slot K0 + k for k < K1, the K0 - K1 unpaired slots below K0) and the butterfly is done in the
-// operands (oz_tile's BF): parity 0 takes the sums, parity 1 the differences.
-template <int N, int T, int K0, int R0, int K1, int R1, int SLOT1, int YROW1, int NT, bool IBF, int XST>
-__device__ __forceinline__ void oz_unit(const double *Xd, double *Yd, const int w, const int c0, const int lane) {
+// of nw takes units w, w + nw, ...  PRE: the operands come from oz_prep (see oz_tile).
+template <int N, int T, int K0, int R0, int K1, int R1, int SLOT1, int YROW1, int NT, bool PRE, int XST>
+__device__ __forceinline__ void oz_unit(const double *Xd, double *Yd, const int w, const int c0, const int lane,
+                                        const int *Ems) {
   constexpr int NT0 = (R0 + 7) / 8;
   if constexpr (NT < 4) {
     if (w == NT) {
-      if constexpr (NT < NT0) {
-        if constexpr (IBF) oz_tile<T, N, K0, R0, 0, 0, (K0 + 15) / 16, 0, NT, 1, K0, K1, XST>(Xd, Yd, c0, lane);
-        else oz_tile<T, N, K0, R0, 0, 0, (K0 + 15) / 16, 0, NT, 0, 0, 0, XST>(Xd, Yd, c0, lane);
-      } else if constexpr (NT - NT0 < (R1 + 7) / 8) {
-        if constexpr (IBF)
-          oz_tile<T, N, K1, R1, 0, YROW1, (K1 + 15) / 16, 1, NT - NT0, 2, K0, K1, XST>(Xd, Yd, c0, lane);
-        else oz_tile<T, N, K1, R1, SLOT1, YROW1, (K1 + 15) / 16, 1, NT - NT0, 0, 0, 0, XST>(Xd, Yd, c0, lane);
-      }
+      if constexpr (NT < NT0)
+        oz_tile<T, N, K0, R0, 0, 0, (K0 + 15) / 16, 0, NT, PRE, XST>(Xd, Yd, c0, lane, Ems);
+      else if constexpr (NT - NT0 < (R1 + 7) / 8)
+        oz_tile<T, N, K1, R1, SLOT1, YROW1, (K1 + 15) / 16, 1, NT - NT0, PRE, XST>(Xd, Yd, c0, lane, Ems);
       return;
     }
-    oz_unit<N, T, K0, R0, K1, R1, SLOT1, YROW1, NT + 1, IBF, XST>(Xd, Yd, w, c0, lane);
+    oz_unit<N, T, K0, R0, K1, R1, SLOT1, YROW1, NT + 1, PRE, XST>(Xd, Yd, w, c0, lane, Ems);
   }
 }
 
-template <int N, int T, int K0, int R0, int K1, int R1, int SLOT1, int YROW1, bool IBF = false, int XST = 128>
+template <int N, int T, int K0, int R0, int K1, int R1, int SLOT1, int YROW1, bool PRE = false, int XST = 128>
 __device__ __forceinline__ void oz_product(const double *Xd, double *Yd, const int warp, const int nw,
-                                           const int lane) {
+                                           const int lane, const int *Ems = nullptr) {
   constexpr int NTT = (R0 + 7) / 8 + (R1 + 7) / 8;
   static_assert(NTT <= 4, "at most 4 n-tiles");
   for (int u = warp; u < 8 * NTT; u += nw)
-    oz_unit<N, T, K0, R0, K1, R1, SLOT1, YROW1, 0, IBF, XST>(Xd, Yd, u >> 3, (u & 7) * 4, lane);
+    oz_unit<N, T, K0, R0, K1, R1, SLOT1, YROW1, 0, PRE, XST>(Xd, Yd, u >> 3, (u & 7) * 4, lane, Ems);
+}
+
+// Sign and magnitude of an integer below 2^63 in one 64-bit word (sign in bit 63).
+__device__ __forceinline__ unsigned long long oz_signmag(const long long v) {
+  return v < 0 ? ((unsigned long long)(-v) | 0x8000000000000000ull) : (unsigned long long)v;
+}
+
+// The even/odd butterfly and the operand alignment of the element kernel's contraction, once per
+// staged value, by the first 256 threads of the block (two per column: the slot pairs are dealt
+// alternately, lanes l and l ^ 16 share a column).  Pairs k < NUo: slot k (x_a) and slot NUe + k
+// (x_b) become x_a + x_b and x_a - x_b; the unpaired slots NUo <= k < NUe stay single.  Every
+// value is aligned to the largest exponent E of its column's NK = NUe + NUo values as a 55-bit
+// integer (so that sums fit 56 bits), the sums and differences are exact, and each is stored as
+// sign and magnitude in its slot's 64 bits; Ems[column] = E (biased).
+template <int NUe, int NUo, int XST>
+__device__ __forceinline__ void oz_prep(double *Xd, int *Ems, const int tid) {
+  if (tid >= 256) return;
+  const int c = (tid & 15) | ((tid >> 5) << 4), h = (tid >> 4) & 1;
+  const uint32_t *Xw = reinterpret_cast<const uint32_t *>(Xd);
+  int e = 0;
+#pragma unroll
+  for (int k = h; k < NUe; k += 2) {
+    e = max(e, (int)((Xw[2 * (k * XST + c) + 1] >> 20) & 0x7FF));
+    if (k < NUo) e = max(e, (int)((Xw[2 * ((NUe + k) * XST + c) + 1] >> 20) & 0x7FF));
+  }
+  e = max(e, __shfl_xor_sync(0xffffffffu, e, 16));
+  if (h == 0) Ems[c] = e;
+#pragma unroll
+  for (int k = h; k < NUe; k += 2) {
+    const long long ma = oz_align<2>((unsigned long long)__double_as_longlong(Xd[k * XST + c]), e);
+    if (k < NUo) {
+      const long long mb = oz_align<2>((unsigned long long)__double_as_longlong(Xd[(NUe + k) * XST + c]), e);
+      Xd[k * XST + c] = __longlong_as_double((long long)oz_signmag(ma + mb));
+      Xd[(NUe + k) * XST + c] = __longlong_as_double((long long)oz_signmag(ma - mb));
+    } else {
+      Xd[k * XST + c] = __longlong_as_double((long long)oz_signmag(ma));
+    }
+  }
 }
 
 // Doubles per staged slot (and per output row) in the element kernel's shared memory: 32 cells x 4
@@ -288,19 +315,17 @@ __device__ __forceinline__ void oz_product(const double *Xd, double *Yd, const i
 // bank conflict; a row offset of 132 doubles (8 banks) spreads them over all 32 banks.
 constexpr int kElemSlot = 132;
 
-// Whether the element kernel leaves the even/odd butterfly to the contraction's operands (IBF):
-// at N = 3, where each parity has one n-tile of outputs, it saves the 128 FP64 adds per cell of
-// the butterfly (step 326 -> 322 us on the K=32768 O-grid); at N = 4, 5 every n-tile would redo
-// the doubled operand alignment, measured slower (501 -> 520 us, 765 -> 812 us).
-constexpr bool oz_ibf(int N) { return N == 3; }
-
-// The element kernel's contraction: Y rows 0..NRe-1 = S_e, Y rows NRe.. = S_o.  With IBF the
-// staged slots hold the pairs unsplit and the operands are x_a + x_b (and the unpaired slots) for
-// S_e, x_a - x_b for S_o; otherwise the slots hold the sums and differences already.
-template <int N, int NUe, int NUo, int NRe, int NRo, bool IBF>
+// The element kernel's contraction: Y rows 0..NRe-1 = S_e, Y rows NRe.. = S_o, on the operands
+// oz_prep made from the staged pairs (sums below slot NUe, differences from slot NUe on).  Earlier
+// forms, measured on the K=32768 O-grid: the FP64 butterfly on the staged doubles with each unit
+// aligning its values (steps 326 / 501 / 765 us at N = 3 / 4 / 5), and the butterfly formed in
+// each unit's operands (322 us at N = 3; slower at N = 4, 5, where every n-tile redid the doubled
+// alignment); oz_prep, once per value and spread over 256 threads, gives 294 / 446 / 652 us (with
+// the padded slots, 308.5 / 484 / 736 us before it).
+template <int N, int NUe, int NUo, int NRe, int NRo>
 __device__ __forceinline__ void oz_contract(const double *Xd, double *Yd, const int warp, const int nw,
-                                            const int lane) {
-  oz_product<N, 0, NUe, NRe, NUo, NRo, NUe, NRe, IBF, kElemSlot>(Xd, Yd, warp, nw, lane);
+                                            const int lane, const int *Ems) {
+  oz_product<N, 0, NUe, NRe, NUo, NRo, NUe, NRe, true, kElemSlot>(Xd, Yd, warp, nw, lane, Ems);
 }
 
 // The dense form: Y rows 0..NP-1 (one per node) = A (NP x NK) applied to the NK slots in their

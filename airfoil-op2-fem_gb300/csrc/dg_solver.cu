@@ -433,8 +433,8 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
   constexpr int kS2 = kElemSlot / 2;  // double2 per staged slot
   constexpr bool DENSE = ozd_used(N, TC);           // dense rows, slots in natural order
   constexpr bool SYMTC = !DENSE && oz_used(N, TC != 0);  // even/odd blocks on the tensor cores
-  constexpr bool IBF = SYMTC && oz_ibf(N);  // the butterfly done in the contraction's operands
   double2 *Y = X + NK * kS2;
+  int *Ems = reinterpret_cast<int *>(Y + Np * kS2);  // column exponents of the prepared operands
   const int nthr = 32 * Np, tid = i * 32 + lane;
   const bool active = i < Np;
   const int e = e0 + lane;
@@ -493,9 +493,13 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
     X[pf * kS2 + el * 2 + 1] = b;
   }
   __syncthreads();
-  if constexpr (!DENSE && !IBF) {
-    // butterfly over the input pairs: slot p <- x_a + x_b, slot NUe + p <- x_a - x_b (with IBF
-    // the tensor-core contraction does it exactly in its operands instead)
+  if constexpr (SYMTC) {
+    // the butterfly in integers and the operand alignment, once per value
+    oz_prep<NUe, NUo, kElemSlot>(reinterpret_cast<double *>(X), Ems, tid);
+    __syncthreads();
+  } else if constexpr (!DENSE) {
+    // butterfly over the input pairs: slot p <- x_a + x_b, slot NUe + p <- x_a - x_b (the
+    // tensor-core form does it exactly in integers instead)
     for (int j = active ? tid : NPin * 32; j < NPin * 32; j += nthr) {
       const int p = j >> 5, el = j & 31;
       double2 *xa = X + p * kS2 + el * 2, *xb = X + (NUe + p) * kS2 + el * 2;
@@ -514,8 +518,9 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
                                  (int)(blockDim.x * blockDim.y) >> 5, lane);
   } else if constexpr (SYMTC) {
     // the contraction on the tensor cores (dg_ozaki.cuh), every warp of the block taking part
-    oz_contract<N, NUe, NUo, NRe, Sym<N>::NRo, IBF>(reinterpret_cast<const double *>(X), reinterpret_cast<double *>(Y),
-                                               i, (int)(blockDim.x * blockDim.y) >> 5, lane);
+    oz_contract<N, NUe, NUo, NRe, Sym<N>::NRo>(reinterpret_cast<const double *>(X),
+                                                     reinterpret_cast<double *>(Y), i,
+                                                     (int)(blockDim.x * blockDim.y) >> 5, lane, Ems);
   } else if (!active) {
   } else if (i < NRe) {
 #pragma unroll
@@ -573,8 +578,11 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
   __syncthreads();
 }
 
-// Dynamic shared memory of the even/odd element kernels: NK staged slots and Np output rows.
-constexpr size_t elem_sym_smem(int N) { return (size_t)(nk_of(N) + np_of(N)) * kElemSlot * sizeof(double); }
+// Dynamic shared memory of the even/odd element kernels: NK staged slots, Np output rows and the
+// 128 column exponents of the prepared tensor-core operands.
+constexpr size_t elem_sym_smem(int N) {
+  return (size_t)(nk_of(N) + np_of(N)) * kElemSlot * sizeof(double) + 128 * sizeof(int);
+}
 
 // MB: minimum resident blocks per SM the register allocation must allow (oz_min_blocks for the
 // tensor-core form; at N = 3 without the bound it takes ~95 registers and runs two blocks per SM,
