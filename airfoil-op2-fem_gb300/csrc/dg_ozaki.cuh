@@ -89,25 +89,45 @@ __device__ __forceinline__ uint32_t oz_pack(const float f_lo, const float f_hi, 
 // bit length of T, at most 1997), so no subnormal or overflow case arises.  The result equals
 // RN(th 2^(32+sc) + tl 2^sc), the sum of the two exact parts rounded once.
 __device__ __forceinline__ double oz_round(const long long th, const long long tl, const int sc) {
-  const __int128 T = (__int128)th * 4294967296LL + (__int128)tl;
-  const unsigned long long sign = T < 0 ? 0x8000000000000000ull : 0ull;
-  const unsigned __int128 mag = (unsigned __int128)(T < 0 ? -T : T);
-  const unsigned long long hi = (unsigned long long)(mag >> 64), lo = (unsigned long long)mag;
-  if ((hi | lo) == 0ull) return 0.0;
-  const int nb = hi ? 128 - __clzll((long long)hi) : 64 - __clzll((long long)lo);  // bit length
+  // T = H 2^32 + L with 0 <= L < 2^32, then |T| = MH 2^32 + ML (MH < 2^42, ML < 2^32)
+  const long long H = th + (tl >> 32);
+  const unsigned long long L = (unsigned long long)tl & 0xFFFFFFFFull;
+  const unsigned long long sign = H < 0 ? 0x8000000000000000ull : 0ull;
+  unsigned long long MH, ML;
+  if (H < 0) {
+    MH = (unsigned long long)(-H) - (L ? 1ull : 0ull);
+    ML = L ? 0x100000000ull - L : 0ull;
+  } else {
+    MH = (unsigned long long)H;
+    ML = L;
+  }
+  // the leading bits in one 64-bit word S = |T| / 2^off; below 2^63 exactly (off = 0), else the
+  // 10 dropped bits of ML only decide ties (sticky)
+  unsigned long long S;
+  int off;
+  bool sticky;
+  if (MH >> 31) {
+    S = (MH << 22) | (ML >> 10);
+    off = 10;
+    sticky = (ML & 0x3FFull) != 0ull;
+  } else {
+    S = (MH << 32) | ML;
+    off = 0;
+    sticky = false;
+  }
+  if (S == 0ull) return 0.0;
+  const int nb = 64 - __clzll((long long)S);  // bit length of S
   unsigned long long q;  // significand, 2^52 <= q < 2^53
   int e2;                // value = q 2^(e2 + sc)
-  if (nb <= 53) {
-    q = lo << (53 - nb);
+  if (nb <= 53) {        // (off = 0 here: S >= 2^53 otherwise)
+    q = S << (53 - nb);
     e2 = nb - 53;
   } else {
     const int sh = nb - 53;
-    const unsigned __int128 qq = mag >> sh;
-    const unsigned __int128 rem = mag - (qq << sh);
-    const unsigned __int128 half = (unsigned __int128)1 << (sh - 1);
-    q = (unsigned long long)qq;
-    if (rem > half || (rem == half && (q & 1ull))) q++;
-    e2 = sh;
+    q = S >> sh;
+    const unsigned long long rem = S & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+    if (rem > half || (rem == half && (sticky || (q & 1ull)))) q++;
+    e2 = sh + off;
     if (q >> 53) {  // rounded up to 2^53
       q >>= 1;
       e2++;

@@ -596,7 +596,11 @@ __global__ void __launch_bounds__(32 * np_of(N), MB) elem_kernel_sym(const Inst 
 }
 
 // ---------------------------------------------------------------- per-step finalize
+// Launched with programmatic dependent launch in the step graph: it waits for the last element
+// kernel (whose dt maximum it reads) and lets the next step's face kernel be scheduled meanwhile.
 __global__ void finalize_kernel(StepState *st, int dt_mode, double *dt_hist, unsigned long long dt_hist_len) {
+  pdl_wait();
+  pdl_trigger();
   if (threadIdx.x | blockIdx.x) return;
   if (dt_hist && st->step < dt_hist_len) dt_hist[st->step] = st->dt;
   st->t += st->dt;
@@ -1219,7 +1223,7 @@ int Solver::set_dt_from_max(std::string &err) {
 
 void Solver::enqueue_step(cudaStream_t s) {
   DG_DISPATCH(cfg.N, (launch_stage<NN>(d, 0, s), launch_stage<NN>(d, 1, s), launch_stage<NN>(d, 2, s)));
-  finalize_kernel<<<1, 32, 0, s>>>(d.st, d.dt_mode, d.dt_hist, d.dt_hist_len);
+  launch_pdl(finalize_kernel, dim3(1), dim3(32), 0, s, d.st, d.dt_mode, d.dt_hist, d.dt_hist_len);
 }
 
 // One step with an event recorded after each of its seven kernels (ev[0] is recorded by the
@@ -1280,7 +1284,7 @@ int Solver::step_io(const double *q_in, double *q_out, std::string &err) {
   DG_DISPATCH(N, (launch_stage<NN>(d, 1, stream), launch_face<NN>(d, 2, stream)));
   if (!q_out) {
     DG_DISPATCH(N, launch_elem<NN>(d, 2, stream));
-    finalize_kernel<<<1, 32, 0, stream>>>(d.st, d.dt_mode, d.dt_hist, d.dt_hist_len);
+    launch_pdl(finalize_kernel, dim3(1), dim3(32), 0, stream, d.st, d.dt_mode, d.dt_hist, d.dt_hist_len);
     CK(cudaGetLastError());
     return 0;
   }
