@@ -295,11 +295,11 @@ def test_tensor_core_contraction_wide_range(pkg, omesh, N):
     assert np.abs(r2 - r1).max() <= 1e-11 * np.abs(r1).max()
 
 
-@pytest.mark.parametrize("N", [2, 3])
+@pytest.mark.parametrize("N", [2, 3, 4, 5])
 def test_tensor_core_contraction_nonfinite(pkg, omesh, N):
     """A non-finite value in a cell's staged column gives NaN there, as the FP64 contraction
     does, and leaves the cells it does not reach finite (the dense rows at N = 2, the even/odd
-    blocks at N = 3)."""
+    blocks with their integer-prepared operands at N = 3, 4, 5)."""
     m = omesh.naca_ogrid(32, 8, farfield="characteristic")
     s = pkg.Solver(pkg.Mesh.from_tables(m), pkg.config(N=N, cfl=0.5)).init()
     q = s.get("q")
