@@ -469,8 +469,8 @@ __global__ void __launch_bounds__(256) adj_face_kernel(const Inst d, const doubl
     qp[0] = c.x; qp[1] = c.y; qp[2] = dd.x; qp[3] = dd.y;
     const double *gl = d.geo + (size_t)cL * 16 + 4 + 3 * fL;
     const double nx = gl[0], ny = gl[1];
-    const double sL = 0.5 * gl[2];
-    const double sR = -0.5 * d.geo[(size_t)cR * 16 + 4 + 3 * fR + 2];
+    const double sL = gl[2];
+    const double sR = -d.geo[(size_t)cR * 16 + 4 + 3 * fR + 2];
     const size_t sl = (((size_t)cL * 3 + fL) * Nfp + i) * 4, sr = (((size_t)cR * 3 + fR) * Nfp + iR) * 4;
     const double2 la = ld2(fluxbar + sl), lb = ld2(fluxbar + sl + 2);
     const double2 ra = ld2(fluxbar + sr), rb = ld2(fluxbar + sr + 2);
@@ -492,7 +492,7 @@ __global__ void __launch_bounds__(256) adj_face_kernel(const Inst d, const doubl
     double2 a = ld2(w), bb = ld2(w + 2);
     qm[0] = a.x; qm[1] = a.y; qm[2] = bb.x; qm[3] = bb.y;
     const double *g = d.geo + (size_t)c * 16 + 4 + 3 * f;
-    const double nx = g[0], ny = g[1], s = 0.5 * g[2];
+    const double nx = g[0], ny = g[1], s = g[2];
     const size_t sl = (((size_t)c * 3 + f) * Nfp + i) * 4;
     const double2 la = ld2(fluxbar + sl), lb = ld2(fluxbar + sl + 2);
     fb[0] = s * la.x; fb[1] = s * la.y; fb[2] = s * lb.x; fb[3] = s * lb.y;

@@ -1,5 +1,5 @@
 // Scalar advection app (advec/src/advec.cpp:171-262) on the device.  Included at the end of
-// dg_solver.cu: it shares the per-order operators [Drw | Dsw | -LIFT] in constant memory, the
+// dg_solver.cu: it shares the per-order operators [Drw | Dsw | -LIFT/2] in constant memory, the
 // reference-node coordinates, the affine geometry kernel and the edge records of the Euler path.
 //
 // One classical RK4 stage is two kernels:
@@ -7,7 +7,8 @@
 //                      n.(F- + F+)/2 + |v|(q- - q+)/2 of advec/src/advec_rhs.h:36-63 once per
 //                      face node, with the trace of the neighbour (advec/src/get_neighbour_q.h)
 //                      or the constant ghost value 4.5e-5 (advec/src/get_bedge_q.h), written
-//                      into both cells' face slots scaled by each side's fscale;
+//                      into both cells' face slots scaled by each side's fscale (twice the flux:
+//                      the 1/2 is in the operator's LIFT columns);
 //   advec_elem_kernel  32 cells x Np node-warps (even/odd form by default, advec_elem_kernel_sym):
 //                      rhs = cr Drw q + cs Dsw q - LIFT flux with
 //                      cr = vx rx + vy ry, cs = vx sx + vy sy (F = vx q, G = vy q on affine
@@ -41,8 +42,8 @@ __global__ void __launch_bounds__(256) advec_face_kernel(const AdvInst d) {
     const double *gl = d.geo + (size_t)cL * 16 + 4 + 3 * fL;
     const double nx = __ldg(gl), ny = __ldg(gl + 1);
     const double f = nx * (vx * qm + vx * qp) + ny * (vy * qm + vy * qp) + a * (qm - qp);
-    d.flux[((size_t)cL * 3 + fL) * Nfp + i] = (0.5 * __ldg(gl + 2)) * f;
-    d.flux[((size_t)cR * 3 + fR) * Nfp + iR] = (-0.5 * __ldg(d.geo + (size_t)cR * 16 + 6 + 3 * fR)) * f;
+    d.flux[((size_t)cL * 3 + fL) * Nfp + i] = __ldg(gl + 2) * f;
+    d.flux[((size_t)cR * 3 + fR) * Nfp + iR] = -__ldg(d.geo + (size_t)cR * 16 + 6 + 3 * fR) * f;
   } else {
     const int b = tid / Nfp, i = tid - b * Nfp;
     const int4 bd = __ldg(&d.bedges[b]);
@@ -51,7 +52,7 @@ __global__ void __launch_bounds__(256) advec_face_kernel(const AdvInst d) {
     const double *g = d.geo + (size_t)c * 16 + 4 + 3 * fc;
     const double nx = __ldg(g), ny = __ldg(g + 1);
     const double f = nx * (vx * qm + vx * qp) + ny * (vy * qm + vy * qp) + a * (qm - qp);
-    d.flux[((size_t)c * 3 + fc) * Nfp + i] = (0.5 * __ldg(g + 2)) * f;
+    d.flux[((size_t)c * 3 + fc) * Nfp + i] = __ldg(g + 2) * f;
   }
 }
 

@@ -4,10 +4,11 @@
 //   face_kernel  one thread per face node of every interior and boundary edge: gathers both
 //                traces (src/get_neighbour_q.h), builds the boundary ghost state
 //                (src/get_bedge_q.h), evaluates the Roe flux once per face node
-//                (src/euler_rhs.h:120-220) and writes it, scaled by each side's fscale, into
-//                both cells' face slots.  Each slot has exactly one writer: no atomics.
+//                (src/euler_rhs.h:120-220) and writes twice it (the 1/2 is in the LIFT
+//                columns), scaled by each side's fscale, into both cells' face slots.  Each
+//                slot has exactly one writer: no atomics.
 //   elem_kernel  32 cells x Np node-warps per block: nodal Euler fluxes combined with the
-//                (affine, per-cell) metric terms, one contraction of [Drw | Dsw | -LIFT]
+//                (affine, per-cell) metric terms, one contraction of [Drw | Dsw | -LIFT/2]
 //                (operators in constant memory, warp-uniform rows) against
 //                [Fr ; Fs ; flux] staged in shared memory (src/euler_rhs.h:226-247,284-286),
 //                then the SSPRK3 stage combine in registers (src/set_workingQ.h,
@@ -148,8 +149,8 @@ __device__ __forceinline__ void face_node(const Inst &d, const int stage, const 
     qp[0] = c.x; qp[1] = c.y; qp[2] = dd.x; qp[3] = dd.y;
     const double *gl = d.geo + (size_t)cL * 16 + 4 + 3 * fL;
     const double nx = __ldg(gl), ny = __ldg(gl + 1);
-    const double sL = 0.5 * __ldg(gl + 2);
-    const double sR = -0.5 * __ldg(d.geo + (size_t)cR * 16 + 4 + 3 * fR + 2);
+    const double sL = __ldg(gl + 2);
+    const double sR = -__ldg(d.geo + (size_t)cR * 16 + 4 + 3 * fR + 2);
     roe_flux2(qm, qp, nx, ny, P, f2);
     double *ol = d.flux + (((size_t)cL * 3 + fL) * Nfp + i) * 4;
     double *orr = d.flux + (((size_t)cR * 3 + fR) * Nfp + iR) * 4;
@@ -166,7 +167,7 @@ __device__ __forceinline__ void face_node(const Inst &d, const int stage, const 
     double2 a = ld2(w), bb = ld2(w + 2);
     qm[0] = a.x; qm[1] = a.y; qm[2] = bb.x; qm[3] = bb.y;
     const double *g = d.geo + (size_t)c * 16 + 4 + 3 * f;
-    const double nx = __ldg(g), ny = __ldg(g + 1), s = 0.5 * __ldg(g + 2);
+    const double nx = __ldg(g), ny = __ldg(g + 1), s = __ldg(g + 2);
     if (d.app == 1) {
       const double frac = stage == 0 ? 0.0 : (stage == 1 ? 1.0 : 0.5);
       const double tst = d.st->t + frac * d.st->dt;
@@ -997,7 +998,9 @@ static int sym_tables(const Operators &o, const std::vector<double> &A, std::str
   return oz_upload(N, t.S, t.NUe, t.NUo, t.NRe, t.NRo, A, o.Np, 2 * o.Np + 3 * o.Nfp, err);
 }
 
-// Dense rows [Drw | Dsw | -LIFT] of order N.
+// Dense rows [Drw | Dsw | -LIFT/2] of order N.  The 1/2 of the reference's flux
+// (src/euler_rhs.h:217, the average of the two sides' fluxes) is taken here, exactly (a power of
+// two), instead of in every face kernel: the face kernels store fscale * (F_L + F_R - dissipation).
 static void dense_rows(const Operators &o, std::vector<double> &A) {
   const int Np = o.Np, Nfp = o.Nfp, NK = 2 * Np + 3 * Nfp;
   A.assign((size_t)Np * NK, 0.0);
@@ -1006,7 +1009,7 @@ static void dense_rows(const Operators &o, std::vector<double> &A) {
       A[(size_t)i * NK + k] = o.Drw[(size_t)i * Np + k];
       A[(size_t)i * NK + Np + k] = o.Dsw[(size_t)i * Np + k];
     }
-    for (int k = 0; k < 3 * Nfp; k++) A[(size_t)i * NK + 2 * Np + k] = -o.LIFT[(size_t)i * 3 * Nfp + k];
+    for (int k = 0; k < 3 * Nfp; k++) A[(size_t)i * NK + 2 * Np + k] = -0.5 * o.LIFT[(size_t)i * 3 * Nfp + k];
   }
 }
 

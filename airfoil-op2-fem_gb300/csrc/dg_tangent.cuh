@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(256) tlm_face_kernel(const Inst d, const doubl
     tl::load_dual(d.W + oL, dW + oL, qm);
     tl::load_dual(d.W + oR, dW + oR, qp);
     const double *gl = d.geo + (size_t)cL * 16 + 4 + 3 * fL;
-    const double sL = 0.5 * gl[2], sR = -0.5 * d.geo[(size_t)cR * 16 + 6 + 3 * fR];
+    const double sL = gl[2], sR = -d.geo[(size_t)cR * 16 + 6 + 3 * fR];
     tl::roe_flux2_t(qm, qp, gl[0], gl[1], P, f2);
     double *ol = dflux + (((size_t)cL * 3 + fL) * Nfp + i) * 4, *orr = dflux + (((size_t)cR * 3 + fR) * Nfp + iR) * 4;
     for (int k = 0; k < 4; k++) {
@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(256) tlm_face_kernel(const Inst d, const doubl
     const size_t o = ((size_t)c * Np + d.fmask[f * Nfp + i]) * 4;
     tl::load_dual(d.W + o, dW + o, qm);
     const double *g = d.geo + (size_t)c * 16 + 4 + 3 * f;
-    const double nx = g[0], ny = g[1], s = 0.5 * g[2];
+    const double nx = g[0], ny = g[1], s = g[2];
     if (d.app == 1) {
       const double *xy = d.bxy + ((size_t)b * Nfp + i) * 2;
       double v[4], dv[4];
