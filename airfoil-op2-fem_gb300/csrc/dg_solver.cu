@@ -127,8 +127,12 @@ __device__ __forceinline__ void st2(double *p, double a, double b) {
 #include "dg_ozaki.cuh"
 
 // ---------------------------------------------------------------- face kernel
-// One face node (tid in [0, (nB + nE) * Nfp)): boundary face nodes come first.
-template <int N>
+// One face node (tid in [0, (nB + nE) * Nfp)): boundary face nodes come first.  PDL: the kernel
+// was launched with programmatic dependent launch; the edge records, node indices and face
+// geometry (fixed for the run) are loaded before waiting for the previous kernel, W and the step
+// state after.  Only after that wait may the next kernel be scheduled: the element kernel reads
+// W before its own wait, so it must not start while the previous element kernel still writes W.
+template <int N, bool PDL = false>
 __device__ __forceinline__ void face_node(const Inst &d, const int stage, const int tid) {
   constexpr int Np = np_of(N), Nfp = N + 1;
   // Boundary face nodes come first: their ghost states (characteristic farfield, vortex exp) cost
@@ -142,15 +146,19 @@ __device__ __forceinline__ void face_node(const Inst &d, const int stage, const 
     const int cL = ed.x, cR = ed.y, fL = ed.z & 3, fR = (ed.z >> 2) & 3;
     const int iR = (ed.z >> 4) ? Nfp - 1 - i : i;
     const int nodeL = __ldg(&d.fmask[fL * Nfp + i]), nodeR = __ldg(&d.fmask[fR * Nfp + iR]);
+    const double *gl = d.geo + (size_t)cL * 16 + 4 + 3 * fL;
+    const double nx = __ldg(gl), ny = __ldg(gl + 1);
+    const double sL = __ldg(gl + 2);
+    const double sR = -__ldg(d.geo + (size_t)cR * 16 + 4 + 3 * fR + 2);
+    if constexpr (PDL) {
+      pdl_wait();
+      pdl_trigger();
+    }
     const double *wl = d.W + ((size_t)cL * Np + nodeL) * 4;
     const double *wr = d.W + ((size_t)cR * Np + nodeR) * 4;
     double2 a = ld2(wl), b = ld2(wl + 2), c = ld2(wr), dd = ld2(wr + 2);
     qm[0] = a.x; qm[1] = a.y; qm[2] = b.x; qm[3] = b.y;
     qp[0] = c.x; qp[1] = c.y; qp[2] = dd.x; qp[3] = dd.y;
-    const double *gl = d.geo + (size_t)cL * 16 + 4 + 3 * fL;
-    const double nx = __ldg(gl), ny = __ldg(gl + 1);
-    const double sL = __ldg(gl + 2);
-    const double sR = -__ldg(d.geo + (size_t)cR * 16 + 4 + 3 * fR + 2);
     roe_flux2(qm, qp, nx, ny, P, f2);
     double *ol = d.flux + (((size_t)cL * 3 + fL) * Nfp + i) * 4;
     double *orr = d.flux + (((size_t)cR * 3 + fR) * Nfp + iR) * 4;
@@ -163,11 +171,15 @@ __device__ __forceinline__ void face_node(const Inst &d, const int stage, const 
     const int4 bd = __ldg(&d.bedges[b]);
     const int c = bd.x, f = bd.y, type = bd.z;
     const int node = __ldg(&d.fmask[f * Nfp + i]);
+    const double *g = d.geo + (size_t)c * 16 + 4 + 3 * f;
+    const double nx = __ldg(g), ny = __ldg(g + 1), s = __ldg(g + 2);
+    if constexpr (PDL) {
+      pdl_wait();
+      pdl_trigger();
+    }
     const double *w = d.W + ((size_t)c * Np + node) * 4;
     double2 a = ld2(w), bb = ld2(w + 2);
     qm[0] = a.x; qm[1] = a.y; qm[2] = bb.x; qm[3] = bb.y;
-    const double *g = d.geo + (size_t)c * 16 + 4 + 3 * f;
-    const double nx = __ldg(g), ny = __ldg(g + 1), s = __ldg(g + 2);
     if (d.app == 1) {
       const double frac = stage == 0 ? 0.0 : (stage == 1 ? 1.0 : 0.5);
       const double tst = d.st->t + frac * d.st->dt;
@@ -185,11 +197,11 @@ __device__ __forceinline__ void face_node(const Inst &d, const int stage, const 
 
 template <int N>
 __global__ void __launch_bounds__(256) face_kernel(const Inst d, const int stage) {
-  pdl_wait();     // W (and the step state) of the previous kernel
-  pdl_trigger();  // the element kernel may start its face-independent part
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   if (tid >= (d.nE + d.nB) * (N + 1)) return;
-  face_node<N>(d, stage, tid);
+  // waits for W (and the step state) of the previous kernel, then lets the element kernel start
+  // its face-independent part
+  face_node<N, true>(d, stage, tid);
 }
 
 // double -> float by truncation of the bit pattern, with integer instructions only (the
