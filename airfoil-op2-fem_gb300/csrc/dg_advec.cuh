@@ -201,6 +201,84 @@ __global__ void __launch_bounds__(32 * np_of(N)) advec_elem_kernel_sym(const Adv
   }
 }
 
+// The element kernel with the even/odd contraction on the bf16 tensor cores (the exact integer
+// product of dg_ozaki.cuh): one variable per column, so a 32-cell tile is two row tiles of 16
+// cells and the units are (row tile, n-tile of outputs).  Staging, butterfly and alignment
+// (oz_prep over 64 threads), the contraction, the recombination and the RK4 combine follow
+// advec_elem_kernel_sym; the right-hand side equals it to rounding.  Used at N = 3 (K = 524288:
+// 0.304 -> 0.254 ms per stage, step 1.45 -> 1.20 ms); at N = 4, 5 a tile has only 6 or 8
+// contraction units for 15 or 21 warps and measured slower than the FP64 kernel (0.562 vs 0.537,
+// 0.931 vs 0.885 ms per stage), so those orders keep it.
+constexpr bool advec_tc(int N) { return N == 3; }
+template <int N>
+__global__ void __launch_bounds__(32 * np_of(N), oz_min_blocks(N)) advec_elem_kernel_tc(const AdvInst d,
+                                                                                         const int stage) {
+  constexpr int Np = np_of(N), NF = 3 * (N + 1), NK = nk_of(N);
+  constexpr int NUe = Sym<N>::NUe, NUo = Sym<N>::NUo, NRe = Sym<N>::NRe, NRo = Sym<N>::NRo;
+  // 32 cells + 4 doubles of padding per slot: the fragment loads' four k-rows fall on different banks
+  constexpr int XS = 36;
+  constexpr int NTT = (NRe + 7) / 8 + (NRo + 7) / 8;  // n-tiles of outputs
+  __shared__ __align__(16) double X[NK * XS];  // [slot][cell]
+  __shared__ __align__(16) double Y[Np * XS];  // even / odd row results [row][cell]
+  __shared__ double R[32 * Np];                // right-hand sides [cell][node]
+  __shared__ int Ems[32];                      // column exponents of the prepared operands
+  const int t = threadIdx.x;
+  const int e0 = blockIdx.x * 32;
+  const int nc = min(32, d.K - e0);
+  const size_t base = (size_t)e0 * Np;
+  {
+    const int el = t / Np, k = t - el * Np;
+    double cr = 0.0, cs = 0.0, w = 0.0;
+    if (el < nc) {
+      const double *g = d.geo + (size_t)(e0 + el) * 16;
+      cr = d.vx * g[0] + d.vy * g[1];
+      cs = d.vx * g[2] + d.vy * g[3];
+      w = d.W[base + t];
+    }
+    X[c_pos[N][k] * XS + el] = cr * w;
+    X[c_pos[N][Np + k] * XS + el] = cs * w;
+    for (int j = t; j < 32 * NF; j += 32 * Np) {
+      const int ef = j / NF, f = j - ef * NF;
+      X[c_pos[N][2 * Np + f] * XS + ef] = ef < nc ? d.flux[(size_t)e0 * NF + j] : 0.0;
+    }
+  }
+  __syncthreads();
+  oz_prep<NUe, NUo, XS, 32>(X, Ems, t);
+  __syncthreads();
+  const int lane = t & 31, i = t >> 5;
+  // unit u: n-tile u >> 1 of the outputs (even rows first), cells 16 (u & 1) .. + 15
+  for (int u = i; u < 2 * NTT; u += Np)
+    oz_unit<N, 0, NUe, NRe, NUo, NRo, NUe, NRe, 0, true, XS>(X, Y, u >> 1, (u & 1) * 4, lane, Ems);
+  __syncthreads();
+  {
+    const int re = c_out[N][3 * i], ro = c_out[N][3 * i + 1], sg = c_out[N][3 * i + 2];
+    double r = Y[re * XS + lane];
+    if (ro >= 0) r = sg > 0 ? r + Y[ro * XS + lane] : r - Y[ro * XS + lane];
+    R[lane * Np + i] = r;
+  }
+  __syncthreads();
+  const int el = t / Np;
+  if (el >= nc) return;
+  const size_t o = base + t;
+  const double r = R[t];
+  if (stage == 4) {
+    d.rhs_out[o] = r;
+    return;
+  }
+  const double q = d.q[o], dt = d.dt;
+  if (stage == 0) {
+    d.acc[o] = r;
+    d.W[o] = __dadd_rn(q, __dmul_rn(dt * 0.5, r));
+  } else if (stage < 3) {
+    d.acc[o] = __dadd_rn(d.acc[o], 2.0 * r);
+    d.W[o] = __dadd_rn(q, __dmul_rn(stage == 1 ? dt * 0.5 : dt, r));
+  } else {
+    const double qn = __dadd_rn(q, __dmul_rn((1.0 / 6.0) * dt, __dadd_rn(d.acc[o], r)));
+    d.q[o] = qn;
+    d.W[o] = qn;
+  }
+}
+
 // advec/src/set_ic.h:3-10 at the node positions of src/init_grid.h.
 template <int N>
 __global__ void advec_ic_kernel(const AdvInst d, const double *coords, const int *cells) {
@@ -231,8 +309,16 @@ __global__ void advec_vertex_kernel(int K, const int *cells, const int *owner, c
   }
 }
 
+// Element-kernel forms 2 and 3 use the tensor-core contraction where advec_tc says, form 1 (and
+// forms 2, 3 at the other orders) the even/odd FP64 kernel, form 0 the dense FP64 kernel.
 template <int N>
 static void advec_launch_elem(const AdvInst &d, int stage, cudaStream_t s) {
+  if constexpr (advec_tc(N)) {
+    if (g_elem_variant >= 2) {
+      advec_elem_kernel_tc<N><<<(d.K + 31) / 32, 32 * np_of(N), 0, s>>>(d, stage);
+      return;
+    }
+  }
   if (g_elem_variant) advec_elem_kernel_sym<N><<<(d.K + 31) / 32, 32 * np_of(N), 0, s>>>(d, stage);
   else advec_elem_kernel<N><<<(d.K + 31) / 32, 32 * np_of(N), 0, s>>>(d, stage);
 }

@@ -297,15 +297,16 @@ __device__ __forceinline__ unsigned long long oz_signmag(const long long v) {
 }
 
 // The even/odd butterfly and the operand alignment of the element kernel's contraction, once per
-// staged value, by the first 256 threads of the block (two per column: the slot pairs are dealt
-// alternately, lanes l and l ^ 16 share a column).  Pairs k < NUo: slot k (x_a) and slot NUe + k
+// staged value, by the first 2 NC threads of the block (two per column of the NC: the slot pairs
+// are dealt alternately, lanes l and l ^ 16 share a column).  Pairs k < NUo: slot k (x_a) and slot NUe + k
 // (x_b) become x_a + x_b and x_a - x_b; the unpaired slots NUo <= k < NUe stay single.  Every
 // value is aligned to the largest exponent E of its column's NK = NUe + NUo values as a 55-bit
 // integer (so that sums fit 56 bits), the sums and differences are exact, and each is stored as
 // sign and magnitude in its slot's 64 bits; Ems[column] = E (biased).
-template <int NUe, int NUo, int XST>
+template <int NUe, int NUo, int XST, int NC = 128>
 __device__ __forceinline__ void oz_prep(double *Xd, int *Ems, const int tid) {
-  if (tid >= 256) return;
+  static_assert(NC % 16 == 0, "columns in groups of 16");
+  if (tid >= 2 * NC) return;
   const int c = (tid & 15) | ((tid >> 5) << 4), h = (tid >> 4) & 1;
   const uint32_t *Xw = reinterpret_cast<const uint32_t *>(Xd);
   int e = 0;

@@ -162,11 +162,13 @@ def test_device_vertex_values_and_vtk(pkg, orc, omesh, tmp_path):
 @pytest.mark.gpu
 @pytest.mark.parametrize("N", [1, 2, 3, 4, 5, 6])
 def test_device_even_odd_equals_dense(pkg, orc, omesh, N):
-    """The even/odd element kernel (default) and the dense one: same RHS and steps."""
+    """The element-kernel forms: dense FP64 (0), even/odd FP64 (1) and the default (3: the
+    even/odd contraction on the tensor cores at N = 3, form 1 at the other orders) give the same
+    RHS and steps."""
     m = omesh.vortex_square(12, 0.0, 1.0)
     out = []
     prev = pkg.lib().dg_elem_variant()
-    for variant in (0, 1):
+    for variant in (0, 1, 3):
         pkg.lib().dg_set_elem_variant(variant)
         try:
             a = pkg.Advection(pkg.Mesh.from_tables(m), N=N, vel_x=0.9, vel_y=-0.4).init()
@@ -178,5 +180,10 @@ def test_device_even_odd_equals_dense(pkg, orc, omesh, N):
             out.append((r, a.get("q")))
         finally:
             pkg.lib().dg_set_elem_variant(prev)
-    assert orc.rel_l2(out[1][0], out[0][0]) < 1e-13
-    assert orc.rel_l2(out[1][1], out[0][1]) < 1e-13
+    for k in (1, 2):
+        assert orc.rel_l2(out[k][0], out[0][0]) < 1e-13
+        assert orc.rel_l2(out[k][1], out[0][1]) < 1e-13
+    if N == 3:
+        assert not np.array_equal(out[2][0], out[1][0])  # the tensor-core kernel ran
+    else:
+        assert np.array_equal(out[2][0], out[1][0])
