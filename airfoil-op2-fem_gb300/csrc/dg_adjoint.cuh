@@ -37,8 +37,7 @@ __constant__ int c_fpt[7][28 * 2]; // face points k with FMASK[k] == node (up to
 
 // ---------------------------------------------------------------- reverse of roe_flux2
 // Adds to qmb, qpb the adjoints of qm, qp given fb, the adjoint of roe_flux2's output f2.  The
-// forward sweep writes the Roe averages with the weights sqrt(rho_L), sqrt(rho_R) (roe_flux2 divides
-// them through by sqrt(rho_L)): the same function, whose reverse sweep is shorter in this form.
+// forward sweep is roe_flux2's (one reciprocal square root of rho_L rho_R for both sides).
 __device__ __forceinline__ void roe_flux2_adj(const double qm[4], const double qp[4], const double nx,
                                               const double ny, const Phys &P, const double fb[4], double qmb[4],
                                               double qpb[4]) {
@@ -47,18 +46,20 @@ __device__ __forceinline__ void roe_flux2_adj(const double qm[4], const double q
   const double tL = fma(nx, qm[2], -ny * qm[1]);
   const double mR = fma(nx, qp[1], ny * qp[2]);
   const double tR = fma(nx, qp[2], -ny * qp[1]);
-  const double rsL = rsqrt(qm[0]), rsR = rsqrt(qp[0]);
-  const double sL = qm[0] * rsL, sR = qp[0] * rsR;
-  const double irL = rsL * rsL, irR = rsR * rsR;
+  const double PLR = qm[0] * qp[0];
+  const double r = rsqrt(PLR);
+  const double r2 = r * r;
+  const double irL = qp[0] * r2, irR = qm[0] * r2;
   const double uL = mL * irL, vL = tL * irL;
   const double uR = mR * irR, vR = tR * irR;
   const double pL = P.gm1 * fma(-0.5, fma(mL, uL, tL * vL), qm[3]);
   const double pR = P.gm1 * fma(-0.5, fma(mR, uR, tR * vR), qp[3]);
   const double EpL = qm[3] + pL, EpR = qp[3] + pR;
   const double HL = EpL * irL, HR = EpR * irR;
-  const double rho = sL * sR;
-  const double isum = rcp(sL + sR);
-  const double us = fma(sL, uL, sR * uR), vs = fma(sL, vL, sR * vR), Hs = fma(sL, HL, sR * HR);
+  const double rho = PLR * r;
+  const double R = qp[0] * r;
+  const double isum = rcp(1.0 + R);
+  const double us = fma(R, uR, uL), vs = fma(R, vR, vL), Hs = fma(R, HR, HL);
   const double u = us * isum, v = vs * isum, H = Hs * isum;
   const double q2 = fma(u, u, v * v);
   const double c2 = P.gm1 * fma(-0.5, q2, H);
@@ -131,20 +132,19 @@ __device__ __forceinline__ void roe_flux2_adj(const double qm[4], const double q
   q2b -= 0.5 * c2b * P.gm1;
   ub += 2.0 * u * q2b;
   vb += 2.0 * v * q2b;
-  // u, v, H = (sL x_L + sR x_R) * isum
-  double isumb = Hb * Hs + ub * us + vb * vs;
+  // u, v, H = (x_L + R x_R) * isum, isum = 1 / (1 + R)
+  const double isumb = Hb * Hs + ub * us + vb * vs;
   const double Hsb = Hb * isum, usb = ub * isum, vsb = vb * isum;
-  double sLb = Hsb * HL + usb * uL + vsb * vL;
-  double sRb = Hsb * HR + usb * uR + vsb * vR;
-  double HLb = Hsb * sL, HRb = Hsb * sR;
-  uLb += usb * sL;
-  uRb += usb * sR;
-  vLb += vsb * sL;
-  vRb += vsb * sR;
-  sLb -= isumb * isum * isum;
-  sRb -= isumb * isum * isum;
-  sLb += rhob * sR;
-  sRb += rhob * sL;
+  const double Rb = Hsb * HR + usb * uR + vsb * vR - isumb * isum * isum;
+  const double HLb = Hsb, HRb = Hsb * R;
+  uLb += usb;
+  uRb += usb * R;
+  vLb += vsb;
+  vRb += vsb * R;
+  // rho = PLR r, R = rho_R r
+  double rb = rhob * PLR + Rb * qp[0];
+  double PLRb = rhob * r;
+  q0pb += Rb * r;
   // H = Ep * ir
   EpLb += HLb * irL;
   double irLb = HLb * EpL;
@@ -173,11 +173,13 @@ __device__ __forceinline__ void roe_flux2_adj(const double qm[4], const double q
   mRb += uRb * irR;
   irRb += uRb * mR + vRb * tR;
   tRb += vRb * irR;
-  // ir = rs^2, s = q0 rs, rs = q0^(-1/2)
-  double rsLb = 2.0 * rsL * irLb + sLb * qm[0];
-  double rsRb = 2.0 * rsR * irRb + sRb * qp[0];
-  q0mb += sLb * rsL + rsLb * (-0.5) * rsL * irL;
-  q0pb += sRb * rsR + rsRb * (-0.5) * rsR * irR;
+  // irL = rho_R r^2, irR = rho_L r^2, r = PLR^(-1/2), PLR = rho_L rho_R
+  q0pb += irLb * r2;
+  q0mb += irRb * r2;
+  rb += 2.0 * r * (irLb * qp[0] + irRb * qm[0]);
+  PLRb += rb * (-0.5) * r * r2;
+  q0mb += PLRb * qp[0];
+  q0pb += PLRb * qm[0];
   // m = nx q1 + ny q2, t = nx q2 - ny q1
   qmb[0] += q0mb;
   qmb[1] += mLb * nx - tLb * ny;
@@ -321,9 +323,12 @@ __global__ void __launch_bounds__(32 * np_of(N), oz_used_t(N, TC) ? 3 : 1)
   constexpr int Np = np_of(N), Nfp = N + 1, NK = nk_of(N);
   constexpr int NUe = Sym<N>::NUe, NUo = Sym<N>::NUo, NRe = Sym<N>::NRe;
   extern __shared__ double2 sm[];
-  double2 *M = sm;                      // [Np][32] x 4 doubles: mu per node
-  double2 *MS = sm + Np * 32 * 2;       // [Np][32] x 4: even rows, then odd rows
-  double2 *XS = sm + 2 * Np * 32 * 2;   // [NK][32] x 4: even columns, then odd columns
+  // rows of 32 cells x 4 doubles, kElemSlot doubles apart (the padding keeps the tensor-core
+  // fragment loads free of bank conflicts)
+  constexpr int kS2 = kElemSlot / 2;
+  double2 *M = sm;                 // [Np] rows: mu per node
+  double2 *MS = sm + Np * kS2;     // [Np] rows: even rows, then odd rows
+  double2 *XS = sm + 2 * Np * kS2; // [NK] rows: even columns, then odd columns
   const int lane = threadIdx.x, i = threadIdx.y;
   const int e0 = blockIdx.x * 32, e = e0 + lane;
   const bool live = e < d.K;
@@ -333,29 +338,29 @@ __global__ void __launch_bounds__(32 * np_of(N), oz_used_t(N, TC) ? 3 : 1)
       m01 = ld2(mu + ((size_t)e * Np + i) * 4);
       m23 = ld2(mu + ((size_t)e * Np + i) * 4 + 2);
     }
-    M[(i * 32 + lane) * 2] = m01;
-    M[(i * 32 + lane) * 2 + 1] = m23;
+    M[i * kS2 + lane * 2] = m01;
+    M[i * kS2 + lane * 2 + 1] = m23;
   }
   __syncthreads();
   {  // R^T: row i of the split from its node pair
     const int a = c_rin[N][2 * i], b = c_rin[N][2 * i + 1];
-    double2 v01 = M[(a * 32 + lane) * 2], v23 = M[(a * 32 + lane) * 2 + 1];
+    double2 v01 = M[a * kS2 + lane * 2], v23 = M[a * kS2 + lane * 2 + 1];
     if (b >= 0) {
-      const double2 w01 = M[(b * 32 + lane) * 2], w23 = M[(b * 32 + lane) * 2 + 1];
+      const double2 w01 = M[b * kS2 + lane * 2], w23 = M[b * kS2 + lane * 2 + 1];
       if (i < NRe) {
         v01.x += w01.x; v01.y += w01.y; v23.x += w23.x; v23.y += w23.y;
       } else {
         v01.x -= w01.x; v01.y -= w01.y; v23.x -= w23.x; v23.y -= w23.y;
       }
     }
-    MS[(i * 32 + lane) * 2] = v01;
-    MS[(i * 32 + lane) * 2 + 1] = v23;
+    MS[i * kS2 + lane * 2] = v01;
+    MS[i * kS2 + lane * 2 + 1] = v23;
   }
   __syncthreads();
   // S^T: column k of the even block (k < NUe) or of the odd block
   if constexpr (oz_used_t(N, TC)) {
-    oz_contract_t<N, NUe, NUo, NRe, Sym<N>::NRo>(reinterpret_cast<const double *>(MS), reinterpret_cast<double *>(XS),
-                                                 i, Np, lane);
+    oz_contract_t<N, NUe, NUo, NRe, Sym<N>::NRo, kElemSlot>(reinterpret_cast<const double *>(MS),
+                                                            reinterpret_cast<double *>(XS), i, Np, lane);
   } else
   for (int k = i; k < NK; k += Np) {
     double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
@@ -363,7 +368,7 @@ __global__ void __launch_bounds__(32 * np_of(N), oz_used_t(N, TC) ? 3 : 1)
 #pragma unroll
       for (int r = 0; r < NRe; r++) {
         const double cc = opS<N>(r * NUe + k);
-        const double2 x01 = MS[(r * 32 + lane) * 2], x23 = MS[(r * 32 + lane) * 2 + 1];
+        const double2 x01 = MS[r * kS2 + lane * 2], x23 = MS[r * kS2 + lane * 2 + 1];
         a0 = fma(cc, x01.x, a0); a1 = fma(cc, x01.y, a1); a2 = fma(cc, x23.x, a2); a3 = fma(cc, x23.y, a3);
       }
     } else {
@@ -371,25 +376,25 @@ __global__ void __launch_bounds__(32 * np_of(N), oz_used_t(N, TC) ? 3 : 1)
 #pragma unroll
       for (int q = 0; q < Np - NRe; q++) {
         const double cc = opS<N>(NRe * NUe + q * NUo + kk);
-        const double2 x01 = MS[((NRe + q) * 32 + lane) * 2], x23 = MS[((NRe + q) * 32 + lane) * 2 + 1];
+        const double2 x01 = MS[(NRe + q) * kS2 + lane * 2], x23 = MS[(NRe + q) * kS2 + lane * 2 + 1];
         a0 = fma(cc, x01.x, a0); a1 = fma(cc, x01.y, a1); a2 = fma(cc, x23.x, a2); a3 = fma(cc, x23.y, a3);
       }
     }
-    XS[(k * 32 + lane) * 2] = make_double2(a0, a1);
-    XS[(k * 32 + lane) * 2 + 1] = make_double2(a2, a3);
+    XS[k * kS2 + lane * 2] = make_double2(a0, a1);
+    XS[k * kS2 + lane * 2 + 1] = make_double2(a2, a3);
   }
   __syncthreads();
   // B^T: the adjoint of original input column c for cell el
   auto col = [&](const int c, const int el, double2 &o01, double2 &o23) {
     const int pos = c_pos[N][c];
     if (pos >= NUo && pos < NUe) {  // a column fixed by the reflection
-      o01 = XS[(pos * 32 + el) * 2];
-      o23 = XS[(pos * 32 + el) * 2 + 1];
+      o01 = XS[pos * kS2 + el * 2];
+      o23 = XS[pos * kS2 + el * 2 + 1];
       return;
     }
     const int p = pos < NUo ? pos : pos - NUe;
-    const double2 e01 = XS[(p * 32 + el) * 2], e23 = XS[(p * 32 + el) * 2 + 1];
-    const double2 d01 = XS[((NUe + p) * 32 + el) * 2], d23 = XS[((NUe + p) * 32 + el) * 2 + 1];
+    const double2 e01 = XS[p * kS2 + el * 2], e23 = XS[p * kS2 + el * 2 + 1];
+    const double2 d01 = XS[(NUe + p) * kS2 + el * 2], d23 = XS[(NUe + p) * kS2 + el * 2 + 1];
     if (pos < NUo) {
       o01 = make_double2(e01.x + d01.x, e01.y + d01.y);
       o23 = make_double2(e23.x + d23.x, e23.y + d23.y);
@@ -805,7 +810,7 @@ struct Adjoint {
         for (auto k : {adj_elem_kernel_sym<NN, false>, adj_elem_kernel_sym<NN, true>})
           if (ce == cudaSuccess)
             ce = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)((size_t)(2 * np_of(NN) + nk_of(NN)) * 32 * 4 * sizeof(double)));
+                                      (int)((size_t)(2 * np_of(NN) + nk_of(NN)) * kElemSlot * sizeof(double)));
       });
     }
     if (ce != cudaSuccess) { err = cudaGetErrorString(ce); return -100; }
@@ -923,7 +928,7 @@ struct Adjoint {
     const int total = (d.nE + d.nB) * (cfg.N + 1);
     DG_DISPATCH(cfg.N, {
       if (g_elem_variant) {
-        const size_t sm = (size_t)(2 * np_of(NN) + nk_of(NN)) * 32 * 4 * sizeof(double);
+        const size_t sm = (size_t)(2 * np_of(NN) + nk_of(NN)) * kElemSlot * sizeof(double);
         if (g_elem_variant >= 2 && oz_used_t(NN, true))
           adj_elem_kernel_sym<NN, true><<<(d.K + 31) / 32, dim3(32, np_of(NN)), sm, st>>>(d, v, wbar, fluxbar);
         else

@@ -359,10 +359,10 @@ __device__ __forceinline__ void oz_contract_dense(const double *Xd, double *Yd, 
 
 // The adjoint element kernel's transposed contraction: columns 0..NUe-1 = S_e^T (even rows of the
 // staged node adjoints), columns NUe.. = S_o^T (odd rows).
-template <int N, int NUe, int NUo, int NRe, int NRo>
+template <int N, int NUe, int NUo, int NRe, int NRo, int XST = 128>
 __device__ __forceinline__ void oz_contract_t(const double *Xd, double *Yd, const int warp, const int nw,
                                               const int lane) {
-  oz_product<N, 1, NRe, NUe, NRo, NUo, NRe, NUe>(Xd, Yd, warp, nw, lane);
+  oz_product<N, 1, NRe, NUe, NRo, NUo, NRe, NUe, false, XST>(Xd, Yd, warp, nw, lane);
 }
 
 // ---------------------------------------------------------------- host: operator digits
