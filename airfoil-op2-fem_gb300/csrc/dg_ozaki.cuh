@@ -11,14 +11,16 @@
 //
 //  * every column of X_p (16 or 32 values) is scaled by its largest binary exponent E, so each
 //    value is x = m 2^(E-55) with m an integer, |m| < 2^56 (the bits below 2^(E-55) are cut);
-//    every operator row by its own F likewise (done once on the host).  m is written in base 256
-//    as seven signed digits d_0..d_6 (|d| <= 255, all with the sign of x), each exact in bf16.
+//    every operator row by its own F likewise (done once on the host).  In the element kernel
+//    oz_prep does this once per staged value and forms the even/odd sums and differences exactly
+//    from values aligned to 2^(E-54).  m is written in base 256 as seven signed digits d_0..d_6
+//    (|d| <= 255, all with the sign of x), each exact in bf16.
 //  * digit products d_j c_s with j + s = L are summed into one FP32 accumulator per level L
 //    (L = 0..6; the levels L >= 7 lie below 2^-56 of the leading term and are dropped).  A level
 //    sums at most 7 pairs x 32 slots x 255^2 < 2^24, so every accumulation is an exact integer
 //    (checked on the GPU: bit-exact against 64-bit integer sums up to 1.46e7).
-//  * the seven level sums are joined as integers, T = sum_L lev_L 256^(6-L) (two 64-bit parts of
-//    < 2^49 each), and T 2^(E+F-62) is rounded to the nearest double with integer instructions
+//  * the seven level sums are joined as integers, T = sum_L lev_L 256^(6-L) (two 64-bit parts,
+//    below 2^41 and 2^49), and T 2^(E+F-62) is rounded to the nearest double with integer instructions
 //    only (oz_round; no FP64 instruction and no int-to-double conversion, which takes several
 //    FP64 issue slots on this part).  The result is the correctly rounded dot product of the
 //    56-bit truncations:
@@ -30,16 +32,17 @@
 
 // Tables of the operator blocks S_p (T = 0: rows of S_p are the outputs, the element kernel),
 // of their transposes (T = 1: columns of S_p are the outputs, the adjoint element kernel) and of
-// the dense rows A = [Drw | Dsw | -LIFT] (T = 2, parity 0 only: the element kernel's dense form).
+// the dense rows A = [Drw | Dsw | -LIFT/2] (T = 2, parity 0 only: the element kernel's dense form).
 constexpr int kOzRows = 32;  // outputs per parity: up to 4 n-tiles of 8
 constexpr int kOzTables = 3;
 __constant__ int c_ozf[kOzTables][7][2][kOzRows];  // biased binary exponent F of every output row: T, order, parity, row
 __device__ uint2 g_ozb[kOzTables][7][2][4][7][2][32];  // B fragments: T, order, parity, n-tile, digit s, k-step, lane
 
-// Orders that use it: N = 3, 4, 5 (steps on the K=32768 O-grid: 365 -> 328, 564 -> 477,
-// 909 -> 720 us).  At N = 1 and 2 the contraction is too small a share of the element kernel and
-// the split costs more than it saves (N = 1: 184 -> 192 us, N = 2: 236 -> 252 us).  Orders up to
-// 5 fit the exactness bound (at most two k-steps of 16 slots); N = 6 needs three.
+// Orders that use the even/odd blocks on the tensor cores: N = 3, 4, 5 (steps on the K=32768
+// O-grid, first form: 365 -> 328, 564 -> 477, 909 -> 720 us).  At N = 1 and 2 the even/odd blocks
+// were too small a share of the element kernel for the split to pay (N = 1: 184 -> 192 us, N = 2:
+// 236 -> 252 us); those orders use the dense rows instead (ozd_used).  Orders up to 5 fit the
+// exactness bound (at most two k-steps of 16 slots); N = 6 needs three.
 constexpr int kOzMaxN = 5;
 constexpr bool oz_used(int N, bool tc) { return tc && (N == 3 || N == 4 || N == 5); }
 // The adjoint element kernel's transposed contraction: N = 3 (the transposed blocks of N = 4
