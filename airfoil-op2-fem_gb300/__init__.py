@@ -126,6 +126,7 @@ def lib():
         "dg_set_elem_variant": (None, [C.c_int]),
         "dg_elem_variant": (C.c_int, []),
         "dg_tc_operator_digits": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+        "dg_tc_round": (C.c_int, [C.c_longlong, C.c_longlong, C.c_int, C.c_void_p]),
         "dg_set_face_block": (None, [C.c_int]),
         "dg_set_pdl": (None, [C.c_int]),
         "dg_batch_create": (C.c_int, [C.c_int, C.POINTER(Config), C.POINTER(vp), C.POINTER(vp)]),

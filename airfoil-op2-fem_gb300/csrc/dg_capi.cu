@@ -640,6 +640,14 @@ int dg_tc_operator_digits(int N, int *dims, double *S, int *fexp, int *digits) {
   if (digits) std::copy(dig.begin(), dig.end(), digits);
   return 0;
 }
+int dg_tc_round(long long th, long long tl, int sc, double *out) {
+  if (!out || sc < -1022 || sc > 900) return fail(DG_ERR_ARG, "dg_tc_round: sc outside -1022..900");
+  const long long lim_h = 1LL << 41, lim_l = 1LL << 49;
+  if (th <= -lim_h || th >= lim_h || tl <= -lim_l || tl >= lim_l)
+    return fail(DG_ERR_ARG, "dg_tc_round: |th| < 2^41 and |tl| < 2^49 required");
+  *out = dg::tc_round(th, tl, sc);
+  return 0;
+}
 void dg_set_face_block(int threads) { dg::set_face_block(threads); }
 void dg_set_pdl(int on) { dg::set_pdl(on); }
 

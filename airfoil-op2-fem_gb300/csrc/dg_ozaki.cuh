@@ -91,7 +91,25 @@ __device__ __forceinline__ uint32_t oz_pack(const float f_lo, const float f_hi, 
 // -1022 <= sc <= 900 the result is a normal double (its biased exponent is sc + 1022 plus the
 // bit length of T, at most 1997), so no subnormal or overflow case arises.  The result equals
 // RN(th 2^(32+sc) + tl 2^sc), the sum of the two exact parts rounded once.
-__device__ __forceinline__ double oz_round(const long long th, const long long tl, const int sc) {
+// Host and device alike (the host copy serves the library's rounding check, dg_tc_round).
+__host__ __device__ __forceinline__ int oz_clz64(const unsigned long long x) {
+#ifdef __CUDA_ARCH__
+  return __clzll((long long)x);
+#else
+  return __builtin_clzll(x);
+#endif
+}
+__host__ __device__ __forceinline__ double oz_double(const unsigned long long b) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)b);
+#else
+  double d;
+  std::memcpy(&d, &b, sizeof d);
+  return d;
+#endif
+}
+
+__host__ __device__ __forceinline__ double oz_round(const long long th, const long long tl, const int sc) {
   // T = H 2^32 + L with 0 <= L < 2^32, then |T| = MH 2^32 + ML (MH < 2^42, ML < 2^32)
   const long long H = th + (tl >> 32);
   const unsigned long long L = (unsigned long long)tl & 0xFFFFFFFFull;
@@ -119,7 +137,7 @@ __device__ __forceinline__ double oz_round(const long long th, const long long t
     sticky = false;
   }
   if (S == 0ull) return 0.0;
-  const int nb = 64 - __clzll((long long)S);  // bit length of S
+  const int nb = 64 - oz_clz64(S);  // bit length of S
   unsigned long long q;  // significand, 2^52 <= q < 2^53
   int e2;                // value = q 2^(e2 + sc)
   if (nb <= 53) {        // (off = 0 here: S >= 2^53 otherwise)
@@ -137,7 +155,7 @@ __device__ __forceinline__ double oz_round(const long long th, const long long t
     }
   }
   const unsigned long long be = (unsigned long long)(e2 + sc + 52 + 1023);
-  return __longlong_as_double((long long)(sign | (be << 52) | (q & 0xFFFFFFFFFFFFFull)));
+  return oz_double(sign | (be << 52) | (q & 0xFFFFFFFFFFFFFull));
 }
 
 // Bit pattern of a double -> its magnitude aligned to the biased column exponent em as an integer,

@@ -1041,6 +1041,10 @@ int tc_operator_tables(int N, int dims[4], std::vector<double> &S, int fexp[2][k
   return oz_digits(t.S, t.NUe, t.NUo, t.NRe, t.NRo, fexp, dig, err);
 }
 
+// Host-only: the tensor-core contraction's final rounding, (th 2^32 + tl) 2^sc to the nearest
+// double, exactly as the device computes it.
+double tc_round(long long th, long long tl, int sc) { return oz_round(th, tl, sc); }
+
 // ---------------------------------------------------------------- operator upload
 static int g_ops_loaded[7] = {0};
 static std::string g_ops_err;

@@ -48,7 +48,9 @@ struct Inst {
 };
 
 int load_order_constants(int N, std::string &err);
-// Element kernel form for launches enqueued from now on: 1 even/odd (default), 0 dense.
+// Element kernel form for launches enqueued from now on: 3 (default) tensor cores (dense rows at
+// N = 1, 2, even/odd blocks at N = 3-5), 2 even/odd blocks on the tensor cores at N = 3-5,
+// 1 even/odd FP64, 0 dense FP64.
 void set_elem_variant(int v);
 int elem_variant();
 // Host-only: parity dimensions {NUe, NUo, NRe, NRo}, even/odd operator blocks, row exponents
@@ -56,6 +58,9 @@ int elem_variant();
 // contraction of order N.
 int tc_operator_tables(int N, int dims[4], std::vector<double> &S, int fexp[2][32], std::vector<int> &dig,
                        std::string &err);
+// Host-only: (th 2^32 + tl) 2^sc rounded to the nearest double as the tensor-core contraction
+// rounds its level sums (valid for -1022 <= sc <= 900).
+double tc_round(long long th, long long tl, int sc);
 // Threads per face-kernel block for launches enqueued from now on (32..256, multiple of 32).
 void set_face_block(int b);
 // Programmatic dependent launch of the plain path's face and element kernels (default on).

@@ -271,6 +271,10 @@ int dg_elem_variant(void);
  * exponent F; digits (2 x 7 x 32 x 32 ints, may be NULL) [parity][digit s][slot k][row n], with
  * S[n][k] = sum_s digit * 256^(6-s) * 2^(F-1023-55) up to the cut bits below 2^(F-1023-55). */
 int dg_tc_operator_digits(int N, int *dims, double *S, int *fexp, int *digits);
+/* Host-only (no GPU needed): the final rounding of the tensor-core contraction, the same code the
+ * device runs.  *out = (th * 2^32 + tl) * 2^sc rounded to the nearest double, ties to even, for
+ * |th| < 2^41, |tl| < 2^49 (the joined level sums) and -1022 <= sc <= 900; DG_ERR_ARG outside. */
+int dg_tc_round(long long th, long long tl, int sc, double *out);
 /* Threads per face-kernel block of the plain path (32..256, multiple of 32; default 64). */
 void dg_set_face_block(int threads);
 /* Launch the plain path's face and element kernels with programmatic dependent launch (1, the

@@ -57,3 +57,50 @@ def test_level_sums_stay_exact(pkg, N):
 def test_orders_without_tensor_cores(pkg, N):
     dims = np.zeros(4, np.int32)
     assert pkg.lib().dg_tc_operator_digits(N, dims.ctypes.data, None, None, None) != 0
+
+
+def _exact_rne(T, sc):
+    """T * 2^sc rounded to the nearest double, ties to even (Python's int and Fraction
+    conversions round correctly)."""
+    if sc >= 0:
+        return float(T * 2 ** sc)
+    return float(Fraction(T, 2 ** (-sc)))
+
+
+def test_integer_rounding_matches_exact(pkg):
+    """The contraction joins its seven FP32 level sums as integers (th 2^32 + tl) and rounds
+    T 2^sc to a double with integer instructions only.  The library's host copy of that code
+    (the device runs the same function) against exact rational rounding: random level sums
+    anywhere below 2^24, sparse and cancelling ones, and exact ties."""
+    import ctypes as C
+    lib = pkg.lib()
+    rng = np.random.default_rng(20261203)
+    out = C.c_double()
+
+    def check(th, tl, sc):
+        assert lib.dg_tc_round(int(th), int(tl), int(sc), C.byref(out)) == 0
+        want = _exact_rne(int(th) * 2 ** 32 + int(tl), int(sc))
+        assert np.float64(out.value).tobytes() == np.float64(want).tobytes(), (th, tl, sc, out.value, want)
+
+    for trial in range(4000):
+        mode = trial % 4
+        lim = [2 ** 24, 2 ** int(rng.integers(0, 25)), 256, 3][mode]
+        lev = [int(x) for x in rng.integers(-lim + 1, lim, 7)]
+        for k in range(int(rng.integers(0, 7)) if trial % 3 == 0 else 0):
+            lev[k] = 0
+        th = lev[0] * 65536 + lev[1] * 256 + lev[2]
+        tl = lev[3] * 16777216 + lev[4] * 65536 + lev[5] * 256 + lev[6]
+        check(th, tl, int(rng.integers(-1022, 901)))
+    # ties: 53 significant bits plus exactly half an ulp, with an even and an odd last bit
+    for e in range(54, 73):
+        for odd in (0, 1):
+            for sign in (1, -1):
+                T = sign * ((1 << e) | (odd << (e - 52)) | (1 << (e - 53)))
+                th, tl = T >> 32, T - ((T >> 32) << 32)
+                check(th, tl, -60)
+    # zero and small values
+    for th, tl in ((0, 0), (0, 1), (0, -1), (1, 0), (-1, 0), (0, 2 ** 32 - 1)):
+        check(th, tl, 0)
+    # outside the stated range: refused
+    assert lib.dg_tc_round(0, 0, 901, C.byref(out)) != 0
+    assert lib.dg_tc_round(2 ** 41, 0, 0, C.byref(out)) != 0
