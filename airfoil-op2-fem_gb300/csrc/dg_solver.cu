@@ -434,9 +434,9 @@ __global__ void __launch_bounds__(32 * np_of(N)) elem_kernel(const Inst d, const
 // differences give y_i - y_P(i).  The contraction shrinks to 0.55-0.62 of the dense one.
 // One tile of 32 cells starting at e0, thread (lane, node i) of a block with at least Np
 // node-warps (warps with i >= Np only take part in the barriers).
-// TC: 0 the even/odd contraction in FP64, 1 the even/odd blocks on the tensor cores (N = 3-5),
-// 2 the dense rows on the tensor cores (N <= 3, no butterfly; the even/odd blocks on the tensor
-// cores at N = 4, 5).
+// TC: 0 the even/odd contraction in FP64, 1 the even/odd blocks on the tensor cores (N = 3-5; the
+// butterfly and the operand alignment by oz_prep), 2 the dense rows on the tensor cores at N = 1, 2
+// (no butterfly) and form 1 at N = 3-5.
 template <int N, bool PDL = false, int TC = 0>
 __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, const int e0, const int lane,
                                               const int i, double2 *X) {
