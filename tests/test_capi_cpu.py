@@ -47,3 +47,20 @@ def test_bad_config_rejected(pkg):
     for cfg in (pkg.config(N=0), pkg.config(N=7), pkg.config(cfl=0.0), pkg.config(gam=1.0), pkg.config(app=5)):
         with pytest.raises(pkg.DGError):
             pkg.Solver(mesh, cfg)
+
+
+def test_element_form_selector(pkg):
+    """Host logic of the element-kernel form selector: 3 (the tensor-core forms) by default,
+    0..3 taken as given, anything else back to the default."""
+    lib = pkg.lib()
+    prev = lib.dg_elem_variant()
+    try:
+        assert prev == 3
+        for v in (0, 1, 2, 3):
+            lib.dg_set_elem_variant(v)
+            assert lib.dg_elem_variant() == v
+        for v in (-1, 4, 99):
+            lib.dg_set_elem_variant(v)
+            assert lib.dg_elem_variant() == 3
+    finally:
+        lib.dg_set_elem_variant(prev)
