@@ -156,6 +156,9 @@ def lib():
         "dg_adjoint_batch_backward": (C.c_int, [C.POINTER(vp), C.c_int, C.c_double, dp, C.POINTER(dp)]),
         "dg_adjoint_free": (None, [vp]),
         "dg_adjoint_last_error": (cp, []),
+        "dg_order_tables_loaded": (C.c_int, [C.c_int, C.c_int]),
+        "dg_rhs_noalloc_ready": (C.c_int, [C.c_int]),
+        "dg_once_table_selftest": (C.c_int, [C.c_int, C.c_int, ip, ip]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -11,7 +11,12 @@
 #include "dg_mesh.h"
 #include "dg_ops.h"
 #include "dg_handles.h"
+#include "dg_once.h"
 #include "dg_solver.h"
+
+#include <atomic>
+#include <chrono>
+#include <thread>
 
 namespace {
 thread_local std::string g_err;
@@ -650,5 +655,45 @@ int dg_tc_round(long long th, long long tl, int sc, double *out) {
 }
 void dg_set_face_block(int threads) { dg::set_face_block(threads); }
 void dg_set_pdl(int on) { dg::set_pdl(on); }
+
+int dg_order_tables_loaded(int device, int N) { return dg::order_constants_loaded(device, N); }
+int dg_rhs_noalloc_ready(int device) { return dg::noalloc_ready(device); }
+
+int dg_once_table_selftest(int threads, int devices, int *uploads, int *attempts) {
+  if (threads < 1 || threads > 64 || devices < 1 || devices > dg::kMaxDevices || !uploads || !attempts)
+    return fail(DG_ERR_ARG, "dg_once_table_selftest: 1..64 threads, 1..64 devices, two output arrays");
+  constexpr int S = dg::OnceTable::kSlots;
+  const int n = devices * S;
+  dg::OnceTable table;
+  std::vector<std::atomic<int>> ok(n), tries(n);
+  for (int k = 0; k < n; k++) { ok[k] = 0; tries[k] = 0; }
+  // the fake upload: takes a little time (so that threads meet inside it) and fails on its first
+  // attempt for every third pair, which must then be retried by a later call
+  auto load = [&](int k) {
+    const int t = tries[k]++;
+    std::this_thread::sleep_for(std::chrono::microseconds(50));
+    if (t == 0 && k % 3 == 0) return -7;
+    ok[k]++;
+    return 0;
+  };
+  std::vector<std::thread> pool;
+  for (int th = 0; th < threads; th++)
+    pool.emplace_back([&, th] {
+      for (int round = 0; round < 3; round++)
+        for (int j = 0; j < n; j++) {
+          const int k = (j * 7 + th * 13 + round * 5) % n;  // a different order in every thread
+          table.ensure(k / S, k % S, [&] { return load(k); });
+        }
+    });
+  for (auto &t : pool) t.join();
+  for (int k = 0; k < n; k++) {
+    if (table.done(k / S, k % S) != 1) return fail(DG_ERR_ARG, "pair left without a successful upload");
+    uploads[k] = ok[k];
+    attempts[k] = tries[k];
+  }
+  if (table.done(devices < dg::kMaxDevices ? devices : 0, S) != -1 || table.done(-1, 0) != -1)
+    return fail(DG_ERR_ARG, "range check");
+  return 0;
+}
 
 }  // extern "C"

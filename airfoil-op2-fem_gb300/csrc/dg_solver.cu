@@ -36,6 +36,7 @@
 
 #include "dg_device.cuh"
 #include "dg_mesh.h"
+#include "dg_once.h"
 #include "dg_ops.h"
 #include "dg_solver.h"
 #include "../../include/dg_gb300.h"
@@ -824,9 +825,9 @@ static void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t s
 
 template <int N>
 static void launch_face(const Inst &d, int stage, cudaStream_t s) {
-  const int nf = (d.nE + d.nB) * (N + 1);
+  const long long nf = ((long long)d.nE + d.nB) * (N + 1);
   const int bs = g_face_block;
-  launch_pdl(face_kernel<N>, dim3((nf + bs - 1) / bs), dim3(bs), 0, s, d, stage);
+  launch_pdl(face_kernel<N>, dim3((unsigned)((nf + bs - 1) / bs)), dim3(bs), 0, s, d, stage);
 }
 
 // 3: dense rows on the bf16 tensor cores at N = 1, 2 (dg_ozaki.cuh), form 2 at the other orders
@@ -1046,12 +1047,11 @@ int tc_operator_tables(int N, int dims[4], std::vector<double> &S, int fexp[2][k
 double tc_round(long long th, long long tl, int sc) { return oz_round(th, tl, sc); }
 
 // ---------------------------------------------------------------- operator upload
-static int g_ops_loaded[7] = {0};
-static std::string g_ops_err;
+// The order's tables go to the device that is current; g_order_table records which (device,
+// order) pairs are uploaded.
+static OnceTable g_order_table;
 
-int load_order_constants(int N, std::string &err) {
-  if (N < 1 || N > 6) { err = "order N must be in 1..6"; return -1; }
-  if (g_ops_loaded[N]) return 0;
+static int upload_order_constants(int N, std::string &err) {
   Operators o;
   if (build_operators(N, o)) { err = "operator construction failed"; return -2; }
   const int Np = o.Np, Nfp = o.Nfp;
@@ -1084,9 +1084,19 @@ int load_order_constants(int N, std::string &err) {
     DG_DISPATCH(N, ce = set_smem_attr<NN>());
   }
   if (ce != cudaSuccess) { err = std::string("constant upload: ") + cudaGetErrorString(ce); return -3; }
-  g_ops_loaded[N] = 1;
   return 0;
 }
+
+int load_order_constants(int N, std::string &err) {
+  if (N < 1 || N > 6) { err = "order N must be in 1..6"; return -1; }
+  int dev = 0;
+  const cudaError_t ce = cudaGetDevice(&dev);
+  if (ce != cudaSuccess) { err = std::string("cudaGetDevice: ") + cudaGetErrorString(ce); return -100; }
+  if (dev >= kMaxDevices) { err = "device ordinal beyond the library's table"; return -1; }
+  return g_order_table.ensure(dev, N, [&] { return upload_order_constants(N, err); });
+}
+
+int order_constants_loaded(int dev, int N) { return (N < 1 || N > 6) ? -1 : g_order_table.done(dev, N); }
 
 void set_elem_variant(int v) { g_elem_variant = (v >= 0 && v <= 3) ? v : 3; }
 int elem_variant() { return g_elem_variant; }
@@ -1408,37 +1418,40 @@ constexpr size_t kNoAllocScratchBytes = 32ull << 20;
 static __device__ __align__(256) double g_noalloc_flux[kNoAllocScratchBytes / sizeof(double)];
 static __device__ __align__(256) int g_noalloc_fmask[7][3 * 7];
 
+// Device addresses of the two arrays on each device (a host-side name of a __device__ array is
+// not a device address); written once per device under g_noalloc_table's lock, read after it.
 struct NoAllocDevice {
-  bool ready = false;
   double *flux = nullptr;
   int *fmask = nullptr;  // [7][21]
-  bool fmask_loaded[7] = {};
 };
-static NoAllocDevice g_noalloc[64];
+static NoAllocDevice g_noalloc[kMaxDevices];
+static OnceTable g_noalloc_table;  // slot 0: this device's addresses, every order's tables, fmasks
 
-// Per device, once, with that device current: the device addresses of the scratch arrays
-// (a host-side name of a __device__ array is not a device address).
-static int noalloc_setup(int dev, int N, std::string &err) {
-  if (dev < 0 || dev >= 64) { err = "device ordinal out of range"; return -1; }
-  NoAllocDevice &nd = g_noalloc[dev];
-  if (!nd.ready) {
+// Once per device, with that device current: the scratch addresses, and the operator tables and
+// face masks of every order 1..6, so that only the first call on a device makes synchronous
+// uploads (whatever its order).
+static int noalloc_setup(int dev, std::string &err) {
+  if (dev < 0 || dev >= kMaxDevices) { err = "device ordinal out of range"; return -1; }
+  return g_noalloc_table.ensure(dev, 0, [&]() -> int {
+    NoAllocDevice nd;
     cudaError_t ce = cudaGetSymbolAddress((void **)&nd.flux, g_noalloc_flux);
     if (ce != cudaSuccess) { err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(ce); return -100; }
     ce = cudaGetSymbolAddress((void **)&nd.fmask, g_noalloc_fmask);
     if (ce != cudaSuccess) { err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(ce); return -100; }
-    nd.ready = true;
-  }
-  if (int rc = load_order_constants(N, err)) return rc;
-  if (!nd.fmask_loaded[N]) {
-    Operators o;
-    if (build_operators(N, o)) { err = "operator construction failed"; return -2; }
-    cudaError_t ce = cudaMemcpyToSymbol(g_noalloc_fmask, o.FMASK.data(), o.FMASK.size() * sizeof(int),
-                                        (size_t)N * 3 * 7 * sizeof(int));
-    if (ce != cudaSuccess) { err = std::string("cudaMemcpyToSymbol: ") + cudaGetErrorString(ce); return -100; }
-    nd.fmask_loaded[N] = true;
-  }
-  return 0;
+    for (int N = 1; N <= 6; N++) {
+      if (int rc = load_order_constants(N, err)) return rc;
+      Operators o;
+      if (build_operators(N, o)) { err = "operator construction failed"; return -2; }
+      ce = cudaMemcpyToSymbol(g_noalloc_fmask, o.FMASK.data(), o.FMASK.size() * sizeof(int),
+                              (size_t)N * 3 * 7 * sizeof(int));
+      if (ce != cudaSuccess) { err = std::string("cudaMemcpyToSymbol: ") + cudaGetErrorString(ce); return -100; }
+    }
+    g_noalloc[dev] = nd;
+    return 0;
+  });
 }
+
+int noalloc_ready(int dev) { return g_noalloc_table.done(dev, 0); }
 
 int rhs_noalloc(const Config &c, int K, int nE, int nB, const double *W, const double *geo,
                 const int4 *edges, const int4 *bedges, double *rhs, cudaStream_t stream,
@@ -1453,8 +1466,8 @@ int rhs_noalloc(const Config &c, int K, int nE, int nB, const double *W, const d
   int dev = 0;
   cudaError_t ce = cudaGetDevice(&dev);
   if (ce != cudaSuccess) { err = std::string("cudaGetDevice: ") + cudaGetErrorString(ce); return -100; }
-  if (int rc = noalloc_setup(dev, N, err)) return rc;
-  const NoAllocDevice &nd = g_noalloc[dev];
+  if (int rc = noalloc_setup(dev, err)) return rc;
+  const NoAllocDevice nd = g_noalloc[dev];
   Inst d{};
   d.N = N;
   d.K = K;
@@ -1510,6 +1523,12 @@ extern "C" int dg_rhs_noalloc(const dg_config_t *cfg, int n_cells, int n_edges, 
   if (!cfg || n_cells <= 0 || n_edges < 0 || n_bedges < 0 || !W || !geo || !rhs || (n_edges && !edges) ||
       (n_bedges && !bedges)) {
     g_noalloc_err = "bad arguments";
+    return DG_ERR_ARG;
+  }
+  // every cell face is one side of exactly one edge or boundary edge; checked here in 64 bits, so
+  // that inconsistent counts never reach the face kernel
+  if (2ll * n_edges + n_bedges != 3ll * n_cells) {
+    g_noalloc_err = "inconsistent mesh counts: 2 n_edges + n_bedges must equal 3 n_cells";
     return DG_ERR_ARG;
   }
   if (cfg->N < 1 || cfg->N > 6 || cfg->app != 0 || !(cfg->gam > 1.0) || !(cfg->rho_inf > 0.0) || !(cfg->p_inf > 0.0)) {

@@ -47,7 +47,13 @@ struct Inst {
   Phys P;
 };
 
+// Uploads order N's operator tables and sets its kernels' shared-memory limits on the current
+// device, once per (device, order); thread-safe.
 int load_order_constants(int N, std::string &err);
+// 1 if order N's tables are on device dev, 0 if not, -1 for an argument out of range.
+int order_constants_loaded(int dev, int N);
+// 1 if the allocation-free entry point is set up on device dev, 0 if not, -1 out of range.
+int noalloc_ready(int dev);
 // Element kernel form for launches enqueued from now on: 3 (default) tensor cores (dense rows at
 // N = 1, 2, even/odd blocks at N = 3-5), 2 even/odd blocks on the tensor cores at N = 3-5,
 // 1 even/odd FP64, 0 dense FP64.

@@ -231,14 +231,32 @@ const char *dg_adjoint_last_error(void);
  *   all 16-byte aligned; every cell face covered by exactly one edge or boundary edge.
  * The face-flux scratch is a file-scope device array of 32 MiB that every GPU loading the
  * library holds until the process exits: meshes needing more (n_cells * 3 * (N+1) * 32 bytes)
- * are rejected with DG_ERR_ARG.  The first call on a device, with that device current, looks
- * up the scratch's device address and uploads the order's operators; make that first call
- * before any stream capture.  All calls share the scratch (cleared at the start of each
- * call): calls that overlap on the GPU race.  stream may be NULL (the legacy default stream).
+ * are rejected with DG_ERR_ARG, and so are counts with 2 n_edges + n_bedges != 3 n_cells.  The
+ * first call on each device, with that device current, looks up the scratch's device address
+ * there and uploads the operator tables of every order 1..6 (synchronous copies); make that
+ * first call on each device before any stream capture.  Later calls on that device, of any
+ * order, make no synchronous call.  The set-up is guarded by a lock, so host threads may make
+ * their first calls concurrently.  All calls on a device share its scratch (cleared at the start
+ * of each call): calls that overlap on the GPU race.  stream may be NULL (the legacy default
+ * stream).
  * Errors: dg_rhs_noalloc_error(). */
 int dg_rhs_noalloc(const dg_config_t *cfg, int n_cells, int n_edges, int n_bedges, const double *W,
                    const double *geo, const int *edges, const int *bedges, double *rhs, void *stream);
 const char *dg_rhs_noalloc_error(void);
+
+/* Set-up bookkeeping queries (host only, no device call): 1 if order N's operator tables (and its
+ * kernels' shared-memory limits) are uploaded to device `device`, 0 if not, -1 out of range.
+ * The tables are per device; every solver, batch, adjoint or allocation-free call uploads them
+ * once per (device, order). */
+int dg_order_tables_loaded(int device, int N);
+/* 1 if dg_rhs_noalloc has set itself up on device `device`, 0 if not, -1 out of range. */
+int dg_rhs_noalloc_ready(int device);
+/* Host-only check of the once-per-(device, slot) table behind both: `threads` host threads race
+ * through every pair of `devices` devices x 7 slots three times, with a fake upload that fails on
+ * its first attempt for every third pair.  uploads[d * 7 + s] receives the successful uploads
+ * of each pair (1 when the bookkeeping is right), attempts[] every attempt (2 for the pairs
+ * that failed once).  0 on success. */
+int dg_once_table_selftest(int threads, int devices, int *uploads, int *attempts);
 
 /* ------------------------------------------------------------------ measurement helpers */
 void *dg_host_alloc(size_t bytes); /* pinned */

@@ -17,7 +17,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libref.so")
-REFERENCE_TREE = "/root/reference"
+# Where the reference source tree is read from (the reference build and the golden fixtures):
+# the environment variable DG_REFERENCE_TREE, else the checkout location of this build machine.
+REFERENCE_TREE = os.environ.get("DG_REFERENCE_TREE", "/root/reference")
 
 APP_AIRFOIL, APP_VORTEX = 0, 1
 DT_EVERY_STEP, DT_FROZEN = 0, 1

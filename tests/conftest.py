@@ -8,7 +8,8 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, ROOT)
 GOLDEN = os.path.join(ROOT, "tests", "golden")
-REFERENCE_TREE = "/root/reference"
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+from oracle import REFERENCE_TREE  # noqa: E402  (one setting: DG_REFERENCE_TREE)
 
 
 def pytest_configure(config):

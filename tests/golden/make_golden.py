@@ -41,7 +41,7 @@ import mesh as om  # noqa: E402
 import operators as oo  # noqa: E402
 import oracle as orc  # noqa: E402
 
-REF = "/root/reference"
+REF = orc.REFERENCE_TREE  # DG_REFERENCE_TREE, see oracle/oracle.py
 PERTURB_SEED = 7
 
 

@@ -64,3 +64,35 @@ def test_element_form_selector(pkg):
             assert lib.dg_elem_variant() == 3
     finally:
         lib.dg_set_elem_variant(prev)
+
+
+def test_once_table_bookkeeping(pkg):
+    """Host logic behind the per-(device, order) operator uploads: threads racing through every
+    (device, slot) pair upload each pair exactly once, a failed upload is retried by a later call,
+    and nothing is marked loaded before it is."""
+    lib = pkg.lib()
+    devices, slots = 4, 7
+    ups = (ctypes.c_int * (devices * slots))()
+    tries = (ctypes.c_int * (devices * slots))()
+    assert lib.dg_once_table_selftest(8, devices, ups, tries) == 0
+    assert list(ups) == [1] * (devices * slots)
+    assert list(tries) == [2 if k % 3 == 0 else 1 for k in range(devices * slots)]
+    assert lib.dg_once_table_selftest(0, devices, ups, tries) != 0
+
+
+def test_order_tables_query_without_device(pkg):
+    """With no device nothing is loaded on any (device, order); out-of-range pairs are -1."""
+    lib = pkg.lib()
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    for dev in (0, 1, 63):
+        for N in range(1, 7):
+            assert lib.dg_order_tables_loaded(dev, N) == 0
+        assert lib.dg_rhs_noalloc_ready(dev) == 0
+    for dev, N in ((-1, 3), (64, 3), (0, 0), (0, 7)):
+        assert lib.dg_order_tables_loaded(dev, N) == -1
+    assert lib.dg_rhs_noalloc_ready(64) == -1

@@ -39,10 +39,9 @@ def noalloc_fn(pkg):
     return f, e
 
 
-def test_noalloc_rhs_matches_solver_rhs_twice(pkg, orc, omesh):
+def run_twice(pkg, orc, m, cfg, seed):
+    """Two allocation-free calls in a row on perturbed states, each against dg_solver_rhs."""
     torch = pytest.importorskip("torch")
-    m = omesh.naca_ogrid(64, 16, farfield="characteristic")
-    cfg = pkg.config(N=3, cfl=0.5, mach=0.5, alpha_deg=1.25)
     s = pkg.Solver(pkg.Mesh.from_tables(m), cfg).init()
     edges, bedges = kernel_tables(m)
     dev = torch.device("cuda", 0)
@@ -50,7 +49,7 @@ def test_noalloc_rhs_matches_solver_rhs_twice(pkg, orc, omesh):
     edges_d = torch.from_numpy(edges).to(dev)
     bedges_d = torch.from_numpy(bedges).to(dev)
     fn, err = noalloc_fn(pkg)
-    rng = np.random.default_rng(11)
+    rng = np.random.default_rng(seed)
     q = s.get("q")
     stream = torch.cuda.current_stream(dev).cuda_stream
     for _ in range(2):
@@ -68,12 +67,35 @@ def test_noalloc_rhs_matches_solver_rhs_twice(pkg, orc, omesh):
         assert orc.rel_l2(got, expect) < RHS_TOL
 
 
-def test_noalloc_rejects_oversize_mesh(pkg):
-    """A mesh whose face fluxes exceed the 32 MiB scratch is refused before any device work."""
+def test_noalloc_rhs_matches_solver_rhs_twice(pkg, orc, omesh):
+    m = omesh.naca_ogrid(64, 16, farfield="characteristic")
+    run_twice(pkg, orc, m, pkg.config(N=3, cfl=0.5, mach=0.5, alpha_deg=1.25), 11)
+
+
+@pytest.mark.parametrize("N", [1, 2, 3, 4, 5, 6])
+def test_noalloc_every_order(pkg, orc, omesh, N):
+    """Each order takes its own element-kernel form (dense rows on the tensor cores at N = 1, 2,
+    the even/odd blocks on the tensor cores at N = 3-5, FP64 at N = 6) and its own tables: every
+    one must be set up by the first call on the device, whatever that call's order was."""
+    m = omesh.naca_ogrid(16, 8, farfield="characteristic")
+    run_twice(pkg, orc, m, pkg.config(N=N, cfl=0.5, mach=0.45, alpha_deg=-1.5), 100 + N)
+    lib = pkg.lib()
+    assert lib.dg_rhs_noalloc_ready(0) == 1
+    assert [lib.dg_order_tables_loaded(0, n) for n in range(1, 7)] == [1] * 6
+
+
+def test_noalloc_rejects_bad_sizes(pkg):
+    """A mesh whose face fluxes exceed the 32 MiB scratch, or whose edge counts cannot cover its
+    cell faces exactly once, is refused before any device work."""
     fn, err = noalloc_fn(pkg)
     cfg = pkg.config(N=4)
-    fake = 256  # never dereferenced: the size check comes first
-    rc = fn(C.byref(cfg), 1 << 20, 1, 1, fake, fake, fake, fake, fake, None)
+    fake = 256  # never dereferenced: the size checks come first
+    K = 1 << 20
+    rc = fn(C.byref(cfg), K, (3 * K - 2) // 2, 2, fake, fake, fake, fake, fake, None)
     assert rc == -1 and b"too large" in err()
-    rc = fn(C.byref(pkg.config(N=3, app=1)), 16, 1, 1, fake, fake, fake, fake, fake, None)
+    rc = fn(C.byref(cfg), 16, 20, 9, fake, fake, fake, fake, fake, None)
+    assert rc == -1 and b"inconsistent" in err()
+    rc = fn(C.byref(cfg), 1 << 30, 1 << 30, 1 << 30, fake, fake, fake, fake, fake, None)
+    assert rc == -1 and b"too large" in err()
+    rc = fn(C.byref(pkg.config(N=3, app=1)), 16, 23, 2, fake, fake, fake, fake, fake, None)
     assert rc == -1 and b"app 0" in err()
