@@ -157,6 +157,8 @@ def lib():
         "dg_adjoint_free": (None, [vp]),
         "dg_adjoint_last_error": (cp, []),
         "dg_order_tables_loaded": (C.c_int, [C.c_int, C.c_int]),
+        "dg_boundary_state": (C.c_int, [C.POINTER(Config), C.c_int, C.c_int, dp, dp, dp]),
+        "dg_boundary_state_error": (cp, []),
         "dg_rhs_noalloc_ready": (C.c_int, [C.c_int]),
         "dg_once_table_selftest": (C.c_int, [C.c_int, C.c_int, ip, ip]),
     }
@@ -673,3 +675,15 @@ def fp64_peak_gflops():
 def fp64_mma_peak_gflops():
     """FP64 tensor-core (DMMA, mma.sync m8n8k4) throughput measured on this GPU, GFLOP/s."""
     return lib().dg_fp64_mma_peak_gflops()
+
+
+def boundary_state(cfg, bc_type, qi, nrm):
+    """The device's ghost state (dg_boundary_state) of boundary type bc_type for interior states
+    qi [n][4] and unit normals nrm [n][2]; returns [n][4]."""
+    qi = _f64(np.asarray(qi).reshape(-1, 4))
+    nrm = _f64(np.asarray(nrm).reshape(-1, 2))
+    out = np.empty_like(qi)
+    rc = lib().dg_boundary_state(C.byref(cfg), int(bc_type), qi.shape[0], _dp(qi), _dp(nrm), _dp(out))
+    if rc != 0:
+        raise DGError(rc, lib().dg_boundary_state_error().decode())
+    return out

@@ -1149,6 +1149,34 @@ static void edge_records(const Mesh &m, std::vector<int4> &edges, std::vector<in
     bedges[i] = make_int4(m.bedge2cell[i], m.bedgeNum[i], m.bedge_type.empty() ? 2 : m.bedge_type[i], 0);
 }
 
+// Freestream and gas constants of a configuration, as src/airfoil.cpp:79-99 computes them.
+Phys make_phys(const Config &c) {
+  Phys P{};
+  const double gam = c.gam;
+  P.gam = gam;
+  P.gm1 = gam - 1.0;
+  double u, v, e;
+  if (c.alpha_deg != 0.0) {
+    u = std::sin((M_PI / 2.0) - (c.alpha_deg * M_PI / 180.0)) * std::sqrt(gam * c.p_inf / c.rho_inf) * c.mach;
+    v = std::cos((M_PI / 2.0) - (c.alpha_deg * M_PI / 180.0)) * std::sqrt(gam * c.p_inf / c.rho_inf) * c.mach;
+    e = c.p_inf / (gam - 1.0) + 0.5 * c.rho_inf * (u * u + v * v);
+  } else {
+    u = std::sqrt(gam * c.p_inf / c.rho_inf) * c.mach;
+    v = 0.0;
+    e = c.p_inf / (gam - 1.0) + 0.5 * c.rho_inf * (u * u);
+  }
+  P.rinf = c.rho_inf;
+  P.uinf = u;
+  P.vinf = v;
+  P.pinf = c.p_inf;
+  P.einf = e;
+  P.vx0 = c.vortex_x0;
+  P.vy0 = c.vortex_y0;
+  P.vbeta = c.vortex_beta;
+  P.derive();
+  return P;
+}
+
 int Solver::create(const Config &c, const Mesh &m, std::string &err) {
   cfg = c;
   if (int rc = validate(m, err)) return rc;
@@ -1552,6 +1580,59 @@ extern "C" int dg_rhs_noalloc(const dg_config_t *cfg, int n_cells, int n_edges, 
   if (rc) {
     g_noalloc_err = err;
     return rc <= -100 ? DG_ERR_CUDA : DG_ERR_ARG;
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------- boundary ghost states
+// dg_boundary_state (include/dg_gb300.h): the device's ghost-state function bc_state applied to
+// n given interior states and unit normals, so that tests can check its physics (Riemann
+// invariants, entropy, tangential velocity of the characteristic farfield) independently of
+// any restatement of the formula.
+namespace dg {
+__global__ void boundary_state_kernel(int n, int type, const double *qi, const double *nrm, Phys P, double *qb) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  double a[4], b[4];
+  for (int j = 0; j < 4; j++) a[j] = qi[4 * k + j];
+  bc_state(type, a, nrm[2 * k], nrm[2 * k + 1], P, b);
+  for (int j = 0; j < 4; j++) qb[4 * k + j] = b[j];
+}
+}  // namespace dg
+
+namespace {
+thread_local std::string g_bstate_err;
+}
+extern "C" const char *dg_boundary_state_error(void) { return g_bstate_err.c_str(); }
+
+extern "C" int dg_boundary_state(const dg_config_t *cfg, int type, int n, const double *qi, const double *nrm,
+                                 double *qb) {
+  if (!cfg || n <= 0 || !qi || !nrm || !qb || type < 0 || type > 3 || !(cfg->gam > 1.0) || !(cfg->rho_inf > 0.0) ||
+      !(cfg->p_inf > 0.0)) {
+    g_bstate_err = "bad arguments";
+    return DG_ERR_ARG;
+  }
+  dg::Config c;
+  c.gam = cfg->gam;
+  c.mach = cfg->mach;
+  c.alpha_deg = cfg->alpha_deg;
+  c.p_inf = cfg->p_inf;
+  c.rho_inf = cfg->rho_inf;
+  const dg::Phys P = dg::make_phys(c);
+  double *d = nullptr;
+  const size_t bytes = (size_t)n * 10 * sizeof(double);
+  cudaError_t ce = cudaMalloc(&d, bytes);
+  if (ce == cudaSuccess) ce = cudaMemcpy(d, qi, (size_t)n * 4 * sizeof(double), cudaMemcpyHostToDevice);
+  if (ce == cudaSuccess) ce = cudaMemcpy(d + 4 * (size_t)n, nrm, (size_t)n * 2 * sizeof(double), cudaMemcpyHostToDevice);
+  if (ce == cudaSuccess) {
+    dg::boundary_state_kernel<<<(n + 127) / 128, 128>>>(n, type, d, d + 4 * (size_t)n, P, d + 6 * (size_t)n);
+    ce = cudaGetLastError();
+  }
+  if (ce == cudaSuccess) ce = cudaMemcpy(qb, d + 6 * (size_t)n, (size_t)n * 4 * sizeof(double), cudaMemcpyDeviceToHost);
+  if (d) cudaFree(d);
+  if (ce != cudaSuccess) {
+    g_bstate_err = std::string("dg_boundary_state: ") + cudaGetErrorString(ce);
+    return DG_ERR_CUDA;
   }
   return 0;
 }

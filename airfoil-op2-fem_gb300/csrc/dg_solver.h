@@ -50,6 +50,8 @@ struct Inst {
 // Uploads order N's operator tables and sets its kernels' shared-memory limits on the current
 // device, once per (device, order); thread-safe.
 int load_order_constants(int N, std::string &err);
+// Freestream and gas constants of a configuration (src/airfoil.cpp:79-99), derived terms set.
+Phys make_phys(const Config &c);
 // 1 if order N's tables are on device dev, 0 if not, -1 for an argument out of range.
 int order_constants_loaded(int dev, int N);
 // 1 if the allocation-free entry point is set up on device dev, 0 if not, -1 out of range.

@@ -244,6 +244,15 @@ int dg_rhs_noalloc(const dg_config_t *cfg, int n_cells, int n_edges, int n_bedge
                    const double *geo, const int *edges, const int *bedges, double *rhs, void *stream);
 const char *dg_rhs_noalloc_error(void);
 
+/* ------------------------------------------------------------------ diagnostics
+ * The device's boundary ghost state (src/get_bedge_q.h types 0 inflow, 1 outflow, 2 wall, and 3
+ * the characteristic farfield, which has no reference counterpart) for n interior states qi
+ * [n][4] and unit normals nrm [n][2], host arrays in and out (qb [n][4]); the freestream comes
+ * from cfg (gam, mach, alpha_deg, p_inf, rho_inf).  The same device function the face kernels
+ * call, so tests can check its physics directly.  Errors: dg_boundary_state_error(). */
+int dg_boundary_state(const dg_config_t *cfg, int type, int n, const double *qi, const double *nrm, double *qb);
+const char *dg_boundary_state_error(void);
+
 /* Set-up bookkeeping queries (host only, no device call): 1 if order N's operator tables (and its
  * kernels' shared-memory limits) are uploaded to device `device`, 0 if not, -1 out of range.
  * The tables are per device; every solver, batch, adjoint or allocation-free call uploads them

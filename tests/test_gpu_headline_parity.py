@@ -1,0 +1,193 @@
+"""Parity of the fused solver where the benchmark numbers are quoted, with the oracle computing
+its OWN geometry (src/init_grid.h: metrics as Dr x per node, normals and fscale per face node)
+from the mesh, so that the solver's per-cell affine geometry kernel is checked too; and checks of
+the characteristic farfield (boundary type 3, which has no reference counterpart) that do not go
+through any restatement of its formula.
+
+Tolerances (relative L2 over all of q, and over the dt sequence):
+  * q after 1000 steps: 1e-11, the parity target; the geometry difference alone (analytic
+    per-cell metrics against Dr x per node) moves q by ~1.4e-13 on the K=32768 O-grid
+    (measured with the oracle both ways);
+  * dt sequence: 1e-10 (the same measurement gives 1.5e-12).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def own_geometry_pair(pkg, orc, oops, m, N, cfl, phys, **cfgkw):
+    cfg = pkg.config(N=N, cfl=cfl, **cfgkw)
+    s = pkg.Solver(pkg.Mesh.from_tables(m), cfg).init()
+    o = orc.Oracle(m, oops.operators(N), phys, kind="port")
+    o.init(cfl)  # the oracle's own init_grid and calc_dt: nothing is pushed from the solver
+    return s, o
+
+
+def test_headline_1000_steps_own_geometry(pkg, orc, oops, omesh):
+    """The benchmark workload itself: NACA 0012 O-grid 256 x 64 (K = 32768), N = 3, M = 0.4,
+    alpha = 0, slip wall + characteristic farfield, CFL 0.5 with dt recomputed every step
+    (src/airfoil.cpp:252-334), 1000 SSPRK3 steps."""
+    m = omesh.naca_ogrid(256, 64, farfield="characteristic")
+    s, o = own_geometry_pair(pkg, orc, oops, m, 3, 0.5, orc.freestream(0.4, 0.0), mach=0.4, alpha_deg=0.0)
+    _, dt0, _ = s.time()
+    assert abs(dt0 / o.dt - 1) < 1e-12
+    s.record_dt(1000)
+    s.run(1000)
+    s.sync()
+    dts = o.run(1000, nthreads=0)
+    assert orc.rel_l2(s.get("q"), o.get("q")) < 1e-11
+    assert np.abs(s.dt_history(1000) / dts - 1).max() < 1e-10
+
+
+@pytest.mark.parametrize("N", [2, 5])
+def test_other_orders_1000_steps_own_geometry(pkg, orc, oops, omesh, N):
+    """N = 2 (dense rows on the tensor cores) and N = 5 (even/odd blocks on the tensor cores, one
+    block per SM) on the 128 x 32 O-grid (K = 8192), M = 0.5, alpha = 2 deg, 1000 steps."""
+    m = omesh.naca_ogrid(128, 32, farfield="characteristic")
+    s, o = own_geometry_pair(pkg, orc, oops, m, N, 0.5, orc.freestream(0.5, 2.0), mach=0.5, alpha_deg=2.0)
+    s.record_dt(1000)
+    s.run(1000)
+    s.sync()
+    dts = o.run(1000, nthreads=0)
+    assert orc.rel_l2(s.get("q"), o.get("q")) < 1e-11
+    assert np.abs(s.dt_history(1000) / dts - 1).max() < 1e-10
+
+
+@pytest.mark.parametrize("mach,alpha", [(0.4, 0.0), (0.6, 25.0), (1.6, -10.0)])
+def test_farfield_freestream_is_fixed_point(pkg, omesh, mach, alpha):
+    """With every boundary edge of an O-grid (its circular farfield gives every normal direction;
+    the inner ring too) set to the characteristic farfield, the freestream must be a fixed point
+    of the discrete step: subsonic inflow and outflow at M 0.4 and 0.6, and at M 1.6 also the
+    supersonic inflow and outflow branches."""
+    mesh = pkg.Mesh.naca_ogrid(128, 32, farfield="characteristic")
+    mesh.set_bedge_type(np.full(mesh.size("bedges"), 3, dtype=np.int32))
+    s = pkg.Solver(mesh, pkg.config(N=3, cfl=0.5, mach=mach, alpha_deg=alpha)).init()
+    q0 = s.get("q")
+    s.run(50)
+    s.sync()
+    assert np.abs(s.get("q") - q0).max() < 1e-12 * np.abs(q0).max()
+
+
+def _prims(q, gam):
+    rho = q[:, 0]
+    u, v = q[:, 1] / rho, q[:, 2] / rho
+    p = (gam - 1) * (q[:, 3] - 0.5 * rho * (u * u + v * v))
+    return rho, u, v, p
+
+
+def test_farfield_riemann_invariants(pkg, orc):
+    """The characteristic farfield ghost state, checked against the theory it is built on rather
+    than against a second copy of its formula: with R+- = v_n +- 2c/(gamma-1) the Riemann
+    invariants of the 1-D isentropic flow normal to the boundary (Toro, Riemann Solvers and
+    Numerical Methods for Fluid Dynamics, 3rd ed. 2009, ch. 3; the farfield treatment of Blazek,
+    Computational Fluid Dynamics: Principles and Applications, 2005), a subsonic boundary state
+    keeps the outgoing invariant R+ of the interior and takes the incoming R- of the freestream;
+    entropy p / rho^gamma and tangential velocity come from the upwind side (interior at
+    outflow, v_n > 0; freestream at inflow).  Supersonic inflow is the freestream, supersonic
+    outflow the interior."""
+    gam, mach, alpha = 1.4, 0.55, 7.0
+    cfg = pkg.config(N=3, mach=mach, alpha_deg=alpha, gam=gam)
+    fs = orc.freestream(mach, alpha)
+    qinf = np.array([fs["bc_r"], fs["bc_r"] * fs["bc_u"], fs["bc_r"] * fs["bc_v"], fs["bc_e"]])
+    rng = np.random.default_rng(5)
+    n = 4000
+    th = rng.uniform(0, 2 * np.pi, n)
+    nrm = np.stack([np.cos(th), np.sin(th)], 1)
+    # interior states: density and pressure within +-30 % of the freestream, velocity of any
+    # direction up to 2.2 times the freestream sound speed (subsonic and supersonic normals)
+    rho = rng.uniform(0.7, 1.3, n)
+    p = rng.uniform(0.7, 1.3, n)
+    c_inf = np.sqrt(gam * fs["bc_p"] / fs["bc_r"])
+    sp = rng.uniform(0.0, 2.2 * c_inf, n)
+    ang = rng.uniform(0, 2 * np.pi, n)
+    u, v = sp * np.cos(ang), sp * np.sin(ang)
+    qi = np.stack([rho, rho * u, rho * v, p / (gam - 1) + 0.5 * rho * (u * u + v * v)], 1)
+    qb = pkg.boundary_state(cfg, 3, qi, nrm)
+    ri, ui, vi, pi = _prims(qi, gam)
+    rb, ub, vb, pb = _prims(qb, gam)
+    ci, cb = np.sqrt(gam * pi / ri), np.sqrt(gam * pb / rb)
+    vni, vnb = ui * nrm[:, 0] + vi * nrm[:, 1], ub * nrm[:, 0] + vb * nrm[:, 1]
+    ti, tb = -ui * nrm[:, 1] + vi * nrm[:, 0], -ub * nrm[:, 1] + vb * nrm[:, 0]
+    vn_inf = fs["bc_u"] * nrm[:, 0] + fs["bc_v"] * nrm[:, 1]
+    t_inf = -fs["bc_u"] * nrm[:, 1] + fs["bc_v"] * nrm[:, 0]
+    k = 2.0 / (gam - 1)
+    sup_in, sup_out = vni <= -ci, vni >= ci
+    sub = ~(sup_in | sup_out)
+    assert sup_in.sum() > 100 and sup_out.sum() > 100 and sub.sum() > 1000
+    np.testing.assert_allclose(qb[sup_in], np.broadcast_to(qinf, qb[sup_in].shape), rtol=1e-15, atol=0)
+    np.testing.assert_array_equal(qb[sup_out], qi[sup_out])
+    # subsonic: both invariants (scale: the sound speed)
+    tol = 1e-13 * c_inf
+    assert np.abs((vnb + k * cb) - (vni + k * ci))[sub].max() < tol
+    assert np.abs((vnb - k * cb) - (vn_inf - k * c_inf))[sub].max() < tol
+    out, inn = sub & (vnb > 0), sub & (vnb <= 0)
+    assert out.sum() > 300 and inn.sum() > 300
+    s_b, s_i, s_inf = pb / rb ** gam, pi / ri ** gam, fs["bc_p"] / fs["bc_r"] ** gam
+    assert np.abs(s_b / s_i - 1)[out].max() < 1e-13
+    assert np.abs(s_b / s_inf - 1)[inn].max() < 1e-13
+    assert np.abs(tb - ti)[out].max() < tol
+    assert np.abs(tb - t_inf)[inn].max() < tol
+
+
+def test_reference_boundary_types(pkg, orc):
+    """Types 0-2 as src/get_bedge_q.h:24-50 defines them: inflow the freestream, outflow the
+    freestream density and momentum with the interior energy, wall the interior state with its
+    normal momentum reversed (density, energy and |momentum| kept)."""
+    gam, mach, alpha = 1.4, 0.4, 3.0
+    cfg = pkg.config(N=3, mach=mach, alpha_deg=alpha)
+    fs = orc.freestream(mach, alpha)
+    rng = np.random.default_rng(9)
+    n = 512
+    th = rng.uniform(0, 2 * np.pi, n)
+    nrm = np.stack([np.cos(th), np.sin(th)], 1)
+    qi = np.stack([rng.uniform(0.8, 1.2, n), rng.normal(0, 0.5, n), rng.normal(0, 0.5, n),
+                   rng.uniform(2.4, 3.0, n)], 1)
+    qinf = np.array([fs["bc_r"], fs["bc_r"] * fs["bc_u"], fs["bc_r"] * fs["bc_v"], fs["bc_e"]])
+    q0 = pkg.boundary_state(cfg, 0, qi, nrm)
+    np.testing.assert_array_equal(q0, np.broadcast_to(qinf, q0.shape))
+    q1 = pkg.boundary_state(cfg, 1, qi, nrm)
+    np.testing.assert_array_equal(q1[:, :3], np.broadcast_to(qinf[:3], q1[:, :3].shape))
+    np.testing.assert_array_equal(q1[:, 3], qi[:, 3])
+    q2 = pkg.boundary_state(cfg, 2, qi, nrm)
+    np.testing.assert_array_equal(q2[:, [0, 3]], qi[:, [0, 3]])
+    mn_i = qi[:, 1] * nrm[:, 0] + qi[:, 2] * nrm[:, 1]
+    mn_b = q2[:, 1] * nrm[:, 0] + q2[:, 2] * nrm[:, 1]
+    mt_i = -qi[:, 1] * nrm[:, 1] + qi[:, 2] * nrm[:, 0]
+    mt_b = -q2[:, 1] * nrm[:, 1] + q2[:, 2] * nrm[:, 0]
+    assert np.abs(mn_b + mn_i).max() < 1e-14
+    assert np.abs(mt_b - mt_i).max() < 1e-14
+
+
+def test_large_vortex_errors_match_oracle(pkg, orc, oops, omesh):
+    """The large vortex case: [-5,5]^2 in 2 x 512^2 = 524288 triangles, beta 5 at the origin,
+    dt = 0.5/dt1 frozen, every order N = 1..5, 50 steps (a bounded sample of the 200-step case
+    so the CPU oracle on all host cores finishes in seconds per order).  The oracle computes its
+    own geometry and node coordinates.  q must agree to 1e-12; each of the four sums of squared
+    nodal errors against the analytic state (vortex/src/l2_error.h) must agree within what the
+    two solutions' difference allows: by the triangle inequality
+    |sqrt(E_gpu) - sqrt(E_oracle)| <= ||q_gpu - q_oracle|| per variable (a few ulps of slack for
+    the summation), and at N = 1, where the discretisation error dominates, to 1e-8 relative."""
+    m = omesh.vortex_square(512)
+    phys = orc.freestream(0.4, 0.0)
+    phys.update(vortex_x0=0.0, vortex_y0=0.0, vortex_beta=5.0)
+    mesh = pkg.Mesh.from_tables(m)
+    for N in range(1, 6):
+        cfg = pkg.config(N=N, app=pkg.APP_VORTEX, dt_mode=pkg.DT_FROZEN, cfl=0.5, vortex_x0=0.0,
+                         vortex_y0=0.0, vortex_beta=5.0)
+        s = pkg.Solver(mesh, cfg).init()
+        o = orc.Oracle(m, oops.operators(N), phys, app=orc.APP_VORTEX, kind="port")
+        o.init(0.5)
+        assert abs(s.time()[1] / o.dt - 1) < 1e-12
+        s.run(50)
+        s.sync()
+        o.run(50, dt_mode=orc.DT_FROZEN, nthreads=0)
+        qg, qo = s.get("q"), o.get("q")
+        assert orc.rel_l2(qg, qo) < 1e-12, N
+        eg, eo = np.asarray(s.l2_error()), np.asarray(o.l2_error())
+        dq = np.sqrt(((qg - qo).reshape(-1, 4) ** 2).sum(axis=0))
+        slack = 1e-14 * np.sqrt(np.maximum(eg, eo)) + 1e-300
+        assert (np.abs(np.sqrt(eg) - np.sqrt(eo)) <= dq + slack).all(), (N, eg, eo, dq)
+        if N == 1:
+            assert np.abs(eg / eo - 1).max() < 1e-8, (N, eg, eo)
+        del s, o
