@@ -157,6 +157,9 @@ def lib():
         "dg_adjoint_free": (None, [vp]),
         "dg_adjoint_last_error": (cp, []),
         "dg_order_tables_loaded": (C.c_int, [C.c_int, C.c_int]),
+        "dg_solver_kernels_per_step": (C.c_int, [vp]),
+        "dg_set_step_parts": (None, [C.c_int]),
+        "dg_step_parts": (C.c_int, []),
         "dg_boundary_state": (C.c_int, [C.POINTER(Config), C.c_int, C.c_int, dp, dp, dp]),
         "dg_boundary_state_error": (cp, []),
         "dg_rhs_noalloc_ready": (C.c_int, [C.c_int]),
@@ -372,6 +375,10 @@ class Solver:
     @property
     def stream(self):
         return lib().dg_solver_stream(self.h)
+
+    def kernels_per_step(self):
+        """Kernel launches of one run() step (the step graph's nodes)."""
+        return lib().dg_solver_kernels_per_step(self.h)
 
     def vertex_fields(self):
         """rho, u, v, p per mesh vertex (src/save_solution.cpp's sampling)."""
@@ -687,3 +694,12 @@ def boundary_state(cfg, bc_type, qi, nrm):
     if rc != 0:
         raise DGError(rc, lib().dg_boundary_state_error().decode())
     return out
+
+
+def set_step_parts(parts):
+    """Cell ranges of step graphs built from now on (0 automatic, 1 one chain, 2..32)."""
+    lib().dg_set_step_parts(int(parts))
+
+
+def step_parts():
+    return lib().dg_step_parts()

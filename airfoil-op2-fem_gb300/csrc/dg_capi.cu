@@ -260,6 +260,8 @@ int dg_solver_run(dg_solver_t *h, int nsteps) {
   return 0;
 }
 
+int dg_solver_kernels_per_step(dg_solver_t *h) { return h ? h->s.kernels_per_step() : -1; }
+
 int dg_solver_sync(dg_solver_t *h) {
   if (!h) return fail(DG_ERR_ARG, "null solver");
   dg::StepState st;
@@ -629,6 +631,8 @@ double dg_fp64_mma_peak_gflops(void) {
   return g;
 }
 int dg_kernels_per_step(void) { return 7; }
+void dg_set_step_parts(int parts) { dg::set_step_parts(parts); }
+int dg_step_parts(void) { return dg::step_parts(); }
 void dg_set_elem_variant(int variant) { dg::set_elem_variant(variant); }
 int dg_elem_variant(void) { return dg::elem_variant(); }
 

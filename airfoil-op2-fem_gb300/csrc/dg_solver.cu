@@ -862,6 +862,28 @@ static void launch_elem(const Inst &d, int stage, cudaStream_t s) {
   }
 }
 
+// Element tiles [t0, t1) of one stage with the launch attributes of launch_elem (the even/odd
+// forms; the dense FP64 form only as a whole-mesh launch).
+template <int N>
+static void launch_elem_range(const Inst &d, int stage, int t0, int t1, cudaStream_t s) {
+  constexpr int Np = np_of(N);
+  if (t1 <= t0) return;
+  const size_t smem = elem_sym_smem(N);
+  if constexpr (ozd_used(N, 2)) {
+    if (g_elem_variant == 3) {
+      launch_pdl(elem_kernel_sym<N, 2, oz_min_blocks(N)>, dim3(t1 - t0), dim3(32, Np), smem, s, d, stage, t0);
+      return;
+    }
+  }
+  if constexpr (oz_used(N, true)) {
+    if (g_elem_variant >= 2) {
+      launch_pdl(elem_kernel_sym<N, true, oz_min_blocks(N)>, dim3(t1 - t0), dim3(32, Np), smem, s, d, stage, t0);
+      return;
+    }
+  }
+  launch_pdl(elem_kernel_sym<N, false>, dim3(t1 - t0), dim3(32, Np), smem, s, d, stage, t0);
+}
+
 // Element tiles [t0, t1) of one stage, in plain stream order on s (the even/odd forms only).
 template <int N>
 static void launch_elem_tiles(const Inst &d, int stage, int t0, int t1, cudaStream_t s) {
@@ -1120,6 +1142,8 @@ Solver::~Solver() {
     if (io_copy[c]) cudaEventDestroy(io_copy[c]);
   }
   if (io_fork) cudaEventDestroy(io_fork);
+  for (cudaStream_t st : pstreams) cudaStreamDestroy(st);
+  for (cudaEvent_t ev : pevents) cudaEventDestroy(ev);
   if (graph_exec) cudaGraphExecDestroy(graph_exec);
   if (graph) cudaGraphDestroy(graph);
   for (void *p : allocs) cudaFree(p);
@@ -1193,32 +1217,10 @@ int Solver::create(const Config &c, const Mesh &m, std::string &err) {
   d.nB = m.n_bedges();
   d.app = c.app;
   d.dt_mode = c.dt_mode;
-  const double gam = c.gam;
-  d.P.gam = gam;
-  d.P.gm1 = gam - 1.0;
-  // Freestream as src/airfoil.cpp:79-99.
-  double u, v, e;
-  if (c.alpha_deg != 0.0) {
-    u = std::sin((M_PI / 2.0) - (c.alpha_deg * M_PI / 180.0)) * std::sqrt(gam * c.p_inf / c.rho_inf) * c.mach;
-    v = std::cos((M_PI / 2.0) - (c.alpha_deg * M_PI / 180.0)) * std::sqrt(gam * c.p_inf / c.rho_inf) * c.mach;
-    e = c.p_inf / (gam - 1.0) + 0.5 * c.rho_inf * (u * u + v * v);
-  } else {
-    u = std::sqrt(gam * c.p_inf / c.rho_inf) * c.mach;
-    v = 0.0;
-    e = c.p_inf / (gam - 1.0) + 0.5 * c.rho_inf * (u * u);
-  }
-  d.P.rinf = c.rho_inf;
-  d.P.uinf = u;
-  d.P.vinf = v;
-  d.P.pinf = c.p_inf;
-  d.P.einf = e;
-  d.P.vx0 = c.vortex_x0;
-  d.P.vy0 = c.vortex_y0;
-  d.P.vbeta = c.vortex_beta;
-  d.P.derive();
+  d.P = make_phys(c);  // freestream as src/airfoil.cpp:79-99
 
-  std::vector<int4> edges, bedges;
-  edge_records(m, edges, bedges);
+  edge_records(m, h_edges, h_bedges);
+  const std::vector<int4> &edges = h_edges, &bedges = h_bedges;
 
   const size_t nq = (size_t)K * Np * 4;
   d.q = (double *)dalloc(nq * 8);
@@ -1298,12 +1300,150 @@ void Solver::enqueue_step_events(cudaStream_t s, cudaEvent_t *ev) {
 
 int Solver::build_graph(std::string &err) {
   if (graph_exec) return 0;
+  const int P = step_parts_for(K);
+  if (P > 1) {
+    if (int rc = build_parts(P, err)) return rc;
+  } else {
+    parts = 1;
+  }
   CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-  enqueue_step(stream);
+  if (parts > 1) enqueue_step_parts(stream);
+  else enqueue_step(stream);
   cudaError_t ce = cudaStreamEndCapture(stream, &graph);
   if (ce != cudaSuccess) { err = std::string("graph capture: ") + cudaGetErrorString(ce); return -6; }
   CK(cudaGraphInstantiate(&graph_exec, graph, 0));
   return 0;
+}
+
+// ---------------------------------------------------------------- the step as a DAG of cell ranges
+// The cells are cut into P ranges of whole 32-cell tiles; every face goes to the range of its
+// higher cell (a boundary face to its cell's).  Per stage, range p has a face launch F_p (its
+// faces, boundary faces first) and an element launch E_p (its tiles).  F_p reads W of ranges
+// lo_p..p and writes face slots of the same cells; E_p reads the face slots of its cells, written
+// by F_p..F_hi_p, and writes W (and q) of its own cells.  So
+//   F_p(s) after E_q(s-1), q in lo_p..p  (W it reads is final; the slots it writes are consumed)
+//   E_p(s) after F_q(s),   q in p..hi_p  (its slots are written; nobody still reads its old W)
+// and nothing else: E_p of stage s can run while later ranges are still in their face launches,
+// and F_p of stage s+1 while later ranges are still in their element launches.  The face kernel
+// is FP64 bound and the element kernel latency bound, so the two overlap on the SMs.  Each
+// launch computes exactly what the one-range step computes for its faces and tiles (every face
+// slot has one writer), so the result is bitwise the same for every P.  With a mesh numbered
+// with locality (O-grid rings, square rows) lo_p and hi_p are p-1 and p+1.
+static int g_step_parts = 0;  // 0: automatic (step_parts_for), 1: the single-range chain
+
+int step_parts_for(int K) {
+  const int T = (K + 31) / 32;
+  if (g_step_parts >= 1) return std::max(1, std::min(g_step_parts, std::min(kMaxStepParts, T)));
+  // automatic: ranges of at least 128 tiles, at most 8
+  return std::max(1, std::min(8, T / 128));
+}
+
+void set_step_parts(int p) { g_step_parts = (p >= 0 && p <= kMaxStepParts) ? p : 0; }
+int step_parts() { return g_step_parts; }
+
+int Solver::build_parts(int P, std::string &err) {
+  const int T = (K + 31) / 32, N = cfg.N, Nfp = N + 1;
+  ptile0.assign(P + 1, 0);
+  for (int p = 0; p <= P; p++) ptile0[p] = (int)((long long)T * p / P);
+  auto part_of = [&](int c) {  // the range holding cell c
+    const int t = c / 32;
+    int p = (int)((long long)t * P / T);
+    while (p + 1 <= P - 1 && ptile0[p + 1] <= t) p++;
+    while (p > 0 && ptile0[p] > t) p--;
+    return p;
+  };
+  std::vector<std::vector<int4>> eb(P), bb(P);
+  plo.assign(P, 0);
+  phi.assign(P, 0);
+  for (int p = 0; p < P; p++) plo[p] = phi[p] = p;
+  for (const int4 &e : h_edges) {
+    const int pl = part_of(e.x), pr = part_of(e.y), q = std::max(pl, pr);
+    eb[q].push_back(e);
+    plo[q] = std::min(plo[q], std::min(pl, pr));
+    phi[pl] = std::max(phi[pl], q);
+    phi[pr] = std::max(phi[pr], q);
+  }
+  for (const int4 &b : h_bedges) bb[part_of(b.x)].push_back(b);
+  std::vector<int4> es, bs;
+  pe0.assign(P + 1, 0);
+  pb0.assign(P + 1, 0);
+  for (int p = 0; p < P; p++) {
+    pe0[p] = (int)es.size();
+    pb0[p] = (int)bs.size();
+    es.insert(es.end(), eb[p].begin(), eb[p].end());
+    bs.insert(bs.end(), bb[p].begin(), bb[p].end());
+  }
+  pe0[P] = (int)es.size();
+  pb0[P] = (int)bs.size();
+  if (!pedges) {
+    pedges = (int4 *)dalloc(sizeof(int4) * std::max<size_t>(1, es.size()));
+    pbedges = (int4 *)dalloc(sizeof(int4) * std::max<size_t>(1, bs.size()));
+    pbxy = (double *)dalloc((size_t)std::max<size_t>(1, bs.size()) * Nfp * 2 * 8);
+    if (!pedges || !pbedges || !pbxy) { err = "cudaMalloc failed"; return -101; }
+  }
+  if (!es.empty()) CK(cudaMemcpyAsync(pedges, es.data(), sizeof(int4) * es.size(), cudaMemcpyHostToDevice, stream));
+  if (!bs.empty()) {
+    CK(cudaMemcpyAsync(pbedges, bs.data(), sizeof(int4) * bs.size(), cudaMemcpyHostToDevice, stream));
+    Inst db = d;
+    db.bedges = pbedges;
+    DG_DISPATCH(N, (bxy_kernel<NN><<<(db.nB * Nfp + 127) / 128, 128, 0, stream>>>(db, coords_d, cells_d, pbxy)));
+    CK(cudaGetLastError());
+  }
+  while ((int)pstreams.size() < P) {
+    cudaStream_t st = nullptr;
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    pstreams.push_back(st);
+  }
+  while ((int)pevents.size() < 6 * P + 1) {
+    cudaEvent_t ev = nullptr;
+    CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    pevents.push_back(ev);
+  }
+  CK(cudaStreamSynchronize(stream));
+  parts = P;
+  return 0;
+}
+
+// Kernel launches of one step of the graph built (or to be built) for this solver.
+int Solver::kernels_per_step() const {
+  const int P = parts ? parts : step_parts_for(K);
+  if (P <= 1) return 7;
+  if (!parts) return 6 * P + 1;  // every range has faces on any mesh of this size
+  int n = 3 * P + 1;
+  for (int p = 0; p < P; p++) n += (pe0[p + 1] - pe0[p] + pb0[p + 1] - pb0[p] > 0) ? 3 : 0;
+  return n;
+}
+
+void Solver::enqueue_step_parts(cudaStream_t s) {
+  const int P = parts, Nfp = cfg.N + 1;
+  cudaEvent_t fork = pevents[6 * P];
+  auto evF = [&](int st, int p) { return pevents[(2 * st) * P + p]; };
+  auto evE = [&](int st, int p) { return pevents[(2 * st + 1) * P + p]; };
+  cudaEventRecord(fork, s);
+  for (int p = 0; p < P; p++) cudaStreamWaitEvent(pstreams[p], fork, 0);
+  for (int stage = 0; stage < 3; stage++) {
+    for (int p = 0; p < P; p++) {
+      cudaStream_t ps = pstreams[p];
+      if (stage > 0)
+        for (int q = plo[p]; q < p; q++) cudaStreamWaitEvent(ps, evE(stage - 1, q), 0);
+      Inst dp = d;
+      dp.edges = pedges + pe0[p];
+      dp.nE = pe0[p + 1] - pe0[p];
+      dp.bedges = pbedges + pb0[p];
+      dp.nB = pb0[p + 1] - pb0[p];
+      dp.bxy = pbxy + (size_t)pb0[p] * Nfp * 2;
+      if (dp.nE + dp.nB > 0) DG_DISPATCH(cfg.N, launch_face<NN>(dp, stage, ps));
+      cudaEventRecord(evF(stage, p), ps);
+    }
+    for (int p = 0; p < P; p++) {
+      cudaStream_t ps = pstreams[p];
+      for (int q = p + 1; q <= phi[p]; q++) cudaStreamWaitEvent(ps, evF(stage, q), 0);
+      DG_DISPATCH(cfg.N, launch_elem_range<NN>(d, stage, ptile0[p], ptile0[p + 1], ps));
+      cudaEventRecord(evE(stage, p), ps);
+    }
+  }
+  for (int p = 0; p < P; p++) cudaStreamWaitEvent(s, evE(2, p), 0);
+  launch_pdl(finalize_kernel, dim3(1), dim3(32), 0, s, d.st, d.dt_mode, d.dt_hist, d.dt_hist_len);
 }
 
 int Solver::step_io(const double *q_in, double *q_out, std::string &err) {

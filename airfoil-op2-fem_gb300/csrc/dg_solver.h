@@ -73,6 +73,13 @@ double tc_round(long long th, long long tl, int sc);
 void set_face_block(int b);
 // Programmatic dependent launch of the plain path's face and element kernels (default on).
 void set_pdl(int on);
+// Cell ranges of the step graph (Solver::build_graph): 0 automatic, 1 one range (a chain of
+// launches), P > 1 a DAG of P ranges whose face and element launches overlap.  Applies to
+// graphs built from now on.
+constexpr int kMaxStepParts = 32;
+void set_step_parts(int p);
+int step_parts();
+int step_parts_for(int K);
 
 struct Solver {
   Config cfg;
@@ -93,6 +100,17 @@ struct Solver {
   void enqueue_step(cudaStream_t s);
   void enqueue_step_events(cudaStream_t s, cudaEvent_t *ev);
   int build_graph(std::string &err);
+  // The step graph as a DAG of cell ranges (build_graph with more than one range).
+  std::vector<int4> h_edges, h_bedges;  // device edge records in mesh order (host copy)
+  int parts = 0;                         // ranges of the graph built (0: none yet)
+  int4 *pedges = nullptr, *pbedges = nullptr;  // edge records sorted by range
+  double *pbxy = nullptr;                // boundary node coordinates in that order
+  std::vector<int> ptile0, pe0, pb0, plo, phi;
+  std::vector<cudaStream_t> pstreams;
+  std::vector<cudaEvent_t> pevents;
+  int build_parts(int P, std::string &err);
+  void enqueue_step_parts(cudaStream_t s);
+  int kernels_per_step() const;
   int step(int nsteps, bool use_graph, std::string &err);
   // One step with host buffers at either end (either may be null): q_in is uploaded first; the
   // last element kernel runs as kOutChunks ranges of tiles on streams of falling priority and

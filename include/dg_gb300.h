@@ -86,8 +86,13 @@ int dg_solver_create(const dg_config_t *cfg, const dg_mesh_t *mesh, dg_solver_t 
 /* set_ic + calc_dt (src/airfoil.cpp:224-237). */
 int dg_solver_init(dg_solver_t *s);
 /* Enqueue nsteps SSPRK3 steps (src/airfoil.cpp:252-334) on the solver's stream; returns
- * without waiting.  Each step is one launch of a captured CUDA graph. */
+ * without waiting.  Each step is one launch of a captured CUDA graph (built on the first call):
+ * the face and element kernels of the three stages over P ranges of cells (dg_set_step_parts),
+ * each range's launches depending only on the launches whose cells they share, so that ranges
+ * in different stages overlap on the GPU; bitwise the same result for every P. */
 int dg_solver_run(dg_solver_t *s, int nsteps);
+/* Kernel launches of one dg_solver_run step for this solver (7 with one range). */
+int dg_solver_kernels_per_step(dg_solver_t *s);
 /* Wait for the solver's stream; DG_ERR_NONPHYSICAL if the density guard fired. */
 int dg_solver_sync(dg_solver_t *s);
 /* Copy a dat to/from the host: "q", "workingQ" ([K][Np][4]), "geo" ([K][16], get only). */
@@ -302,6 +307,11 @@ int dg_tc_operator_digits(int N, int *dims, double *S, int *fexp, int *digits);
  * device runs.  *out = (th * 2^32 + tl) * 2^sc rounded to the nearest double, ties to even, for
  * |th| < 2^41, |tl| < 2^49 (the joined level sums) and -1022 <= sc <= 900; DG_ERR_ARG outside. */
 int dg_tc_round(long long th, long long tl, int sc, double *out);
+/* Cell ranges of the step graph for solvers whose graph is built from now on: 0 automatic (the
+ * default: ranges of at least 128 tiles of 32 cells, at most 8), 1 a single range (the seven
+ * launches as one chain), 2..32 that many ranges (fewer if the mesh has fewer tiles). */
+void dg_set_step_parts(int parts);
+int dg_step_parts(void);
 /* Threads per face-kernel block of the plain path (32..256, multiple of 32; default 64). */
 void dg_set_face_block(int threads);
 /* Launch the plain path's face and element kernels with programmatic dependent launch (1, the
