@@ -140,6 +140,7 @@ def lib():
         "dg_batch_uses_graph": (C.c_int, [vp]),
         "dg_batch_use_shape": (C.c_int, [vp, C.c_int, C.c_int]),
         "dg_batch_inject_barrier_timeout": (C.c_int, [vp]),
+        "dg_batch_tried": (C.c_int, [vp, C.c_int, ip, ip, dp]),
         "dg_batch_stream": (vp, [vp]),
         "dg_batch_free": (None, [vp]),
         "dg_batch_last_error": (cp, []),
@@ -158,8 +159,11 @@ def lib():
         "dg_adjoint_last_error": (cp, []),
         "dg_order_tables_loaded": (C.c_int, [C.c_int, C.c_int]),
         "dg_solver_kernels_per_step": (C.c_int, [vp]),
+        "dg_bf16_mma_peak_gflops": (C.c_double, []),
         "dg_set_step_parts": (None, [C.c_int]),
         "dg_step_parts": (C.c_int, []),
+        "dg_set_step_graph_flags": (None, [C.c_int]),
+        "dg_step_graph_flags": (C.c_int, []),
         "dg_boundary_state": (C.c_int, [C.POINTER(Config), C.c_int, C.c_int, dp, dp, dp]),
         "dg_boundary_state_error": (cp, []),
         "dg_rhs_noalloc_ready": (C.c_int, [C.c_int]),
@@ -452,6 +456,16 @@ class Batch:
         """Select a launch shape without timing (variant BATCH_GROUPED for grouped launches)."""
         self._check(lib().dg_batch_use_shape(self.h, variant, face_tile))
 
+    def tried(self):
+        """Every shape the last autotune timed: [(variant, face_tile, ms_per_step, kind)]."""
+        n = lib().dg_batch_tried(self.h, -1, None, None, None)
+        out = []
+        for i in range(max(0, n)):
+            v, f, ms = C.c_int(), C.c_int(), C.c_double()
+            lib().dg_batch_tried(self.h, i, C.byref(v), C.byref(f), C.byref(ms))
+            out.append((v.value, f.value, ms.value, "grouped" if v.value == BATCH_GROUPED else "persistent"))
+        return out
+
     @property
     def stream(self):
         return lib().dg_batch_stream(self.h)
@@ -677,6 +691,10 @@ def l2_flush(stream):
 
 def fp64_peak_gflops():
     return lib().dg_fp64_peak_gflops()
+
+
+def bf16_mma_peak_gflops():
+    return lib().dg_bf16_mma_peak_gflops()
 
 
 def fp64_mma_peak_gflops():

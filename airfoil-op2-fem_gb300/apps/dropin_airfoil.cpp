@@ -1,10 +1,13 @@
 // A C++ application of the OP2 drop-in (include/op2_gb300.h): the airfoil app's declarations
 // and loop sequence (src/airfoil.cpp:135-334) written against the OP2 API, with op_arg passed
-// by value exactly as a translated driver (src/airfoil_op.cpp) passes it.  Test driver for
-// tests/test_gpu_dropin_cpp.py: reads a mesh, operator tables and freestream constants from a
-// binary file, runs `iters` SSPRK3 steps and writes q and the dt of each step.
+// by value exactly as a translated driver (src/airfoil_op.cpp) passes it: what a user who links
+// libdg_gb300.so in place of an OP2 backend runs.  Reads a mesh, operator tables and freestream
+// constants from a binary file (dropin_app.py writes it), runs `iters` SSPRK3 steps, writes q
+// and the dt of each step, and prints its wall-clock times: from the first declaration (host
+// arrays in) to op_fetch_data (q out), and of the step loop alone.
 //
 //   dropin_airfoil <input> <output>
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -55,6 +58,8 @@ int main(int argc, char **argv) {
   read_into(in, FMASK, 3 * (size_t)Nfp);
   std::fclose(in);
 
+  using clk = std::chrono::steady_clock;
+  const auto t_begin = clk::now();
   op_init(argc, argv, 2);
   op_set nodes = op_decl_set(nn, "nodes");
   op_set cells = op_decl_set(nc, "cells");
@@ -118,6 +123,7 @@ int main(int argc, char **argv) {
   };
   double dt = calc_dt();
   std::vector<double> dts;
+  const auto t_steps = clk::now();  // calc_dt's OP_MAX returned: the set-up loops are done
   for (int it = 0; it < iters; it++) {
     dts.push_back(dt);
     for (int j = 0; j < 3; j++) {
@@ -157,9 +163,14 @@ int main(int argc, char **argv) {
                          op_arg_dat(workingQ, -1, OP_ID, d4, "double", OP_WRITE));
     dt = calc_dt();
   }
+  const auto t_loop_end = clk::now();  // the last calc_dt's OP_MAX returned: every step is done
   std::vector<double> qh((size_t)nc * d4);
   op_fetch_data(q, qh.data());
+  const auto t_end = clk::now();
   op_timing_output();
+  std::printf("dropin_timing total_s=%.9f steps_s=%.9f iters=%d\n",
+              std::chrono::duration<double>(t_end - t_begin).count(),
+              std::chrono::duration<double>(t_loop_end - t_steps).count(), iters);
   op_exit();
   FILE *out = std::fopen(argv[2], "wb");
   if (!out) return 2;

@@ -197,10 +197,120 @@ struct AlphaSens {
   double dru, drv, dE;  // d(rho u)/d alpha, d(rho v)/d alpha, dE/d alpha
 };
 
-// Adds to qmb the adjoint of the interior state through the ghost state of types 0..2
-// (src/get_bedge_q.h:23-50) and returns qbb . d(ghost)/d(alpha).
-__device__ __forceinline__ double bc_state_adj(const int type, const double nx, const double ny, const double qbb[4],
-                                               const AlphaSens &S, double qmb[4]) {
+// Reverse sweep of the characteristic farfield ghost state (farfield_state, dg_device.cuh):
+// adds (d qb / d qi)^T qbb to qmb and returns qbb . d qb / d alpha (alpha enters through the
+// freestream velocity (u_inf, v_inf) = |V| (cos a, sin a); rho_inf, p_inf, c_inf and E_inf do not
+// depend on it).  The branch (supersonic inflow / outflow, subsonic outflow or inflow) is the one
+// the forward evaluation took at qi.
+__device__ __forceinline__ double farfield_state_adj(const double qi[4], const double nx, const double ny,
+                                                     const Phys &P, const double qbb[4], const AlphaSens &S,
+                                                     double qmb[4]) {
+  // forward sweep (farfield_state, same operations)
+  const double rhoi = qi[0], ir = rcp(rhoi);
+  const double ui = qi[1] * ir, vi = qi[2] * ir;
+  const double pi = P.gm1 * fma(-0.5, fma(qi[1], ui, qi[2] * vi), qi[3]);
+  const double c2s = P.gam * pi * ir;
+  const double c2i = fabs(c2s);
+  const double rci = rsqrt(c2i), ci = c2i * rci;
+  const double vni = fma(ui, nx, vi * ny);
+  const double irinf = rcp(P.rinf);
+  const double duinf = S.dru * irinf, dvinf = S.drv * irinf;  // d u_inf / d alpha, d v_inf / d alpha
+  if (vni <= -ci) return qbb[1] * S.dru + qbb[2] * S.drv + qbb[3] * S.dE;
+  if (vni >= ci) {
+    for (int k = 0; k < 4; k++) qmb[k] += qbb[k];
+    return 0.0;
+  }
+  const double vninf = fma(P.uinf, nx, P.vinf * ny);
+  const double rp = fma(P.tgm1, ci, vni);
+  const double rm = fma(-P.tgm1, P.cinf, vninf);
+  const double vnb = 0.5 * (rp + rm);
+  const double cb = 0.25 * P.gm1 * (rp - rm);
+  const bool out = vnb > 0.0;
+  const double rho_u = out ? rhoi : P.rinf;
+  const double rc_u = out ? rci : P.rcinf;
+  const double acb = fabs(cb);
+  const double ratio = acb * rc_u;
+  double pw, dpow;  // ratio^k (k = 2 / (gam - 1)) and its derivative
+  if (P.pow5) {
+    const double r2 = ratio * ratio, r4 = r2 * r2;
+    pw = r4 * ratio;
+    dpow = 5.0 * r4;
+  } else {
+    pw = pow(ratio, P.tgm1);
+    dpow = P.tgm1 * pow(ratio, P.tgm1 - 1.0);
+  }
+  const double rhob = rho_u * pw;
+  const double ut = out ? fma(-vni, nx, ui) : fma(-vninf, nx, P.uinf);
+  const double vt = out ? fma(-vni, ny, vi) : fma(-vninf, ny, P.vinf);
+  const double ub = fma(vnb, nx, ut), vb = fma(vnb, ny, vt);
+  // reverse sweep
+  // qb = (rhob, rhob ub, rhob vb, pb / (gam - 1) + rhob (ub^2 + vb^2) / 2), pb = rhob cb^2 / gam
+  double rhobb = qbb[0] + qbb[1] * ub + qbb[2] * vb + qbb[3] * 0.5 * fma(ub, ub, vb * vb);
+  const double ubb = (qbb[1] + qbb[3] * ub) * rhob, vbb = (qbb[2] + qbb[3] * vb) * rhob;
+  const double pbb = qbb[3] * P.igm1;
+  rhobb += pbb * cb * cb * P.igam;
+  double cbb = pbb * 2.0 * rhob * cb * P.igam;
+  // ub = vnb nx + ut, vb = vnb ny + vt
+  double vnbb = ubb * nx + vbb * ny;
+  const double utb = ubb, vtb = vbb;
+  // rhob = rho_u ratio^k, ratio = |cb| rc_u
+  const double rho_ub = rhobb * pw;
+  const double ratiob = rhobb * rho_u * dpow;
+  cbb += ratiob * rc_u * (cb < 0.0 ? -1.0 : 1.0);
+  const double rc_ub = ratiob * acb;
+  double rhoib = 0.0, uib = 0.0, vib = 0.0, vnib = 0.0, rcib = 0.0, uinfb = 0.0, vinfb = 0.0, vninfb = 0.0;
+  if (out) {
+    rhoib += rho_ub;
+    rcib += rc_ub;
+    uib += utb;
+    vib += vtb;
+    vnib -= utb * nx + vtb * ny;
+  } else {
+    uinfb += utb;
+    vinfb += vtb;
+    vninfb -= utb * nx + vtb * ny;
+  }
+  // vnb = (rp + rm) / 2, cb = (gam - 1) (rp - rm) / 4
+  const double rpb = 0.5 * vnbb + 0.25 * P.gm1 * cbb;
+  const double rmb = 0.5 * vnbb - 0.25 * P.gm1 * cbb;
+  vninfb += rmb;                          // rm = vninf - 2 c_inf / (gam - 1)
+  const double cib = P.tgm1 * rpb;        // rp = vni + 2 ci / (gam - 1)
+  vnib += rpb;
+  uinfb += vninfb * nx;
+  vinfb += vninfb * ny;
+  uib += vnib * nx;
+  vib += vnib * ny;
+  // ci = c2i rci = sqrt(c2i), rci = c2i^(-1/2), c2i = |gam pi / rhoi|
+  //   d ci / d c2i = rci / 2, d rci / d c2i = -rci^3 / 2
+  const double c2ib = 0.5 * (cib - rcib * rci * rci) * rci * (c2s < 0.0 ? -1.0 : 1.0);
+  const double pib = c2ib * P.gam * ir;
+  double irb = c2ib * P.gam * pi;
+  // pi = (gam - 1) (q3 - (q1 ui + q2 vi) / 2)
+  double q1b = 0.0, q2b = 0.0, q3b = pib * P.gm1;
+  const double kk = -0.5 * P.gm1 * pib;
+  q1b += kk * ui;
+  uib += kk * qi[1];
+  q2b += kk * vi;
+  vib += kk * qi[2];
+  // ui = q1 ir, vi = q2 ir, ir = 1 / rhoi
+  q1b += uib * ir;
+  q2b += vib * ir;
+  irb += uib * qi[1] + vib * qi[2];
+  rhoib -= irb * ir * ir;
+  qmb[0] += rhoib;
+  qmb[1] += q1b;
+  qmb[2] += q2b;
+  qmb[3] += q3b;
+  return uinfb * duinf + vinfb * dvinf;
+}
+
+// Adds to qmb the adjoint of the interior state qi through the ghost state of types 0..2
+// (src/get_bedge_q.h:23-50) and 3 (the characteristic farfield) and returns
+// qbb . d(ghost)/d(alpha).
+__device__ __forceinline__ double bc_state_adj(const int type, const double qi[4], const double nx, const double ny,
+                                               const double qbb[4], const Phys &P, const AlphaSens &S,
+                                               double qmb[4]) {
+  if (type == 3) return farfield_state_adj(qi, nx, ny, P, qbb, S, qmb);
   if (type == 0) return qbb[1] * S.dru + qbb[2] * S.drv + qbb[3] * S.dE;
   if (type == 1) {
     qmb[3] += qbb[3];
@@ -512,7 +622,7 @@ __global__ void __launch_bounds__(256) adj_face_kernel(const Inst d, const doubl
     } else {
       bc_state(type, qm, nx, ny, P, qp);
       roe_flux2_adj(qm, qp, nx, ny, P, fb, qmb, qpb);
-      galpha[tid] += ascale * bc_state_adj(type, nx, ny, qpb, S, qmb);
+      galpha[tid] += ascale * bc_state_adj(type, qm, nx, ny, qpb, P, S, qmb);
     }
     st2(tracebar + sl, qmb[0], qmb[1]);
     st2(tracebar + sl + 2, qmb[2], qmb[3]);
@@ -714,9 +824,6 @@ struct Adjoint {
 
   int create(const Config &c, const Mesh &m, int nsteps_, int navg_, int C_, std::string &err) {
     if (c.app != 0 && c.app != 1) { err = "app must be 0 (airfoil) or 1 (vortex)"; return -1; }
-    if (c.app == 0)
-      for (int t : m.bedge_type)
-        if (t == 3) { err = "the adjoint supports boundary types 0, 1, 2 (no characteristic farfield)"; return -1; }
     if (nsteps_ < 1 || navg_ < 1 || navg_ > nsteps_ || C_ < 1) { err = "bad step counts"; return -1; }
     cfg = c;
     mesh = m;

@@ -69,6 +69,29 @@ __global__ void dmma_peak_kernel(double *out, int iters, double a, double b) {
   out[blockIdx.x * blockDim.x + threadIdx.x] = acc;
 }
 
+// bf16 tensor-core throughput probe for the warp-level mma.sync.m16n8k16 (f32 accumulate) the
+// element kernel's contraction issues: four independent accumulator chains per warp.  4096 flops
+// per mma.
+__global__ void bf16_mma_peak_kernel(float *out, int iters, uint32_t a0, uint32_t b0) {
+  float c[4][4];
+  for (int k = 0; k < 4; k++)
+    for (int j = 0; j < 4; j++) c[k][j] = 0.0f;
+  const uint32_t a[4] = {a0, a0 ^ threadIdx.x, a0, a0 ^ 1u};
+  const uint32_t b[2] = {b0, b0 ^ threadIdx.x};
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+      asm volatile(
+          "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+          "{%0,%1,%2,%3};"
+          : "+f"(c[k][0]), "+f"(c[k][1]), "+f"(c[k][2]), "+f"(c[k][3])
+          : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+  }
+  float acc = 0.0f;
+  for (int k = 0; k < 4; k++) acc += c[k][0] + c[k][1] + c[k][2] + c[k][3];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = acc;
+}
+
 template <class F>
 double time_peak(F launch, double flops) {
   cudaEvent_t a, b;
@@ -630,9 +653,25 @@ double dg_fp64_mma_peak_gflops(void) {
   cudaFree(out);
   return g;
 }
+double dg_bf16_mma_peak_gflops(void) {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return -1.0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = sms * 4, threads = 256, iters = 4096;
+  float *out = nullptr;
+  if (cudaMalloc(&out, sizeof(float) * blocks * threads) != cudaSuccess) return -1.0;
+  const double warps = (double)blocks * threads / 32;
+  // bf16 1.0 = 0x3F80 in both halves: small values, no overflow over the iterations
+  const double g = time_peak([&] { bf16_mma_peak_kernel<<<blocks, threads>>>(out, iters, 0x3F803F80u, 0x3C003C00u); },
+                             4096.0 * 4 * iters * warps);
+  cudaFree(out);
+  return g;
+}
 int dg_kernels_per_step(void) { return 7; }
 void dg_set_step_parts(int parts) { dg::set_step_parts(parts); }
 int dg_step_parts(void) { return dg::step_parts(); }
+void dg_set_step_graph_flags(int flags) { dg::set_step_graph_flags(flags); }
+int dg_step_graph_flags(void) { return dg::step_graph_flags(); }
 void dg_set_elem_variant(int variant) { dg::set_elem_variant(variant); }
 int dg_elem_variant(void) { return dg::elem_variant(); }
 

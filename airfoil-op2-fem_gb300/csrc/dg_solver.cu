@@ -807,6 +807,10 @@ static int g_face_block = 64;
 // serialisation (each may start while its predecessor drains), 0: plain stream order.
 static int g_pdl = 1;
 
+// Scheduling priority given to the launches made while g_launch_prio_on is set (the step graph
+// over cell ranges sets it per range; lower numbers are scheduled first).
+static int g_launch_prio_on = 0, g_launch_prio = 0;
+
 template <class... KArgs, class... Args>
 static void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
                        Args... args) {
@@ -815,11 +819,20 @@ static void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t s
   cfg.blockDim = block;
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchAttribute attr[2];
+  int na = 0;
+  if (g_pdl) {
+    attr[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[na].val.programmaticStreamSerializationAllowed = 1;
+    na++;
+  }
+  if (g_launch_prio_on) {
+    attr[na].id = cudaLaunchAttributePriority;
+    attr[na].val.priority = g_launch_prio;
+    na++;
+  }
   cfg.attrs = attr;
-  cfg.numAttrs = g_pdl ? 1 : 0;
+  cfg.numAttrs = na;
   cudaLaunchKernelEx(&cfg, kernel, args...);
 }
 
@@ -1311,7 +1324,8 @@ int Solver::build_graph(std::string &err) {
   else enqueue_step(stream);
   cudaError_t ce = cudaStreamEndCapture(stream, &graph);
   if (ce != cudaSuccess) { err = std::string("graph capture: ") + cudaGetErrorString(ce); return -6; }
-  CK(cudaGraphInstantiate(&graph_exec, graph, 0));
+  const unsigned long long flags = (parts > 1 && (g_step_graph_flags & 2)) ? cudaGraphInstantiateFlagUseNodePriority : 0;
+  CK(cudaGraphInstantiate(&graph_exec, graph, flags));
   return 0;
 }
 
@@ -1330,6 +1344,11 @@ int Solver::build_graph(std::string &err) {
 // slot has one writer), so the result is bitwise the same for every P.  With a mesh numbered
 // with locality (O-grid rings, square rows) lo_p and hi_p are p-1 and p+1.
 static int g_step_parts = 0;  // 0: automatic (step_parts_for), 1: the single-range chain
+// bit 0: launch the ranges' kernels without programmatic dependent launch; bit 1: give range p's
+// launches a scheduling priority that falls with p (earlier ranges first).
+static int g_step_graph_flags = 0;
+void set_step_graph_flags(int f) { g_step_graph_flags = f & 3; }
+int step_graph_flags() { return g_step_graph_flags; }
 
 int step_parts_for(int K) {
   const int T = (K + 31) / 32;
@@ -1416,6 +1435,15 @@ int Solver::kernels_per_step() const {
 
 void Solver::enqueue_step_parts(cudaStream_t s) {
   const int P = parts, Nfp = cfg.N + 1;
+  const int pdl_saved = g_pdl;
+  if (g_step_graph_flags & 1) g_pdl = 0;
+  int prio_lo = 0, prio_hi = 0;  // least and greatest priority (numerically: hi <= lo)
+  cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+  auto set_prio = [&](int p) {
+    if (!(g_step_graph_flags & 2)) return;
+    g_launch_prio_on = 1;
+    g_launch_prio = prio_hi + (int)((long long)(prio_lo - prio_hi) * p / std::max(1, P - 1));
+  };
   cudaEvent_t fork = pevents[6 * P];
   auto evF = [&](int st, int p) { return pevents[(2 * st) * P + p]; };
   auto evE = [&](int st, int p) { return pevents[(2 * st + 1) * P + p]; };
@@ -1432,18 +1460,23 @@ void Solver::enqueue_step_parts(cudaStream_t s) {
       dp.bedges = pbedges + pb0[p];
       dp.nB = pb0[p + 1] - pb0[p];
       dp.bxy = pbxy + (size_t)pb0[p] * Nfp * 2;
+      set_prio(p);
       if (dp.nE + dp.nB > 0) DG_DISPATCH(cfg.N, launch_face<NN>(dp, stage, ps));
+      g_launch_prio_on = 0;
       cudaEventRecord(evF(stage, p), ps);
     }
     for (int p = 0; p < P; p++) {
       cudaStream_t ps = pstreams[p];
       for (int q = p + 1; q <= phi[p]; q++) cudaStreamWaitEvent(ps, evF(stage, q), 0);
+      set_prio(p);
       DG_DISPATCH(cfg.N, launch_elem_range<NN>(d, stage, ptile0[p], ptile0[p + 1], ps));
+      g_launch_prio_on = 0;
       cudaEventRecord(evE(stage, p), ps);
     }
   }
   for (int p = 0; p < P; p++) cudaStreamWaitEvent(s, evE(2, p), 0);
   launch_pdl(finalize_kernel, dim3(1), dim3(32), 0, s, d.st, d.dt_mode, d.dt_hist, d.dt_hist_len);
+  g_pdl = pdl_saved;
 }
 
 int Solver::step_io(const double *q_in, double *q_out, std::string &err) {
@@ -1917,6 +1950,18 @@ extern "C" int dg_batch_use_shape(dg_batch_t *h, int variant, int face_tile) {
   if (h->b.graph) { cudaGraphDestroy(h->b.graph); h->b.graph = nullptr; }
   h->b.graph_ok = true;
   return 0;
+}
+
+extern "C" int dg_batch_tried(dg_batch_t *h, int i, int *variant, int *face_tile, double *ms_per_step) {
+  if (!h) return batch_fail(DG_ERR_ARG, "null batch");
+  const int n = (int)h->b.tried.size();
+  if (i < 0) return n;
+  if (i >= n) return batch_fail(DG_ERR_ARG, "no such shape");
+  const dg::BatchShape &sh = h->b.tried[i];
+  if (variant) *variant = sh.variant;
+  if (face_tile) *face_tile = sh.face_tile;
+  if (ms_per_step) *ms_per_step = sh.ms_per_step;
+  return n;
 }
 
 extern "C" int dg_batch_uses_graph(dg_batch_t *h) { return h && h->b.graph_exec ? 1 : 0; }

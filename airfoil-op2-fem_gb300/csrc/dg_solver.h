@@ -78,6 +78,10 @@ void set_pdl(int on);
 // graphs built from now on.
 constexpr int kMaxStepParts = 32;
 void set_step_parts(int p);
+// Tuning of that graph: bit 0 no programmatic dependent launch between its kernels, bit 1
+// per-range scheduling priorities (earlier ranges first).
+void set_step_graph_flags(int f);
+int step_graph_flags();
 int step_parts();
 int step_parts_for(int K);
 

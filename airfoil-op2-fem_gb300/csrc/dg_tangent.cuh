@@ -43,6 +43,53 @@ __device__ __forceinline__ Dual rcp(Dual a) {
   return {r, -r * r * a.d};
 }
 __device__ __forceinline__ Dual fabs(Dual a) { return a.v < 0.0 ? -a : a; }
+__device__ __forceinline__ Dual pow(Dual a, double k) { return {::pow(a.v, k), k * ::pow(a.v, k - 1.0) * a.d}; }
+__device__ __forceinline__ double val(double a) { return a; }
+__device__ __forceinline__ double val(Dual a) { return a.v; }
+
+// farfield_state (dg_device.cuh) for a generic scalar, line for line, with the freestream
+// velocity and energy as arguments (they carry the alpha derivative).
+template <class T>
+__device__ __forceinline__ void farfield_state_t(const T qi[4], double nx, double ny, const Phys &P, const T uinf,
+                                                 const T vinf, const T einf, T qb[4]) {
+  const T rhoi = qi[0], ir = rcp(rhoi);
+  const T ui = qi[1] * ir, vi = qi[2] * ir;
+  const T pi = P.gm1 * fma(-0.5, fma(qi[1], ui, qi[2] * vi), qi[3]);
+  const T c2i = fabs(P.gam * pi * ir);
+  const T rci = rsqrt(c2i), ci = c2i * rci;
+  const T vni = fma(ui, nx, vi * ny);
+  if (val(vni) <= -val(ci)) {
+    qb[0] = T{P.rinf}; qb[1] = P.rinf * uinf; qb[2] = P.rinf * vinf; qb[3] = einf;
+    return;
+  }
+  if (val(vni) >= val(ci)) {
+    qb[0] = qi[0]; qb[1] = qi[1]; qb[2] = qi[2]; qb[3] = qi[3];
+    return;
+  }
+  const T vninf = fma(uinf, nx, vinf * ny);
+  const T rp = fma(P.tgm1, ci, vni);
+  const T rm = fma(-P.tgm1, T{P.cinf}, vninf);
+  const T vnb = 0.5 * (rp + rm);
+  const T cb = (0.25 * P.gm1) * (rp - rm);
+  const bool out = val(vnb) > 0.0;
+  const T rho_u = out ? rhoi : T{P.rinf};
+  const T ratio = fabs(cb) * (out ? rci : T{P.rcinf});
+  T rhob;
+  if (P.pow5) {
+    const T r2 = ratio * ratio;
+    rhob = rho_u * (r2 * r2 * ratio);
+  } else {
+    rhob = rho_u * pow(ratio, P.tgm1);
+  }
+  const T ut = out ? fma(-vni, nx, ui) : fma(-vninf, nx, uinf);
+  const T vt = out ? fma(-vni, ny, vi) : fma(-vninf, ny, vinf);
+  const T ub = fma(vnb, nx, ut), vb = fma(vnb, ny, vt);
+  const T pb = rhob * cb * cb * P.igam;
+  qb[0] = rhob;
+  qb[1] = rhob * ub;
+  qb[2] = rhob * vb;
+  qb[3] = fma(pb, P.igm1, 0.5 * rhob * fma(ub, ub, vb * vb));
+}
 
 // roe_flux2 (dg_device.cuh) for a generic scalar, line for line.
 template <class T>
@@ -176,6 +223,10 @@ __global__ void __launch_bounds__(256) tlm_face_kernel(const Inst d, const doubl
       qp[1] = {P.rinf * P.uinf, S.dru * dpar};
       qp[2] = {P.rinf * P.vinf, S.drv * dpar};
       qp[3] = qm[3];
+    } else if (type == 3) {  // characteristic farfield
+      const double irinf = 1.0 / P.rinf;
+      const Dual uinf = {P.uinf, S.dru * irinf * dpar}, vinf = {P.vinf, S.drv * irinf * dpar};
+      tl::farfield_state_t(qm, nx, ny, P, uinf, vinf, Dual{P.einf, S.dE * dpar}, qp);
     } else {  // wall mirror (bc_state type 2)
       const Dual mn = 2.0 * tl::fma(nx, qm[1], ny * qm[2]);
       qp[0] = qm[0];

@@ -26,6 +26,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -73,6 +74,108 @@ def algo_bytes(n):
     """Algorithmic HBM bytes per cell-stage of the fused path: 8 (32 Np/3 + 12 Nfp + 16)."""
     p, f = np_of(n), n + 1
     return 8 * (32 * p / 3 + 12 * f + 16)
+
+
+def elem_bytes(n):
+    """Algorithmic HBM bytes of the element kernel per cell-stage: W read and written
+    (4 Np doubles each), q read in two stages of three and written in one (4 Np each), the face
+    slots read (12 Nfp), the four metrics (and the fscale floats of the dt estimate)."""
+    p, f = np_of(n), n + 1
+    return 8 * (4 * p * (2 + 2 / 3 + 1 / 3) + 12 * f + 4 + 2 / 3)
+
+
+def face_bytes(n):
+    """Algorithmic HBM bytes of the face kernel per face node: the two traces read and the two
+    scaled fluxes written (4 doubles each), the face normal and both fscale, the node indices
+    and the edge record shared by the face's Nfp nodes."""
+    return 8 * (4 * 4 + 4) + 2 * 4 + 16 / (n + 1)
+
+
+def elem_mma(n):
+    """mma.sync.m16n8k16 instructions of the element kernel per 32-cell tile: per parity block,
+    8 row tiles (4 cells x 4 variables) x n-tiles of 8 operator rows x 28 digit products per
+    k-step of 16 slots (orders 3-5); the dense rows at orders 1, 2."""
+    sym = {3: (16, 16, 6, 4), 4: (23, 22, 9, 6), 5: (30, 30, 12, 9)}
+    if n in sym:
+        nue, nuo, nre, nro = sym[n]
+        return 8 * 28 * (((nre + 7) // 8) * ((nue + 15) // 16) + ((nro + 7) // 8) * ((nuo + 15) // 16))
+    if n in (1, 2):
+        p, nk = np_of(n), 2 * np_of(n) + 3 * (n + 1)
+        return 8 * 28 * ((p + 7) // 8) * ((nk + 15) // 16)
+    return 0
+
+
+# FP64-pipe thread instructions per unit (DFMA + DMUL + DADD and the rest of the FP64 pipe's
+# instructions, smsp__thread_inst_executed_pipe_fp64_pred_on.sum per launch over the units the
+# launch processes), counted by ncu on GB300 for the N = 3 kernels of this workload (profiles/
+# fp64_instructions_naca_ogrid_K32768_N3.md).  They are properties of the compiled kernels, like
+# the algorithmic bytes: re-count them when a kernel changes.
+FP64_INST_PER_FACE_NODE = {3: None}
+FP64_INST_PER_CELL_STAGE = {3: None}
+
+
+def roofline(K, nf, face_ms, elem_ms, step_ms, peak_tf, hbm_peak, bf16_mma_tf=None):
+    """Which roof binds, per kernel and for the overlapped step.
+
+    The path is FP64 bound: the FP64 pipe issues one thread instruction per lane slot at the rate
+    of half the DFMA flop peak (DFMA = 2 flops), measured live.  Each kernel's FP64 fraction is
+    its FP64-pipe instructions (per unit, above) over its event-timed duration against that
+    rate; its HBM fraction its algorithmic bytes over the same time against the measured copy
+    bandwidth; the element kernel's tensor fraction its mma flops against the measured mma.sync
+    bf16 rate.  frac is the largest (the binding roof) of the dominant kernel."""
+    N = N_ORDER
+    inst_rate = peak_tf * 1e12 / 2
+    face_s, elem_s = face_ms * 1e-3, elem_ms * 1e-3
+    fi, ei = FP64_INST_PER_FACE_NODE.get(N), FP64_INST_PER_CELL_STAGE.get(N)
+    face_fp64 = fi * nf / face_s / inst_rate if fi else None
+    elem_fp64 = ei * K / elem_s / inst_rate if ei else None
+    face_hbm = face_bytes(N) * nf / face_s * 1e-9 / hbm_peak
+    elem_hbm = elem_bytes(N) * K / elem_s * 1e-9 / hbm_peak
+    tiles = (K + 31) // 32
+    elem_tensor_tf = elem_mma(N) * tiles * 4096 / elem_s * 1e-12
+    elem_tensor = elem_tensor_tf / bf16_mma_tf if bf16_mma_tf else None
+    step_fp64 = ((3 * (fi * nf + ei * K)) / (step_ms * 1e-3) / inst_rate) if (fi and ei) else None
+    dominant = "elem_kernel" if elem_ms >= face_ms else "face_kernel"
+    if dominant == "elem_kernel":
+        roofs = {"fp64": elem_fp64, "hbm": elem_hbm, "tensor": elem_tensor}
+        units, t = K, elem_s
+    else:
+        roofs = {"fp64": face_fp64, "hbm": face_hbm}
+        units, t = nf, face_s
+    bound = max((k for k in roofs if roofs[k] is not None), key=lambda k: roofs[k])
+    if bound == "fp64":
+        per = ei if dominant == "elem_kernel" else fi
+        achieved, peak, unit = per * units / t * 1e-9, inst_rate * 1e-9, "G FP64-pipe thread-inst/s"
+    elif bound == "hbm":
+        per = elem_bytes(N) if dominant == "elem_kernel" else face_bytes(N)
+        achieved, peak, unit = per * units / t * 1e-9, hbm_peak, "GB/s"
+    else:
+        achieved, peak, unit = elem_tensor_tf, bf16_mma_tf, "TFLOP/s"
+    return {
+        "bound": bound, "kernel": dominant, "achieved": achieved, "peak": peak, "unit": unit,
+        "frac": achieved / peak, "traffic": None,
+        "traffic_note": "DRAM bytes need hardware counters: measured by ncu, not in this run (profiles/)",
+        "peak_source": {"fp64": "DFMA peak measured live on this GPU / 2 (instructions)",
+                        "hbm": "MEASURED_PEAKS.json hbm_gbs", "tensor": "mma.sync bf16 measured live"}[bound],
+        "hbm_frac": elem_hbm if dominant == "elem_kernel" else face_hbm,
+        "fp64_pipe_frac": elem_fp64 if dominant == "elem_kernel" else face_fp64,
+        "tensor_pipe_frac": elem_tensor if dominant == "elem_kernel" else 0.0,
+        "face_fp64_pipe_frac": face_fp64, "face_hbm_frac": face_hbm,
+        "elem_fp64_pipe_frac": elem_fp64, "elem_hbm_frac": elem_hbm, "elem_tensor_pipe_frac": elem_tensor,
+        "elem_tensor_tflops": elem_tensor_tf, "bf16_mma_peak_tflops": bf16_mma_tf,
+        "step_fp64_pipe_frac": step_fp64,
+        "step_note": "the graph step overlaps face and element launches of different cell ranges; "
+                     "step_fp64_pipe_frac is both kernels' FP64-pipe instructions over the graph step time",
+        "fp64_inst_per_face_node": fi, "fp64_inst_per_cell_stage": ei,
+        "elem_bytes_per_cell_stage": elem_bytes(N), "face_bytes_per_face_node": face_bytes(N),
+        "elem_flops_fp64_equivalent": elem_flops(N) * K / elem_s * 1e-12,
+        "elem_flops_fp64_equivalent_note": "FP64-equivalent TFLOP/s of the element kernel: this build's count "
+                                           "16Np^2 + 24NpNfp + 52Np = %d per cell-stage (the reference "
+                                           "algorithm's, 32Np^2 + 24NpNfp + 60Np + 330Nfp = %d, covers "
+                                           "the face kernel's Roe flux too); the contraction runs on the "
+                                           "tensor cores, so this is not a fraction of any pipe"
+                                           % (elem_flops(N), survey_flops(N)),
+    }
 
 
 class Clocks:
@@ -183,33 +286,56 @@ def batched_measure(pkg, steps, n_inst=64, seed=20261203):
     b.sync()
     bms = sum(a.elapsed_ms(c) for a, c in evs) / steps
     solvers = [pkg.Solver(m, c).init() for m, c in zip(meshes, cfgs)]
-    for s in solvers:
-        s.run(2)
-    for s in solvers:
-        s.sync()
     psteps = max(3, steps // 4)
-    t0 = time.perf_counter()
-    for _ in range(psteps):
-        for s in solvers:
-            s.run(1)
-        for s in solvers:
-            s.sync()
-    pms = (time.perf_counter() - t0) / psteps * 1e3
-    # the plain path one instance at a time (each instance's steps, then the next)
-    t0 = time.perf_counter()
-    for s in solvers:
-        s.run(psteps)
-        s.sync()
-    sms = (time.perf_counter() - t0) / psteps * 1e3
+    pms, sms = plain_device_times(pkg, solvers, psteps)
     del solvers
+    tried = b.tried()
+    best_persistent = min((t for t in tried if t[3] == "persistent"), key=lambda t: t[2], default=None)
+    best_grouped = min((t for t in tried if t[3] == "grouped"), key=lambda t: t[2], default=None)
     return {"value": 3 * dof / (bms * 1e-3), "unit": "DOF-stage/s", "ms_per_step": bms, "steps": steps,
             "instances": n_inst, "cells": cells, "dof_stage_per_step": 3 * dof, "shape": b.shape(),
             "autotune_ms_per_step": tuned,
-            "plain_same_instances": {"value": 3 * dof / (pms * 1e-3), "ms_per_step": pms,
-                                     "how": "64 plain solvers, each on its own stream, host-timed"},
-            "plain_sequential": {"value": 3 * dof / (sms * 1e-3), "ms_per_step": sms,
-                                 "how": "the 64 plain solvers one after another, host-timed"},
+            "persistent_ms_per_step": best_persistent[2] if best_persistent else None,
+            "grouped_ms_per_step": best_grouped[2] if best_grouped else None,
+            "shapes_timed": len(tried),
+            "plain_concurrent_ms_per_step": pms, "plain_concurrent_value": 3 * dof / (pms * 1e-3),
+            "plain_sequential_ms_per_step": sms, "plain_sequential_value": 3 * dof / (sms * 1e-3),
+            "plain_how": "64 plain solvers (their step graphs); concurrent: each on its own stream, makespan "
+                         "between CUDA events; sequential: sum of each solver's event-timed steps",
             "speedup_vs_plain": pms / bms, "speedup_vs_plain_sequential": sms / bms}
+
+
+def plain_device_times(pkg, solvers, steps):
+    """Device times per step of many plain solvers: all running at once on their own streams
+    (makespan from the first start event to the last end event), and one after another (the
+    sum of each solver's own event-timed steps, host gaps excluded)."""
+    for s_ in solvers:
+        s_.run(2)
+    for s_ in solvers:
+        s_.sync()
+    starts = [pkg.Event() for _ in solvers]
+    ends = [pkg.Event() for _ in solvers]
+    for s_, a in zip(solvers, starts):
+        a.record(s_.stream)
+    for s_ in solvers:
+        s_.run(steps)
+    for s_, b in zip(solvers, ends):
+        b.record(s_.stream)
+    for s_ in solvers:
+        s_.sync()
+    t0 = starts[0]
+    first = min(t0.elapsed_ms(a) for a in starts)
+    last = max(t0.elapsed_ms(b) for b in ends)
+    concurrent = (last - first) / steps
+    seq = 0.0
+    for s_ in solvers:
+        a, b = pkg.Event(), pkg.Event()
+        a.record(s_.stream)
+        s_.run(steps)
+        b.record(s_.stream)
+        s_.sync()
+        seq += a.elapsed_ms(b)
+    return concurrent, seq / steps
 
 
 def batched_small_measure(pkg, steps=100, n_inst=64, seed=20261203):
@@ -233,27 +359,13 @@ def batched_small_measure(pkg, steps=100, n_inst=64, seed=20261203):
     b.sync()
     bms = e0.elapsed_ms(e1) / steps
     solvers = [pkg.Solver(m, c).init() for m, c in zip(meshes, cfgs)]
-    for s_ in solvers:
-        s_.run(2)
-    for s_ in solvers:
-        s_.sync()
-    t0 = time.perf_counter()
-    for s_ in solvers:
-        s_.run(steps)
-    for s_ in solvers:
-        s_.sync()
-    pms = (time.perf_counter() - t0) / steps * 1e3
-    t0 = time.perf_counter()
-    for s_ in solvers:
-        s_.run(steps)
-        s_.sync()
-    sms = (time.perf_counter() - t0) / steps * 1e3
+    pms, sms = plain_device_times(pkg, solvers, steps)
     return {"value": 3 * dof / (bms * 1e-3), "unit": "DOF-stage/s", "ms_per_step": bms, "instances": n_inst,
             "cells": sum(m.size("cells") for m in meshes), "shape": b.shape(),
-            "plain_same_instances": {"value": 3 * dof / (pms * 1e-3), "ms_per_step": pms,
-                                     "how": "64 plain solvers, graph launches on their own streams, host-timed"},
-            "plain_sequential": {"value": 3 * dof / (sms * 1e-3), "ms_per_step": sms,
-                                 "how": "the 64 plain solvers one after another, host-timed"},
+            "outside_config": "not the 64-instance sweep of the benchmark (O-grids 128x32..384x96): 64 small "
+                              "O-grids 32x8..64x16, where the plain path is launch bound",
+            "plain_concurrent_ms_per_step": pms, "plain_concurrent_value": 3 * dof / (pms * 1e-3),
+            "plain_sequential_ms_per_step": sms, "plain_sequential_value": 3 * dof / (sms * 1e-3),
             "speedup_vs_plain": pms / bms, "speedup_vs_plain_sequential": sms / bms}
 
 
@@ -403,6 +515,39 @@ def large_vortex_measure(pkg, n=512, orders=(1, 2, 3, 4, 5), steps=200, n_inst=1
                                                         "rel_diff": abs(g[0] - fd) / max(abs(fd), 1e-300)}}}
 
 
+def dropin_measure(pkg, steps=20):
+    """The OP2 drop-in as its user runs it: the reference's airfoil main loop
+    (src/airfoil.cpp:135-334: declarations from host arrays, the set-up loops, then per step
+    get_neighbour_q, get_bedge_q, euler_rhs (x3), set_workingQ (x2), update_Q and calc_dt with
+    its OP_MAX reduction back to the host) compiled in C++ against include/op2_gb300.h
+    (apps/dropin_airfoil.cpp), on the benchmark's mesh and order (NACA 0012 O-grid 256 x 64,
+    K = 32768, N = 3, M = 0.4) with the reference's own boundary typing (inflow / outflow by
+    x < 0, wall) and dt = 1/dt1 (CFL 1, src/airfoil.cpp:237).  Wall-clock times from the
+    application: from the first declaration to op_fetch_data(q), and the step loop alone."""
+    import importlib
+    import tempfile
+    app = importlib.import_module(pkg.__name__ + ".dropin_app")
+    mesh = pkg.Mesh.naca_ogrid(N_THETA, N_R, farfield="reference")
+    m = mesh.arrays()
+    ops = pkg.operators(N_ORDER)
+    p = {"gam": 1.4, "bc_mach": MACH, "bc_alpha": ALPHA, "bc_p": 1.0, "bc_r": 1.0}
+    p["bc_u"] = math.sqrt(1.4 * 1.0 / 1.0) * MACH
+    p["bc_v"] = 0.0
+    p["bc_e"] = 1.0 / (1.4 - 1.0) + 0.5 * 1.0 * p["bc_u"] ** 2
+    with tempfile.TemporaryDirectory() as wd:
+        exe = app.compile_app(wd, pkg.LIB_PATH)
+        _, _, tm, _ = app.run_app(exe, m, ops, p, 2, wd)  # warm-up run (context, code load)
+        q, dts, tm, _ = app.run_app(exe, m, ops, p, steps, wd)
+    K = mesh.size("cells")
+    dof = 3 * 4 * K * np_of(N_ORDER)
+    return {"value": dof * steps / tm["steps_s"], "unit": "DOF-stage/s", "ms_per_step": tm["steps_s"] / steps * 1e3,
+            "steps": steps, "end_to_end_s": tm["total_s"],
+            "end_to_end_value": dof * steps / tm["total_s"],
+            "loops_per_step": 13, "finite": bool(np.isfinite(q).all()),
+            "how": "C++ application of the OP2 drop-in (host arrays in, op_fetch_data out); value over the step "
+                   "loop, end_to_end from the first op_decl to op_fetch_data"}
+
+
 def run_reference(args):
     """The reference arm: the reference's user kernels (restated; the reference's own build is
     N=4-only and cannot run this N=3 workload) on all host cores."""
@@ -450,10 +595,11 @@ def main():
     ap.add_argument("--batched-steps", type=int, default=20)
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-advection", action="store_true")
+    ap.add_argument("--no-dropin", action="store_true")
+    ap.add_argument("--no-large-vortex", action="store_true",
+                    help="skip the large vortex convergence + 16-instance batched beta gradient (~1 min)")
     ap.add_argument("--adjoint-steps", type=int, default=2000)
     ap.add_argument("--advection-steps", type=int, default=200)
-    ap.add_argument("--large-vortex", action="store_true",
-                    help="also run the large vortex convergence + 16-instance batched beta gradient (~1 min)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -469,6 +615,10 @@ def main():
     import __graft_entry__ as g
     pkg = g.load_package()
     pkg.lib()
+    # clocks sampled over every GPU leg of the run (the main timed region alone is a few ms,
+    # shorter than the sampling interval)
+    clocks = Clocks(local)
+    t_gpu0 = time.perf_counter()
 
     mesh = pkg.Mesh.naca_ogrid(N_THETA, N_R, farfield="characteristic")
     cfg = pkg.config(N=N_ORDER, cfl=CFL, mach=MACH, alpha_deg=ALPHA)
@@ -486,21 +636,21 @@ def main():
     # timed region: device-resident steps, L2 flushed between steps outside the events
     evs = [(pkg.Event(), pkg.Event()) for _ in range(args.steps)]
     barrier(dist)
-    clocks = Clocks(local)
     for i in range(args.steps):
         pkg.l2_flush(stream)
         evs[i][0].record(stream)
         s.run(1)
         evs[i][1].record(stream)
     s.sync()
-    clk = clocks.stop()
     step_ms = [a.elapsed_ms(b) for a, b in evs]
     total_ms = dist_max(dist, sum(step_ms))
     barrier(dist)
     ms_per_step = total_ms / args.steps
     value = world * dof_stage_per_step * args.steps / (total_ms * 1e-3)
+    launches_per_step = s.kernels_per_step()
 
-    # per-kernel durations (same workload, separate launches with events between kernels)
+    # per-kernel durations (same workload, the seven kernels of one step launched one after the
+    # other with events between them: no overlap, so each kernel's own time)
     nk = min(args.steps, 50)
     kt = np.zeros(7)
     for _ in range(nk):
@@ -510,44 +660,15 @@ def main():
     face_ms = float(np.mean(kt[[0, 2, 4]]))
     elem_ms = float(np.mean(kt[[1, 3, 5]]))
     nf = (mesh.size("edges") + mesh.size("bedges")) * (N_ORDER + 1)
-    elem_tf = elem_flops(N_ORDER) * K / (elem_ms * 1e-3) * 1e-12
-    face_tf = face_flops(N_ORDER) * nf / (face_ms * 1e-3) * 1e-12
-    step_tf = survey_flops(N_ORDER) * K / ((face_ms + elem_ms) * 1e-3) * 1e-12
-    dominant = "elem_kernel" if elem_ms >= face_ms else "face_kernel"
-    peak_tf = peak_gflops * 1e-3
+    serial_ms = 3 * (face_ms + elem_ms) + float(kt[6])
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             hbm_peak = float(json.load(f)["hbm_gbs"])
         hbm_src = "measured (MEASURED_PEAKS.json)"
     except (OSError, KeyError, ValueError):
         hbm_peak, hbm_src = 6800.0, "fallback"
-    traffic = None
-    try:  # ncu-measured DRAM bytes per element-kernel launch (stage average), committed profile
-        with open(os.path.join(ROOT, "profiles", "elem_kernel_sym_face_kernel_naca_ogrid_K32768_N3.md")) as f:
-            for ln in f:
-                if ln.startswith("traffic_bytes_per_launch_elem_kernel:"):
-                    traffic = float(ln.split(":")[1])
-    except OSError:
-        traffic = None
-    stage_bytes = algo_bytes(N_ORDER) * K
-    hbm_gbs = stage_bytes / ((face_ms + elem_ms) * 1e-3) * 1e-9
-    # the element kernel in its all-FP64 even/odd form on the same workload, for comparison
-    variant = pkg.lib().dg_elem_variant()
-    elem_ms_fp64 = None
-    if variant >= 2:
-        pkg.lib().dg_set_elem_variant(1)
-        try:
-            s64 = pkg.Solver(mesh, pkg.config(N=N_ORDER, cfl=CFL)).init()
-            k64 = np.zeros(7)
-            for _ in range(3):
-                s64.step_timed()
-            for _ in range(nk):
-                pkg.l2_flush(stream)
-                k64 += s64.step_timed()
-            elem_ms_fp64 = float(np.mean(k64[[1, 3, 5]])) / nk
-            del s64
-        finally:
-            pkg.lib().dg_set_elem_variant(variant)
+    peak_tf = peak_gflops * 1e-3
+    roof = roofline(K, nf, face_ms, elem_ms, ms_per_step, peak_tf, hbm_peak, pkg.bf16_mma_peak_gflops() * 1e-3)
 
     # end to end through the C ABI with pinned host buffers
     nq = K * Np * 4
@@ -574,46 +695,24 @@ def main():
         "config": {"workload": WORKLOAD, "cells": K, "order": N_ORDER, "np": Np,
                    "dof_stage_per_step": dof_stage_per_step, "parallelism": "replicas" if world > 1 else "single",
                    "l2": "flushed between timed steps (512 MB write outside the events)",
-                   "graph": "one CUDA graph launch per step (7 kernels)"},
-        "gpu_launches": 7 * args.steps,
+                   "graph": "one CUDA graph launch per step: %d kernels over %d cell ranges"
+                            % (launches_per_step, (launches_per_step - 1) // 6 if launches_per_step > 7 else 1)},
+        "gpu_launches": launches_per_step * args.steps,
         "nodes_per_s": value / 4,
-        "roofline": {"bound": "fp64", "kernel": dominant, "achieved": elem_tf if dominant == "elem_kernel" else face_tf,
-                     "peak": peak_tf, "unit": "TFLOP/s",
-                     "frac": (elem_tf if dominant == "elem_kernel" else face_tf) / peak_tf,
-                     "traffic": traffic if dominant == "elem_kernel" else None,
-                     "traffic_source": "ncu dram__bytes_read+write per launch, stage average (profiles/)",
-                     "peak_source": "DFMA throughput measured live on this GPU (MEASURED_PEAKS.json has no FP64 figure)",
-                     "elem_form": {3: "even/odd, contraction and butterfly on the bf16 tensor cores (exact integer product)",
-                                   2: "even/odd, contraction on the bf16 tensor cores (exact integer product)",
-                                   1: "even/odd, FP64", 0: "dense FP64"}[variant],
-                     "frac_note": ("FP64-equivalent: algorithmic FP64 flops over the DFMA peak; the contraction "
-                                   "runs on the tensor cores, so frac can exceed 1 (FP64 pipe busy 45-50 % of "
-                                   "active cycles per ncu)") if variant >= 2 else "FP64 flops over the DFMA peak",
-                     "elem_ms_fp64_form": elem_ms_fp64,
-                     "fp64_tensor_peak_tflops": dmma_gflops * 1e-3,
-                     "fp64_tensor_note": "DMMA (mma.sync m8n8k4 f64) measured live; below DFMA and on the same pipe, so unused",
-                     "flops_per_unit": elem_flops(N_ORDER) if dominant == "elem_kernel" else face_flops(N_ORDER),
-                     "unit_def": "cell-stage" if dominant == "elem_kernel" else "face node",
-                     "kernel_ms": {"face": face_ms, "elem": elem_ms, "elem_stage2": float(kt[5]),
-                                   "finalize": float(kt[6])},
-                     "face_kernel_tflops": face_tf,
-                     "step_tflops_survey_count": step_tf,
-                     "hbm": {"achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_gbs / hbm_peak,
-                             "peak_source": hbm_src}},
+        "roofline": roof,
+        "kernel_face_ms": face_ms, "kernel_elem_ms": elem_ms, "kernel_elem_stage2_ms": float(kt[5]),
+        "kernel_finalize_ms": float(kt[6]), "serial_step_ms": serial_ms,
+        "overlap_gain": serial_ms / ms_per_step,
+        "fp64_dfma_peak_tflops": peak_tf, "fp64_mma_peak_tflops": dmma_gflops * 1e-3,
         "e2e": {"value": e2e_value, "unit": "DOF-stage/s", "h2d_bytes_per_step": nq * 8,
                 "d2h_bytes_per_step": nq * 8, "steps": e2e_steps,
                 "call": "dg_solver_step_host (pinned host q in/out, 1 step per call)"},
-        "clocks": clk,
     }
-    if rank == 0 and not args.no_cpu:
-        nthreads = os.cpu_count() or 1
-        rate, secs = cpu_oracle_rate(args.cpu_steps, nthreads)
-        line["cpu_baseline"] = {"value": rate, "unit": "DOF-stage/s", "cores": nthreads, "kind": "port",
-                                "sample": "%d SSPRK3 steps of the full workload (%.1f s)" % (args.cpu_steps, secs)}
-        one_steps = max(1, args.cpu_steps // 16)
-        rate1, secs1 = cpu_oracle_rate(one_steps, 1)
-        line["cpu_baseline"]["single_core"] = {"value": rate1, "cores": 1,
-                                               "sample": "%d steps (%.1f s)" % (one_steps, secs1)}
+    if not args.no_dropin:
+        try:
+            line["dropin"] = dropin_measure(pkg)
+        except (RuntimeError, OSError) as exc:
+            line["dropin"] = {"unavailable": str(exc)[:200]}
     if not args.no_batched:
         line["batched"] = batched_measure(pkg, args.batched_steps)
         line["batched"]["small_instances"] = batched_small_measure(pkg)
@@ -623,8 +722,21 @@ def main():
     if not args.no_advection:
         line["advection"] = advection_measure(pkg, steps=args.advection_steps)
         line["mesh_setup"] = mesh_setup_measure(pkg)
-    if args.large_vortex:
+    if not args.no_large_vortex:
         line["large_vortex"] = large_vortex_measure(pkg)
+    clk = clocks.stop()
+    clk["window_s"] = time.perf_counter() - t_gpu0
+    clk["window"] = "every GPU leg of this run"
+    line["clocks"] = clk
+    if rank == 0 and not args.no_cpu:
+        nthreads = os.cpu_count() or 1
+        rate, secs = cpu_oracle_rate(args.cpu_steps, nthreads)
+        one_steps = max(1, args.cpu_steps // 16)
+        rate1, secs1 = cpu_oracle_rate(one_steps, 1)
+        line["cpu_baseline"] = {"value": rate, "unit": "DOF-stage/s", "cores": nthreads, "kind": "port",
+                                "sample": "%d SSPRK3 steps of the full workload (%.1f s)" % (args.cpu_steps, secs),
+                                "single_core_value": rate1,
+                                "single_core_sample": "%d steps (%.1f s)" % (one_steps, secs1)}
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:

@@ -176,6 +176,9 @@ int dg_batch_shape(dg_batch_t *b, int *variant, int *block, int *face_tile, int 
 int dg_batch_inject_barrier_timeout(dg_batch_t *b);
 /* Use one launch shape (variant as above) without timing. */
 int dg_batch_use_shape(dg_batch_t *b, int variant, int face_tile);
+/* The shapes the last dg_batch_autotune timed: with i < 0 returns their count; else shape i's
+ * variant (99: grouped launches), face tile and ms per step, and the count. */
+int dg_batch_tried(dg_batch_t *b, int i, int *variant, int *face_tile, double *ms_per_step);
 int dg_batch_uses_graph(dg_batch_t *b);
 void *dg_batch_stream(dg_batch_t *b);
 void dg_batch_free(dg_batch_t *b);
@@ -286,6 +289,9 @@ int dg_l2_flush(void *stream);
 double dg_fp64_peak_gflops(void);
 /* Measured FP64 tensor-core (mma.sync m8n8k4 f64) throughput of this GPU, GFLOP/s. */
 double dg_fp64_mma_peak_gflops(void);
+/* Measured bf16 tensor-core throughput of this GPU for mma.sync.m16n8k16 with FP32 accumulation
+ * (the element kernel's contraction instruction), GFLOP/s. */
+double dg_bf16_mma_peak_gflops(void);
 /* Number of kernels one dg_solver_run step launches. */
 int dg_kernels_per_step(void);
 /* Element-kernel form for launches and graphs built from now on: 3 (default) the dense rows
@@ -312,6 +318,11 @@ int dg_tc_round(long long th, long long tl, int sc, double *out);
  * launches as one chain), 2..32 that many ranges (fewer if the mesh has fewer tiles). */
 void dg_set_step_parts(int parts);
 int dg_step_parts(void);
+/* Tuning of that graph for graphs built from now on: bit 0 launches its kernels without
+ * programmatic dependent launch, bit 1 gives range p's launches a scheduling priority falling
+ * with p (earlier ranges scheduled first).  0 by default.  Results are bitwise the same. */
+void dg_set_step_graph_flags(int flags);
+int dg_step_graph_flags(void);
 /* Threads per face-kernel block of the plain path (32..256, multiple of 32; default 64). */
 void dg_set_face_block(int threads);
 /* Launch the plain path's face and element kernels with programmatic dependent launch (1, the

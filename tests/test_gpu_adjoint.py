@@ -12,15 +12,17 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def setup(pkg, N=3, ntheta=32, nr=8, nsteps=60, navg=20, C=7, alpha=2.0, mach=0.5):
-    mesh = pkg.Mesh.naca_ogrid(ntheta, nr, radius=4.0, farfield="reference")
+def setup(pkg, N=3, ntheta=32, nr=8, nsteps=60, navg=20, C=7, alpha=2.0, mach=0.5, farfield="reference"):
+    mesh = pkg.Mesh.naca_ogrid(ntheta, nr, radius=4.0, farfield=farfield)
     cfg = pkg.config(N=N, cfl=0.5, mach=mach, alpha_deg=alpha)
     return mesh, cfg, pkg.LiftObjective(mesh, cfg, nsteps, navg, C)
 
 
-@pytest.mark.parametrize("N", [1, 2, 3, 4, 5, 6])
-def test_rhs_vjp_dot_product(pkg, N):
-    mesh, cfg, obj = setup(pkg, N=N)
+@pytest.mark.parametrize("N,farfield", [(1, "reference"), (2, "reference"), (3, "reference"), (4, "reference"),
+                                        (5, "reference"), (6, "reference"), (2, "characteristic"),
+                                        (3, "characteristic"), (5, "characteristic")])
+def test_rhs_vjp_dot_product(pkg, N, farfield):
+    mesh, cfg, obj = setup(pkg, N=N, farfield=farfield)
     s = pkg.Solver(mesh, cfg).init()
     rng = np.random.default_rng(N)
     q = s.get("q")
@@ -32,7 +34,7 @@ def test_rhs_vjp_dot_product(pkg, N):
     vjp, _ = obj.rhs_vjp(W, v)
     lhs, rhs = np.dot(v, jvp), np.dot(vjp, u)
     assert abs(lhs - rhs) <= 1e-7 * max(abs(lhs), abs(rhs))
-    # alpha: through the inflow/outflow ghost states
+    # alpha: through the inflow/outflow (or characteristic farfield) ghost states
     def rhs_at(alpha):
         c2 = pkg.config(N=N, cfl=0.5, mach=cfg.mach, alpha_deg=alpha)
         return pkg.Solver(mesh, c2).init().rhs(W)
@@ -42,8 +44,9 @@ def test_rhs_vjp_dot_product(pkg, N):
     assert abs(da - ap) <= 1e-6 * max(abs(da), 1e-30)
 
 
-def test_gradient_matches_finite_differences(pkg):
-    mesh, cfg, obj = setup(pkg)
+@pytest.mark.parametrize("farfield", ["reference", "characteristic"])
+def test_gradient_matches_finite_differences(pkg, farfield):
+    mesh, cfg, obj = setup(pkg, farfield=farfield)
     J = obj.forward()
     ga, gq = obj.backward()
     assert obj.evaluate(cfg.alpha_deg) == J  # frozen-dt re-evaluation is the same function
@@ -77,10 +80,32 @@ def test_backward_scales_with_grad_output(pkg):
     assert ga2 == -2.5 * ga1 and np.allclose(gq2, -2.5 * gq1, rtol=0, atol=0)
 
 
-def test_rejects_characteristic_farfield(pkg):
-    mesh = pkg.Mesh.naca_ogrid(32, 8, farfield="characteristic")
-    with pytest.raises(pkg.DGError):
-        pkg.LiftObjective(mesh, pkg.config(N=3), 10, 5)
+def test_farfield_branches_dot_product(pkg):
+    """The reverse sweep of the characteristic farfield in each of its branches: at M 1.3 the
+    circular farfield of the O-grid has supersonic inflow and outflow faces as well as subsonic
+    ones (where |v_n| < c); with every boundary edge of type 3 all four branches are taken."""
+    mesh = pkg.Mesh.naca_ogrid(32, 8, radius=4.0, farfield="characteristic")
+    mesh.set_bedge_type(np.full(mesh.size("bedges"), 3, dtype=np.int32))
+    for mach in (0.5, 1.3):
+        cfg = pkg.config(N=3, cfl=0.5, mach=mach, alpha_deg=10.0)
+        obj = pkg.LiftObjective(mesh, cfg, 10, 5, 5)
+        s = pkg.Solver(mesh, cfg).init()
+        rng = np.random.default_rng(31)
+        q = s.get("q")
+        W = q * (1.0 + 0.05 * rng.standard_normal(q.size))
+        u = q * rng.standard_normal(q.size)
+        v = rng.standard_normal(q.size)
+        h = 1e-6
+        jvp = (s.rhs(W + h * u) - s.rhs(W - h * u)) / (2 * h)
+        vjp, ap = obj.rhs_vjp(W, v)
+        lhs, rhs = np.dot(v, jvp), np.dot(vjp, u)
+        assert abs(lhs - rhs) <= 1e-7 * max(abs(lhs), abs(rhs)), mach
+
+        def rhs_at(alpha):
+            return pkg.Solver(mesh, pkg.config(N=3, cfl=0.5, mach=mach, alpha_deg=alpha)).init().rhs(W)
+        ha = 1e-5
+        da = np.dot(v, (rhs_at(10.0 + ha) - rhs_at(10.0 - ha)) / (2 * ha))
+        assert abs(da - ap) <= 1e-6 * max(abs(da), 1e-30), mach
 
 
 # ---------------------------------------------------------------- isentropic vortex: d/d beta
@@ -147,11 +172,12 @@ def test_vortex_batched_gradient_equals_individual(pkg):
 
 
 # ---------------------------------------------------------------- tangent-linear FP64 run
-def test_tangent_linear_matches_adjoint(pkg):
+@pytest.mark.parametrize("farfield", ["reference", "characteristic"])
+def test_tangent_linear_matches_adjoint(pkg, farfield):
     """Forward-mode derivative (dual numbers through the forward formulas, hand-written ghost
     state and stage tangents) against the reverse-mode gradient: the same discrete derivative
     by two independent routes."""
-    mesh, cfg, obj = setup(pkg)
+    mesh, cfg, obj = setup(pkg, farfield=farfield)
     obj.forward()
     ga, gq = obj.backward()
     ta = obj.tangent(1.0)
