@@ -1324,7 +1324,7 @@ int Solver::build_graph(std::string &err) {
   else enqueue_step(stream);
   cudaError_t ce = cudaStreamEndCapture(stream, &graph);
   if (ce != cudaSuccess) { err = std::string("graph capture: ") + cudaGetErrorString(ce); return -6; }
-  const unsigned long long flags = (parts > 1 && (g_step_graph_flags & 2)) ? cudaGraphInstantiateFlagUseNodePriority : 0;
+  const unsigned long long flags = (parts > 1 && (step_graph_flags() & 2)) ? cudaGraphInstantiateFlagUseNodePriority : 0;
   CK(cudaGraphInstantiate(&graph_exec, graph, flags));
   return 0;
 }
