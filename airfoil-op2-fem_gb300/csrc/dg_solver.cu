@@ -125,7 +125,22 @@ __device__ __forceinline__ void st2(double *p, double a, double b) {
   *reinterpret_cast<double2 *>(p) = make_double2(a, b);
 }
 
+// Asynchronous 16-byte global -> shared copies (cp.async, completion per thread by
+// cp.async.wait_all, then a block barrier for the other threads' copies).  valid = false fills
+// the 16 bytes with zeros and reads nothing.
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, const bool valid) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(sa), "l"(gmem), "r"(valid ? 16 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 #include "dg_ozaki.cuh"
+
+// Orders whose element kernels keep each node's W and q for the stage combine in shared memory
+// (copied there while the tile is staged) instead of reading them again from HBM after the
+// contraction.  At N = 1, 2 the extra shared memory would cost resident blocks.
+constexpr bool elem_staged(int N) { return N >= 3; }
 
 // ---------------------------------------------------------------- face kernel
 // One face node (tid in [0, (nB + nE) * Nfp)): boundary face nodes come first.  PDL: the kernel
@@ -221,10 +236,13 @@ __device__ __forceinline__ float f32_trunc(const double x) {
 // calc_dt maximum.  Every thread of the block calls it: `active` is false for warps beyond the
 // Np node-warps of a wider block (they only take part in the barrier), `live` is false for
 // lanes past the last cell (they take part in the warp reductions).
+// qs: this node's q staged in shared memory (qs[0] variables 0, 1 and qs[qstride] variables 2, 3)
+// or null to read it from q.
 template <int N>
 __device__ __forceinline__ void stage_combine(const Inst &d, const int stage, const int e, const bool active,
                                               const bool live, const int i, const int lane, const double w[4],
-                                              double r0, double r1, double r2, double r3, double2 *scratch) {
+                                              double r0, double r1, double r2, double r3, double2 *scratch,
+                                              const double2 *qs = nullptr, const int qstride = 0) {
   constexpr int Np = np_of(N);
   const Phys &P = d.P;
   const size_t off = ((size_t)(live ? e : 0) * Np + (active ? i : 0)) * 4;
@@ -249,8 +267,13 @@ __device__ __forceinline__ void stage_combine(const Inst &d, const int stage, co
   double *qp = d.q + off;
   double2 qa = make_double2(0.0, 0.0), qb = make_double2(0.0, 0.0);
   if (live) {
-    qa = ld2(qp);
-    qb = ld2(qp + 2);
+    if (qs) {
+      qa = qs[0];
+      qb = qs[qstride];
+    } else {
+      qa = ld2(qp);
+      qb = ld2(qp + 2);
+    }
   }
   if (stage == 1) {
     if (live) {
@@ -447,13 +470,27 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
   constexpr int kS2 = kElemSlot / 2;  // double2 per staged slot
   constexpr bool DENSE = ozd_used(N, TC);           // dense rows, slots in natural order
   constexpr bool SYMTC = !DENSE && oz_used(N, TC != 0);  // even/odd blocks on the tensor cores
+  constexpr bool STG = elem_staged(N);  // W and q of the stage combine kept in shared memory
   double2 *Y = X + NK * kS2;
   int *Ems = reinterpret_cast<int *>(Y + Np * kS2);  // column exponents of the prepared operands
+  double2 *WQ = reinterpret_cast<double2 *>(Ems + 128);  // [4][32 Np]: W 0-1, W 2-3, q 0-1, q 2-3
   const int nthr = 32 * Np, tid = i * 32 + lane;
   const bool active = i < Np;
   const int e = e0 + lane;
   const bool live = active && e < d.K;
   const Phys &P = d.P;
+  // the tile's face fluxes (contiguous in HBM) go straight into their slots by asynchronous
+  // copies: j = tid + m*nthr, so the face point f = j / 32 is uniform in a warp
+  auto stage_face_fluxes = [&]() {
+    for (int j = active ? tid : 3 * Nfp * 32; j < 3 * Nfp * 32; j += nthr) {
+      const int f = j >> 5, el = j & 31;
+      const bool ok = e0 + el < d.K;
+      const double *fp = d.flux + (((size_t)(ok ? e0 + el : 0)) * 3 * Nfp + f) * 4;
+      const int pf = DENSE ? 2 * Np + f : c_pos[N][2 * Np + f];
+      cp_async16(X + pf * kS2 + el * 2, fp, ok);
+      cp_async16(X + pf * kS2 + el * 2 + 1, fp + 2, ok);
+    }
+  };
 
   double w[4] = {0.0, 0.0, 0.0, 0.0};
   double g[4] = {0.0, 0.0, 0.0, 0.0};
@@ -463,7 +500,19 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
     w[0] = a.x; w[1] = a.y; w[2] = b.x; w[3] = b.y;
     double2 ga = ld2(d.geo + (size_t)e * 16), gb = ld2(d.geo + (size_t)e * 16 + 2);
     g[0] = ga.x; g[1] = ga.y; g[2] = gb.x; g[3] = gb.y;
+    if constexpr (STG) {
+      WQ[tid] = a;
+      WQ[nthr + tid] = b;
+      // q (stages 1, 2) is not the face kernel's output: copied before the launch wait
+      if (stage == 1 || stage == 2) {
+        const double *qp = d.q + ((size_t)e * Np + i) * 4;
+        cp_async16(WQ + 2 * nthr + tid, qp, true);
+        cp_async16(WQ + 3 * nthr + tid, qp + 2, true);
+      }
+    }
   }
+  // Without programmatic launch the face fluxes are ready: their copies overlap the nodal fluxes.
+  if constexpr (!PDL) stage_face_fluxes();
   {
     const double rx = g[0], ry = g[1], sx = g[2], sy = g[3];
     double fr0 = 0, fr1 = 0, fr2 = 0, fr3 = 0, fs0 = 0, fs1 = 0, fs2 = 0, fs3 = 0;
@@ -490,22 +539,13 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
       X[ps * kS2 + lane * 2 + 1] = make_double2(fs2, fs3);
     }
   }
-  // Everything above reads only W and the metrics (written before the face kernel ran); the face
-  // fluxes below are the face kernel's output.
-  if constexpr (PDL) pdl_wait();
-  // face fluxes: j = tid + m*nthr, so the face point f = j / 32 is uniform in a warp
-  for (int j = active ? tid : 3 * Nfp * 32; j < 3 * Nfp * 32; j += nthr) {
-    const int f = j >> 5, el = j & 31;
-    double2 a = make_double2(0.0, 0.0), b = make_double2(0.0, 0.0);
-    if (e0 + el < d.K) {
-      const double *fp = d.flux + (((size_t)(e0 + el)) * 3 * Nfp + f) * 4;
-      a = ld2(fp);
-      b = ld2(fp + 2);
-    }
-    const int pf = DENSE ? 2 * Np + f : c_pos[N][2 * Np + f];
-    X[pf * kS2 + el * 2] = a;
-    X[pf * kS2 + el * 2 + 1] = b;
+  // Everything above reads only W, q and the metrics (written before the face kernel ran); the
+  // face fluxes are the face kernel's output.
+  if constexpr (PDL) {
+    pdl_wait();
+    stage_face_fluxes();
   }
+  cp_async_wait_all();  // this thread's copies; the barrier publishes everyone's
   __syncthreads();
   if constexpr (SYMTC) {
     // the butterfly in integers and the operand alignment, once per value
@@ -579,34 +619,49 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
     }
   }
   if constexpr (DENSE || SYMTC) {
-    // re-read this node's W rather than holding it through the contraction (registers); the
-    // node is written only below, by this thread
+    // this node's W again rather than held in registers through the contraction: from shared
+    // memory where it was staged, else from W (the node is written only below, by this thread)
     if (live) {
-      const double *wp = d.W + ((size_t)e * Np + i) * 4;
-      const double2 a = ld2(wp), b = ld2(wp + 2);
+      double2 a, b;
+      if constexpr (STG) {
+        a = WQ[tid];
+        b = WQ[nthr + tid];
+      } else {
+        const double *wp = d.W + ((size_t)e * Np + i) * 4;
+        a = ld2(wp);
+        b = ld2(wp + 2);
+      }
       w[0] = a.x; w[1] = a.y; w[2] = b.x; w[3] = b.y;
     }
   }
-  stage_combine<N>(d, stage, e, active, live, i, lane, w, r0, r1, r2, r3, X);
+  if constexpr (STG)
+    stage_combine<N>(d, stage, e, active, live, i, lane, w, r0, r1, r2, r3, X,
+                     (stage == 1 || stage == 2) ? WQ + 2 * nthr + tid : nullptr, nthr);
+  else
+    stage_combine<N>(d, stage, e, active, live, i, lane, w, r0, r1, r2, r3, X);
   // X and Y are rewritten by the next tile only after every warp is past this point
   __syncthreads();
 }
 
-// Dynamic shared memory of the even/odd element kernels: NK staged slots, Np output rows and the
-// 128 column exponents of the prepared tensor-core operands.
+// Dynamic shared memory of the even/odd element kernels: NK staged slots, Np output rows, the
+// 128 column exponents of the prepared tensor-core operands and, at N >= 3, W and q of every node
+// of the tile for the stage combine (elem_staged).
 constexpr size_t elem_sym_smem(int N) {
-  return (size_t)(nk_of(N) + np_of(N)) * kElemSlot * sizeof(double) + 128 * sizeof(int);
+  return (size_t)(nk_of(N) + np_of(N)) * kElemSlot * sizeof(double) + 128 * sizeof(int) +
+         (elem_staged(N) ? (size_t)4 * 32 * np_of(N) * 16 : 0);
 }
 
 // MB: minimum resident blocks per SM the register allocation must allow (oz_min_blocks for the
 // tensor-core form; at N = 3 without the bound it takes ~95 registers and runs two blocks per SM,
 // measured slower).
 // tile0: first 32-cell tile of this launch (a launch may cover a range of the tiles).
-template <int N, int TC, int MB = 1>
+// PW: launched with programmatic dependence on the face kernel (its fluxes are read after the
+// launch wait) or not (they are complete when the kernel starts).
+template <int N, int TC, int MB = 1, bool PW = true>
 __global__ void __launch_bounds__(32 * np_of(N), MB) elem_kernel_sym(const Inst d, const int stage, const int tile0) {
   extern __shared__ double2 Xs[];  // [NK][32] x 4 doubles, then [Np][32] x 4 doubles
   pdl_trigger();  // the next face kernel may be scheduled (it waits for this grid's writes)
-  elem_tile_sym<N, true, TC>(d, stage, (tile0 + (int)blockIdx.x) * 32, threadIdx.x, threadIdx.y, Xs);
+  elem_tile_sym<N, PW, TC>(d, stage, (tile0 + (int)blockIdx.x) * 32, threadIdx.x, threadIdx.y, Xs);
 }
 
 // ---------------------------------------------------------------- per-step finalize
@@ -849,72 +904,57 @@ static void launch_face(const Inst &d, int stage, cudaStream_t s) {
 // kernel at the other orders), 1: even/odd element kernel, 0: dense FP64.
 static int g_elem_variant = 3;
 
+// The even/odd element kernel instance for form TC at order N, launched over tiles [t0, t1):
+// with the launch attributes of launch_pdl (attr true) or as a plain launch.  The instance
+// knows whether it was launched with programmatic dependence (PW): without it the face fluxes
+// are complete at the start and their copies are issued first.
+template <int N, int TC, int MB>
+static void elem_sym_launch(const Inst &d, int stage, int t0, int t1, cudaStream_t s, bool attr) {
+  constexpr int Np = np_of(N);
+  const size_t smem = elem_sym_smem(N);
+  if (attr && g_pdl)
+    launch_pdl(elem_kernel_sym<N, TC, MB, true>, dim3(t1 - t0), dim3(32, Np), smem, s, d, stage, t0);
+  else if (attr)
+    launch_pdl(elem_kernel_sym<N, TC, MB, false>, dim3(t1 - t0), dim3(32, Np), smem, s, d, stage, t0);
+  else
+    elem_kernel_sym<N, TC, MB, false><<<t1 - t0, dim3(32, Np), smem, s>>>(d, stage, t0);
+}
+
+// Element tiles [t0, t1) of one stage in the current form (the even/odd forms; form 0, dense FP64,
+// only as a whole-mesh launch with attr).
+template <int N>
+static void launch_elem_form(const Inst &d, int stage, int t0, int t1, cudaStream_t s, bool attr) {
+  if (t1 <= t0) return;
+  if constexpr (ozd_used(N, 2)) {
+    if (g_elem_variant == 3) return elem_sym_launch<N, 2, oz_min_blocks(N)>(d, stage, t0, t1, s, attr);
+  }
+  if constexpr (oz_used(N, true)) {
+    if (g_elem_variant >= 2) return elem_sym_launch<N, 1, oz_min_blocks(N)>(d, stage, t0, t1, s, attr);
+  }
+  elem_sym_launch<N, 0, 1>(d, stage, t0, t1, s, attr);
+}
+
 template <int N>
 static void launch_elem(const Inst &d, int stage, cudaStream_t s) {
   constexpr int Np = np_of(N), NK = nk_of(N);
   if (g_elem_variant) {
-    const size_t smem = elem_sym_smem(N);
-    if constexpr (ozd_used(N, 2)) {
-      if (g_elem_variant == 3) {
-        launch_pdl(elem_kernel_sym<N, 2, oz_min_blocks(N)>, dim3((d.K + 31) / 32), dim3(32, Np), smem, s, d,
-                   stage, 0);
-        return;
-      }
-    }
-    if constexpr (oz_used(N, true)) {
-      if (g_elem_variant >= 2) {
-        launch_pdl(elem_kernel_sym<N, true, oz_min_blocks(N)>, dim3((d.K + 31) / 32), dim3(32, Np), smem, s, d,
-                   stage, 0);
-        return;
-      }
-    }
-    launch_pdl(elem_kernel_sym<N, false>, dim3((d.K + 31) / 32), dim3(32, Np), smem, s, d, stage, 0);
+    launch_elem_form<N>(d, stage, 0, (d.K + 31) / 32, s, true);
   } else {
     const size_t smem = (size_t)NK * 32 * 4 * sizeof(double);
     launch_pdl(elem_kernel<N>, dim3((d.K + 31) / 32), dim3(32, Np), smem, s, d, stage);
   }
 }
 
-// Element tiles [t0, t1) of one stage with the launch attributes of launch_elem (the even/odd
-// forms; the dense FP64 form only as a whole-mesh launch).
+// Element tiles [t0, t1) of one stage with the launch attributes of launch_elem.
 template <int N>
 static void launch_elem_range(const Inst &d, int stage, int t0, int t1, cudaStream_t s) {
-  constexpr int Np = np_of(N);
-  if (t1 <= t0) return;
-  const size_t smem = elem_sym_smem(N);
-  if constexpr (ozd_used(N, 2)) {
-    if (g_elem_variant == 3) {
-      launch_pdl(elem_kernel_sym<N, 2, oz_min_blocks(N)>, dim3(t1 - t0), dim3(32, Np), smem, s, d, stage, t0);
-      return;
-    }
-  }
-  if constexpr (oz_used(N, true)) {
-    if (g_elem_variant >= 2) {
-      launch_pdl(elem_kernel_sym<N, true, oz_min_blocks(N)>, dim3(t1 - t0), dim3(32, Np), smem, s, d, stage, t0);
-      return;
-    }
-  }
-  launch_pdl(elem_kernel_sym<N, false>, dim3(t1 - t0), dim3(32, Np), smem, s, d, stage, t0);
+  launch_elem_form<N>(d, stage, t0, t1, s, true);
 }
 
 // Element tiles [t0, t1) of one stage, in plain stream order on s (the even/odd forms only).
 template <int N>
 static void launch_elem_tiles(const Inst &d, int stage, int t0, int t1, cudaStream_t s) {
-  constexpr int Np = np_of(N);
-  const size_t smem = elem_sym_smem(N);
-  if constexpr (ozd_used(N, 2)) {
-    if (g_elem_variant == 3) {
-      elem_kernel_sym<N, 2, oz_min_blocks(N)><<<t1 - t0, dim3(32, Np), smem, s>>>(d, stage, t0);
-      return;
-    }
-  }
-  if constexpr (oz_used(N, true)) {
-    if (g_elem_variant >= 2) {
-      elem_kernel_sym<N, true, oz_min_blocks(N)><<<t1 - t0, dim3(32, Np), smem, s>>>(d, stage, t0);
-      return;
-    }
-  }
-  elem_kernel_sym<N, false><<<t1 - t0, dim3(32, Np), smem, s>>>(d, stage, t0);
+  launch_elem_form<N>(d, stage, t0, t1, s, false);
 }
 
 template <int N>
@@ -929,17 +969,15 @@ static cudaError_t set_smem_attr() {
   cudaError_t e = cudaFuncSetAttribute(elem_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const size_t smem_sym = elem_sym_smem(N);
-  e = cudaFuncSetAttribute(elem_kernel_sym<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_sym);
-  if constexpr (oz_used(N, true)) {
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(elem_kernel_sym<N, true, oz_min_blocks(N)>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)smem_sym);
-  }
-  if constexpr (ozd_used(N, 2)) {
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(elem_kernel_sym<N, 2, oz_min_blocks(N)>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)smem_sym);
-  }
+  auto both = [&](auto k_pdl, auto k_plain) {
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pdl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_sym);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_plain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_sym);
+  };
+  both(elem_kernel_sym<N, 0, 1, true>, elem_kernel_sym<N, 0, 1, false>);
+  if constexpr (oz_used(N, true))
+    both(elem_kernel_sym<N, 1, oz_min_blocks(N), true>, elem_kernel_sym<N, 1, oz_min_blocks(N), false>);
+  if constexpr (ozd_used(N, 2))
+    both(elem_kernel_sym<N, 2, oz_min_blocks(N), true>, elem_kernel_sym<N, 2, oz_min_blocks(N), false>);
   return e;
 }
 
@@ -1344,17 +1382,20 @@ int Solver::build_graph(std::string &err) {
 // slot has one writer), so the result is bitwise the same for every P.  With a mesh numbered
 // with locality (O-grid rings, square rows) lo_p and hi_p are p-1 and p+1.
 static int g_step_parts = 0;  // 0: automatic (step_parts_for), 1: the single-range chain
-// bit 0: launch the ranges' kernels without programmatic dependent launch; bit 1: give range p's
-// launches a scheduling priority that falls with p (earlier ranges first).
-static int g_step_graph_flags = 0;
+// bit 0: launch the ranges' kernels without programmatic dependent launch (the default: with it,
+// dependent launches start early and their waiting blocks hold SM slots the other ranges' kernels
+// could use: 300 vs 267 us per step at 4 ranges); bit 1: give range p's launches a scheduling
+// priority that falls with p (earlier ranges first; measured no faster).
+static int g_step_graph_flags = 1;
 void set_step_graph_flags(int f) { g_step_graph_flags = f & 3; }
 int step_graph_flags() { return g_step_graph_flags; }
 
 int step_parts_for(int K) {
   const int T = (K + 31) / 32;
   if (g_step_parts >= 1) return std::max(1, std::min(g_step_parts, std::min(kMaxStepParts, T)));
-  // automatic: ranges of at least 128 tiles, at most 8
-  return std::max(1, std::min(8, T / 128));
+  // automatic: ranges of at least 128 tiles, at most 4 (on the K = 32768 O-grid at N = 3, steps of
+  // 290 / 267 / 269 / 271 us with 1 / 4 / 8 / 16 ranges; more ranges add launches and edges)
+  return std::max(1, std::min(4, T / 128));
 }
 
 void set_step_parts(int p) { g_step_parts = (p >= 0 && p <= kMaxStepParts) ? p : 0; }

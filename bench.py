@@ -110,8 +110,8 @@ def elem_mma(n):
 # launch processes), counted by ncu on GB300 for the N = 3 kernels of this workload (profiles/
 # fp64_instructions_naca_ogrid_K32768_N3.md).  They are properties of the compiled kernels, like
 # the algorithmic bytes: re-count them when a kernel changes.
-FP64_INST_PER_FACE_NODE = {3: None}
-FP64_INST_PER_CELL_STAGE = {3: None}
+FP64_INST_PER_FACE_NODE = {3: 110.3}
+FP64_INST_PER_CELL_STAGE = {3: 407.0}
 
 
 def roofline(K, nf, face_ms, elem_ms, step_ms, peak_tf, hbm_peak, bf16_mma_tf=None):
@@ -598,6 +598,8 @@ def main():
     ap.add_argument("--no-dropin", action="store_true")
     ap.add_argument("--no-large-vortex", action="store_true",
                     help="skip the large vortex convergence + 16-instance batched beta gradient (~1 min)")
+    ap.add_argument("--parts", type=int, default=0,
+                    help="cell ranges of the step graph (0: the library's automatic choice; 1: one chain)")
     ap.add_argument("--adjoint-steps", type=int, default=2000)
     ap.add_argument("--advection-steps", type=int, default=200)
     args = ap.parse_args()
@@ -615,6 +617,7 @@ def main():
     import __graft_entry__ as g
     pkg = g.load_package()
     pkg.lib()
+    pkg.set_step_parts(args.parts)
     # clocks sampled over every GPU leg of the run (the main timed region alone is a few ms,
     # shorter than the sampling interval)
     clocks = Clocks(local)

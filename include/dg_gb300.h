@@ -314,13 +314,14 @@ int dg_tc_operator_digits(int N, int *dims, double *S, int *fexp, int *digits);
  * |th| < 2^41, |tl| < 2^49 (the joined level sums) and -1022 <= sc <= 900; DG_ERR_ARG outside. */
 int dg_tc_round(long long th, long long tl, int sc, double *out);
 /* Cell ranges of the step graph for solvers whose graph is built from now on: 0 automatic (the
- * default: ranges of at least 128 tiles of 32 cells, at most 8), 1 a single range (the seven
+ * default: ranges of at least 128 tiles of 32 cells, at most 4), 1 a single range (the seven
  * launches as one chain), 2..32 that many ranges (fewer if the mesh has fewer tiles). */
 void dg_set_step_parts(int parts);
 int dg_step_parts(void);
-/* Tuning of that graph for graphs built from now on: bit 0 launches its kernels without
- * programmatic dependent launch, bit 1 gives range p's launches a scheduling priority falling
- * with p (earlier ranges scheduled first).  0 by default.  Results are bitwise the same. */
+/* Tuning of that graph (more than one range) for graphs built from now on: bit 0 launches its
+ * kernels without programmatic dependent launch, bit 1 gives range p's launches a scheduling
+ * priority falling with p (earlier ranges scheduled first).  1 by default.  Results are
+ * bitwise the same. */
 void dg_set_step_graph_flags(int flags);
 int dg_step_graph_flags(void);
 /* Threads per face-kernel block of the plain path (32..256, multiple of 32; default 64). */

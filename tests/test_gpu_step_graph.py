@@ -37,6 +37,22 @@ def shuffled(m, seed):
     return out
 
 
+@pytest.mark.parametrize("flags", [0, 1, 2, 3])
+def test_graph_flags_bitwise_equal(pkg, flags):
+    """With and without programmatic dependent launch between the ranges' kernels, with and
+    without per-range priorities: the same bits."""
+    mesh = pkg.Mesh.naca_ogrid(96, 24, farfield="characteristic")
+    cfg = pkg.config(N=3, cfl=0.5, mach=0.5, alpha_deg=2.0)
+    q1, dt1, _, _ = run_parts(pkg, mesh, cfg, 1, 20)
+    prev = pkg.lib().dg_step_graph_flags()
+    pkg.lib().dg_set_step_graph_flags(flags)
+    try:
+        q, dt, _, _ = run_parts(pkg, mesh, cfg, 4, 20)
+    finally:
+        pkg.lib().dg_set_step_graph_flags(prev)
+    assert np.array_equal(q, q1) and np.array_equal(dt, dt1)
+
+
 @pytest.mark.parametrize("N", [3, 4])
 def test_parts_bitwise_equal_airfoil(pkg, omesh, N):
     mesh = pkg.Mesh.naca_ogrid(128, 32, farfield="characteristic")
@@ -71,7 +87,7 @@ def test_parts_bitwise_equal_vortex(pkg):
 
 def test_parts_setting(pkg):
     """0 (automatic) by default; out-of-range values fall back to it; the automatic choice
-    takes ranges of at least 128 tiles, at most 8."""
+    takes ranges of at least 128 tiles, at most 4."""
     lib = pkg.lib()
     assert pkg.step_parts() == 0
     for v in (-1, 33, 1000):
@@ -81,5 +97,5 @@ def test_parts_setting(pkg):
     small = pkg.Solver(pkg.Mesh.naca_ogrid(32, 8), pkg.config(N=3)).init()
     assert small.kernels_per_step() == 7
     big = pkg.Solver(pkg.Mesh.naca_ogrid(256, 64), pkg.config(N=3)).init()
-    assert big.kernels_per_step() == 6 * 8 + 1
+    assert big.kernels_per_step() == 6 * 4 + 1
     assert lib.dg_step_parts() == 0
