@@ -367,9 +367,8 @@ int dg_solver_record_dt(dg_solver_t *h, int max_steps) {
   h->dt_hist_len = (int)(st.step + max_steps);
   h->s.d.dt_hist = h->dt_hist;
   h->s.d.dt_hist_len = h->dt_hist ? (unsigned long long)h->dt_hist_len : 0ull;
-  // the captured graph holds the old pointer: rebuild on next run
-  if (h->s.graph_exec) { cudaGraphExecDestroy(h->s.graph_exec); h->s.graph_exec = nullptr; }
-  if (h->s.graph) { cudaGraphDestroy(h->s.graph); h->s.graph = nullptr; }
+  // the captured graphs hold the old pointer: rebuild on next run
+  h->s.drop_graphs();
   return 0;
 }
 

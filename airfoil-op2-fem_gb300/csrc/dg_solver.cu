@@ -1197,6 +1197,8 @@ Solver::~Solver() {
   for (cudaEvent_t ev : pevents) cudaEventDestroy(ev);
   if (graph_exec) cudaGraphExecDestroy(graph_exec);
   if (graph) cudaGraphDestroy(graph);
+  if (io_graph_exec) cudaGraphExecDestroy(io_graph_exec);
+  if (io_graph) cudaGraphDestroy(io_graph);
   for (void *p : allocs) cudaFree(p);
   if (stream) cudaStreamDestroy(stream);
 }
@@ -1351,7 +1353,7 @@ void Solver::enqueue_step_events(cudaStream_t s, cudaEvent_t *ev) {
 
 int Solver::build_graph(std::string &err) {
   if (graph_exec) return 0;
-  const int P = step_parts_for(K);
+  const int P = g_elem_variant ? step_parts_for(K) : 1;  // the dense FP64 form has no tile ranges
   if (P > 1) {
     if (int rc = build_parts(P, err)) return rc;
   } else {
@@ -1454,7 +1456,7 @@ int Solver::build_parts(int P, std::string &err) {
     CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     pstreams.push_back(st);
   }
-  while ((int)pevents.size() < 6 * P + 1) {
+  while ((int)pevents.size() < 7 * P + 1) {
     cudaEvent_t ev = nullptr;
     CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     pevents.push_back(ev);
@@ -1474,8 +1476,13 @@ int Solver::kernels_per_step() const {
   return n;
 }
 
-void Solver::enqueue_step_parts(cudaStream_t s) {
+void Solver::enqueue_step_parts(cudaStream_t s, const double *q_in, double *q_out) {
   const int P = parts, Nfp = cfg.N + 1;
+  const size_t cell_bytes = (size_t)np_of(cfg.N) * 4 * sizeof(double);
+  auto cells_of = [&](int p, size_t &c0, size_t &nc) {
+    c0 = (size_t)ptile0[p] * 32;
+    nc = std::min((size_t)ptile0[p + 1] * 32, (size_t)K) - c0;
+  };
   const int pdl_saved = g_pdl;
   if (g_step_graph_flags & 1) g_pdl = 0;
   int prio_lo = 0, prio_hi = 0;  // least and greatest priority (numerically: hi <= lo)
@@ -1488,13 +1495,28 @@ void Solver::enqueue_step_parts(cudaStream_t s) {
   cudaEvent_t fork = pevents[6 * P];
   auto evF = [&](int st, int p) { return pevents[(2 * st) * P + p]; };
   auto evE = [&](int st, int p) { return pevents[(2 * st + 1) * P + p]; };
+  auto evU = [&](int p) { return pevents[6 * P + 1 + p]; };
   cudaEventRecord(fork, s);
   for (int p = 0; p < P; p++) cudaStreamWaitEvent(pstreams[p], fork, 0);
+  if (q_in) {
+    // the input range by range: q, then W = q, on the range's own stream
+    for (int p = 0; p < P; p++) {
+      size_t c0, nc;
+      cells_of(p, c0, nc);
+      cudaMemcpyAsync(d.q + c0 * cell_bytes / 8, q_in + c0 * cell_bytes / 8, nc * cell_bytes, cudaMemcpyHostToDevice,
+                      pstreams[p]);
+      cudaMemcpyAsync(d.W + c0 * cell_bytes / 8, d.q + c0 * cell_bytes / 8, nc * cell_bytes,
+                      cudaMemcpyDeviceToDevice, pstreams[p]);
+      cudaEventRecord(evU(p), pstreams[p]);
+    }
+  }
   for (int stage = 0; stage < 3; stage++) {
     for (int p = 0; p < P; p++) {
       cudaStream_t ps = pstreams[p];
       if (stage > 0)
         for (int q = plo[p]; q < p; q++) cudaStreamWaitEvent(ps, evE(stage - 1, q), 0);
+      else if (q_in)
+        for (int q = plo[p]; q < p; q++) cudaStreamWaitEvent(ps, evU(q), 0);  // the W it reads
       Inst dp = d;
       dp.edges = pedges + pe0[p];
       dp.nE = pe0[p + 1] - pe0[p];
@@ -1513,14 +1535,61 @@ void Solver::enqueue_step_parts(cudaStream_t s) {
       DG_DISPATCH(cfg.N, launch_elem_range<NN>(d, stage, ptile0[p], ptile0[p + 1], ps));
       g_launch_prio_on = 0;
       cudaEventRecord(evE(stage, p), ps);
+      if (stage == 2 && q_out) {  // this range's result leaves while the others compute
+        size_t c0, nc;
+        cells_of(p, c0, nc);
+        cudaMemcpyAsync(q_out + c0 * cell_bytes / 8, d.q + c0 * cell_bytes / 8, nc * cell_bytes,
+                        cudaMemcpyDeviceToHost, ps);
+      }
     }
   }
-  for (int p = 0; p < P; p++) cudaStreamWaitEvent(s, evE(2, p), 0);
+  for (int p = 0; p < P; p++) {
+    cudaEventRecord(evE(2, p), pstreams[p]);  // after the range's copy too
+    cudaStreamWaitEvent(s, evE(2, p), 0);
+  }
   launch_pdl(finalize_kernel, dim3(1), dim3(32), 0, s, d.st, d.dt_mode, d.dt_hist, d.dt_hist_len);
   g_pdl = pdl_saved;
 }
 
+// One step with host buffers through a captured graph over the cell ranges: each range's input
+// is uploaded on its own stream before its first face launch (which also waits for the ranges
+// whose W it reads), and each range's result is downloaded as soon as its last element launch is
+// done.  The graph is kept for the last pair of host pointers; host buffers that are not pinned
+// (or registered) take the single-range path below.
+int Solver::step_io_parts(const double *q_in, double *q_out, bool &done, std::string &err) {
+  done = false;
+  if (int rc = build_graph(err)) return rc;
+  if (parts <= 1) return 0;
+  for (const void *hp : {(const void *)q_in, (const void *)q_out}) {
+    if (!hp) continue;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, hp) != cudaSuccess || at.type != cudaMemoryTypeHost) {
+      cudaGetLastError();
+      return 0;
+    }
+  }
+  if (!io_graph_exec || io_in != q_in || io_out != q_out) {
+    if (io_graph_exec) { cudaGraphExecDestroy(io_graph_exec); io_graph_exec = nullptr; }
+    if (io_graph) { cudaGraphDestroy(io_graph); io_graph = nullptr; }
+    CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_step_parts(stream, q_in, q_out);
+    cudaError_t ce = cudaStreamEndCapture(stream, &io_graph);
+    if (ce != cudaSuccess) { err = std::string("io graph capture: ") + cudaGetErrorString(ce); return -6; }
+    CK(cudaGraphInstantiate(&io_graph_exec, io_graph, 0));
+    io_in = q_in;
+    io_out = q_out;
+  }
+  CK(cudaGraphLaunch(io_graph_exec, stream));
+  done = true;
+  return 0;
+}
+
 int Solver::step_io(const double *q_in, double *q_out, std::string &err) {
+  if (g_elem_variant) {
+    bool done = false;
+    if (int rc = step_io_parts(q_in, q_out, done, err)) return rc;
+    if (done) return 0;
+  }
   if (!g_elem_variant) {  // the dense form has no tile ranges: plain copies around a whole step
     const size_t n = q_count() * 8;
     if (q_in) {

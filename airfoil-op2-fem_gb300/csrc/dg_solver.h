@@ -113,7 +113,24 @@ struct Solver {
   std::vector<cudaStream_t> pstreams;
   std::vector<cudaEvent_t> pevents;
   int build_parts(int P, std::string &err);
-  void enqueue_step_parts(cudaStream_t s);
+  // One step of the ranges' DAG on s; with q_in, the input is uploaded range by range first, with
+  // q_out the result is downloaded range by range (host buffers, pinned).
+  void enqueue_step_parts(cudaStream_t s, const double *q_in = nullptr, double *q_out = nullptr);
+  int step_io_parts(const double *q_in, double *q_out, bool &done, std::string &err);
+  // Forget the captured step graphs (rebuilt on the next run), e.g. after a pointer they hold
+  // changed.
+  void drop_graphs() {
+    if (graph_exec) { cudaGraphExecDestroy(graph_exec); graph_exec = nullptr; }
+    if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
+    if (io_graph_exec) { cudaGraphExecDestroy(io_graph_exec); io_graph_exec = nullptr; }
+    if (io_graph) { cudaGraphDestroy(io_graph); io_graph = nullptr; }
+    io_in = nullptr;
+    io_out = nullptr;
+  }
+  cudaGraph_t io_graph = nullptr;
+  cudaGraphExec_t io_graph_exec = nullptr;
+  const double *io_in = nullptr;
+  double *io_out = nullptr;
   int kernels_per_step() const;
   int step(int nsteps, bool use_graph, std::string &err);
   // One step with host buffers at either end (either may be null): q_in is uploaded first; the

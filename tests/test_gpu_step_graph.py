@@ -99,3 +99,34 @@ def test_parts_setting(pkg):
     big = pkg.Solver(pkg.Mesh.naca_ogrid(256, 64), pkg.config(N=3)).init()
     assert big.kernels_per_step() == 6 * 4 + 1
     assert lib.dg_step_parts() == 0
+
+
+@pytest.mark.parametrize("nsteps", [1, 3])
+@pytest.mark.parametrize("pinned", [True, False])
+def test_step_host_over_ranges_equals_run(pkg, nsteps, pinned):
+    """The host-buffer call over cell ranges (each range uploaded before its first face launch,
+    downloaded after its last element launch, in one captured graph; pageable buffers take the
+    single-range path): bitwise the same as run(), on two calls with the same buffers (the second
+    reuses the graph) and one with new buffers (a new graph)."""
+    mesh = pkg.Mesh.naca_ogrid(96, 24, farfield="characteristic")
+    cfg = pkg.config(N=3, cfl=0.5, mach=0.45, alpha_deg=1.0)
+    pkg.set_step_parts(4)
+    try:
+        a = pkg.Solver(mesh, cfg).init()
+        b = pkg.Solver(mesh, cfg).init()
+    finally:
+        pkg.set_step_parts(0)
+    q = a.get("q")
+    if pinned:
+        bufs = [(pkg.PinnedArray(q.size), pkg.PinnedArray(q.size)) for _ in range(2)]
+        views = [(x.array, y.array) for x, y in bufs]
+    else:
+        views = [(np.empty_like(q), np.empty_like(q)) for _ in range(2)]
+    for call, (h_in, h_out) in enumerate((views[0], views[0], views[1])):
+        h_in[:] = b.get("q")
+        h_out[:] = np.nan
+        a.step_host(h_in, nsteps, h_out)
+        b.run(nsteps)
+        b.sync()
+        assert np.array_equal(h_out, b.get("q")), call
+        assert np.array_equal(a.get("q"), b.get("q")) and a.time() == b.time(), call
