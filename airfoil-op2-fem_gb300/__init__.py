@@ -141,6 +141,8 @@ def lib():
         "dg_batch_use_shape": (C.c_int, [vp, C.c_int, C.c_int]),
         "dg_batch_inject_barrier_timeout": (C.c_int, [vp]),
         "dg_batch_tried": (C.c_int, [vp, C.c_int, ip, ip, dp]),
+        "dg_batch_set_barrier_limit": (C.c_int, [vp, C.c_ulonglong]),
+        "dg_batch_barrier_check": (C.c_int, [vp, C.c_ulonglong]),
         "dg_batch_stream": (vp, [vp]),
         "dg_batch_free": (None, [vp]),
         "dg_batch_last_error": (cp, []),

@@ -20,10 +20,11 @@ struct GridBarrier {
   unsigned gen;
   unsigned err;  // bit 1: a barrier wait gave up (the stage's results are then invalid)
   unsigned pad;
+  unsigned long long limit;  // longest wait in SM clocks; 0: 2^32 (about 2 s)
 };
 
-// Generation barrier over all blocks of a cooperative launch.  The wait is bounded by ~2^32
-// SM clocks (about 2 s): on timeout the block records the error and the caller stops.
+// Generation barrier over all blocks of a cooperative launch.  The wait is bounded by b->limit
+// SM clocks: on timeout the block records the error and the caller stops.
 __device__ __forceinline__ bool grid_barrier(GridBarrier *b, const unsigned nblocks) {
   __shared__ int s_ok;
   __syncthreads();
@@ -31,6 +32,7 @@ __device__ __forceinline__ bool grid_barrier(GridBarrier *b, const unsigned nblo
     int ok = 1;
     volatile unsigned *vgen = &b->gen;
     const unsigned gen = *vgen;
+    const long long limit = b->limit ? (long long)b->limit : (1ll << 32);
     __threadfence();
     if (atomicAdd(&b->count, 1u) == nblocks - 1) {
       b->count = 0;
@@ -39,7 +41,7 @@ __device__ __forceinline__ bool grid_barrier(GridBarrier *b, const unsigned nblo
     } else {
       const long long start = clock64();
       while (*vgen == gen) {
-        if (clock64() - start > (1ll << 32)) {
+        if (clock64() - start > limit) {
           atomicOr(&b->err, 2u);
           ok = 0;
           break;
@@ -52,6 +54,18 @@ __device__ __forceinline__ bool grid_barrier(GridBarrier *b, const unsigned nblo
   }
   __syncthreads();
   return s_ok != 0;
+}
+
+// Check of the barrier's bounded wait: one cooperative launch that runs only a grid barrier, with
+// block 0 held back before it by a bounded delay of `hold` SM clocks.  With hold above the
+// barrier's limit the other blocks' waits run out (the error is recorded and they return), and
+// block 0 then arrives last and completes the barrier alone: every wait ends.
+__global__ void barrier_check_kernel(GridBarrier *b, const long long hold) {
+  if (blockIdx.x == 0 && threadIdx.x == 0 && hold > 0) {
+    const long long t0 = clock64();
+    while (clock64() - t0 < hold) __nanosleep(256);
+  }
+  grid_barrier(b, gridDim.x);
 }
 
 #define DG_DISPATCH_RT(N_, CALL)                             \
@@ -497,6 +511,36 @@ struct Batch {
     return 0;
   }
 
+  // The grid barrier's longest wait, SM clocks (0: the default, 2^32).
+  int set_barrier_limit(unsigned long long cycles, std::string &err) {
+    cudaError_t ce = cudaStreamSynchronize(stream);
+    if (ce == cudaSuccess)
+      ce = cudaMemcpy((char *)d_bar + offsetof(GridBarrier, limit), &cycles, sizeof(cycles), cudaMemcpyHostToDevice);
+    if (ce != cudaSuccess) { err = cudaGetErrorString(ce); return -100; }
+    return 0;
+  }
+
+  // One launch of barrier_check_kernel over one block per SM on the batch's stream and barrier
+  // (its outcome is read by sync()).
+  int barrier_check(unsigned long long hold, std::string &err) {
+    int dev = 0, sms = 0;
+    cudaError_t ce = cudaGetDevice(&dev);
+    if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (ce != cudaSuccess) { err = cudaGetErrorString(ce); return -100; }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(sms);
+    cfg.blockDim = dim3(64);
+    cfg.stream = stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    ce = cudaLaunchKernelEx(&cfg, barrier_check_kernel, d_bar, (long long)hold);
+    if (ce != cudaSuccess) { err = cudaGetErrorString(ce); return -100; }
+    return 0;
+  }
+
   int sync(std::string &err) {
     cudaError_t ce = cudaStreamSynchronize(stream);
     if (ce != cudaSuccess) { err = cudaGetErrorString(ce); return -100; }
@@ -506,6 +550,7 @@ struct Batch {
     if (b.err) {
       // report once: the flag is cleared so that the batch can be re-initialised and run again
       GridBarrier z = {};
+      z.limit = b.limit;
       cudaMemcpy(d_bar, &z, sizeof(z), cudaMemcpyHostToDevice);
       err = "a grid barrier wait timed out: results of that step are invalid";
       return -8;

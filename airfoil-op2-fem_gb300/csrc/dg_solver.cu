@@ -27,6 +27,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstddef>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -2005,10 +2006,24 @@ extern "C" int dg_batch_sync(dg_batch_t *h) {
 // bounded wait gave up would (no kernel is made to wait).
 extern "C" int dg_batch_inject_barrier_timeout(dg_batch_t *h) {
   if (!h) return batch_fail(DG_ERR_ARG, "null batch");
-  dg::GridBarrier b = {};
-  b.err = 2u;
-  if (cudaMemcpy(h->b.d_bar, &b, sizeof(b), cudaMemcpyHostToDevice) != cudaSuccess)
+  const unsigned e = 2u;
+  if (cudaStreamSynchronize(h->b.stream) != cudaSuccess ||
+      cudaMemcpy((char *)h->b.d_bar + offsetof(dg::GridBarrier, err), &e, sizeof(e), cudaMemcpyHostToDevice) != cudaSuccess)
     return batch_fail(DG_ERR_CUDA, "cudaMemcpy");
+  return 0;
+}
+
+extern "C" int dg_batch_set_barrier_limit(dg_batch_t *h, unsigned long long cycles) {
+  if (!h) return batch_fail(DG_ERR_ARG, "null batch");
+  std::string err;
+  if (h->b.set_barrier_limit(cycles, err)) return batch_fail(DG_ERR_CUDA, err);
+  return 0;
+}
+
+extern "C" int dg_batch_barrier_check(dg_batch_t *h, unsigned long long hold_cycles) {
+  if (!h || hold_cycles > (1ull << 40)) return batch_fail(DG_ERR_ARG, "bad arguments (hold at most 2^40 clocks)");
+  std::string err;
+  if (h->b.barrier_check(hold_cycles, err)) return batch_fail(DG_ERR_CUDA, err);
   return 0;
 }
 

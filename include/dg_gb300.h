@@ -174,6 +174,15 @@ int dg_batch_shape(dg_batch_t *b, int *variant, int *block, int *face_tile, int 
 /* Host-side fault injection for tests: record a grid-barrier timeout as a kernel whose bounded
  * wait gave up would; the next dg_batch_sync reports DG_ERR_TIMEOUT and clears it. */
 int dg_batch_inject_barrier_timeout(dg_batch_t *b);
+/* The persistent kernel's grid barrier waits at most `cycles` SM clocks (0: the default, 2^32,
+ * about 2 s at 2 GHz) before recording a timeout and returning; applies to launches from now on. */
+int dg_batch_set_barrier_limit(dg_batch_t *b, unsigned long long cycles);
+/* Device-side check of that bounded wait: one cooperative launch (one 64-thread block per SM) that
+ * runs only the grid barrier, with block 0 held back before it by a bounded delay of hold_cycles
+ * SM clocks (at most 2^40).  With hold_cycles above the limit the other blocks' waits run out and
+ * the next dg_batch_sync reports DG_ERR_TIMEOUT; with 0 the barrier completes normally.  No wait is
+ * unbounded either way. */
+int dg_batch_barrier_check(dg_batch_t *b, unsigned long long hold_cycles);
 /* Use one launch shape (variant as above) without timing. */
 int dg_batch_use_shape(dg_batch_t *b, int variant, int face_tile);
 /* The shapes the last dg_batch_autotune timed: with i < 0 returns their count; else shape i's

@@ -96,3 +96,26 @@ def test_batch_reports_barrier_timeout(pkg):
     b.init()
     b.run(2)
     b.sync()
+
+
+def test_batch_barrier_wait_runs_out_on_device(pkg):
+    """The grid barrier's bounded wait, on the device: with a limit of 20,000 SM clocks (~10 us)
+    and block 0 held back 4,000,000 clocks (~2 ms, a bounded delay) the other blocks' waits run
+    out, they record the timeout and return, block 0 then completes the barrier alone, and sync
+    reports DG_ERR_TIMEOUT.  Without the hold the same launch completes normally, and the batch
+    steps on afterwards with the default limit."""
+    meshes, cfgs = instances(pkg)
+    b = pkg.Batch(meshes[:2], cfgs[:2]).init()
+    lib = pkg.lib()
+    assert lib.dg_batch_barrier_check(b.h, 0) == 0
+    b.sync()  # no hold: completes
+    assert lib.dg_batch_set_barrier_limit(b.h, 20000) == 0
+    assert lib.dg_batch_barrier_check(b.h, 4000000) == 0
+    with pytest.raises(pkg.DGError) as e:
+        b.sync()
+    assert e.value.code == pkg.ERR_TIMEOUT
+    assert lib.dg_batch_barrier_check(b.h, 1 << 41) != 0  # beyond the longest hold: refused
+    assert lib.dg_batch_set_barrier_limit(b.h, 0) == 0
+    b.init()
+    b.run(2)
+    b.sync()
