@@ -291,6 +291,7 @@ int dg_solver_sync(dg_solver_t *h) {
   std::string err;
   if (h->s.state(st, err)) return fail(DG_ERR_CUDA, err);
   if (st.err & 1u) return fail(DG_ERR_NONPHYSICAL, "non-positive or non-finite density");
+  if (st.err & 4u) return fail(DG_ERR_TIMEOUT, "a bounded wait of the element kernel ran out: results are invalid");
   return 0;
 }
 
@@ -673,6 +674,8 @@ void dg_set_step_graph_flags(int flags) { dg::set_step_graph_flags(flags); }
 int dg_step_graph_flags(void) { return dg::step_graph_flags(); }
 void dg_set_elem_variant(int variant) { dg::set_elem_variant(variant); }
 int dg_elem_variant(void) { return dg::elem_variant(); }
+void dg_set_elem_ws(int mode) { dg::set_elem_ws(mode); }
+int dg_elem_ws(void) { return dg::elem_ws(); }
 
 int dg_tc_operator_digits(int N, int *dims, double *S, int *fexp, int *digits) {
   if (!dims) return fail(DG_ERR_ARG, "bad arguments");

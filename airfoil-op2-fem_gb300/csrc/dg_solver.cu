@@ -237,13 +237,20 @@ __device__ __forceinline__ float f32_trunc(const double x) {
 // calc_dt maximum.  Every thread of the block calls it: `active` is false for warps beyond the
 // Np node-warps of a wider block (they only take part in the barrier), `live` is false for
 // lanes past the last cell (they take part in the warp reductions).
+// The barrier among the threads that run the stage combine: the whole block here; the
+// warp-specialised element kernel passes its own (the node warps only, bounded waits).
+struct BlockSync {
+  __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+
 // qs: this node's q staged in shared memory (qs[0] variables 0, 1 and qs[qstride] variables 2, 3)
-// or null to read it from q.
-template <int N>
+// or null to read it from q.  sync: see BlockSync.
+template <int N, class SyncF = BlockSync>
 __device__ __forceinline__ void stage_combine(const Inst &d, const int stage, const int e, const bool active,
                                               const bool live, const int i, const int lane, const double w[4],
                                               double r0, double r1, double r2, double r3, double2 *scratch,
-                                              const double2 *qs = nullptr, const int qstride = 0) {
+                                              const double2 *qs = nullptr, const int qstride = 0,
+                                              const SyncF &sync = SyncF()) {
   constexpr int Np = np_of(N);
   const Phys &P = d.P;
   const size_t off = ((size_t)(live ? e : 0) * Np + (active ? i : 0)) * 4;
@@ -329,7 +336,7 @@ __device__ __forceinline__ void stage_combine(const Inst &d, const int stage, co
     }
     if (i == 0 && lane == 0) s_ncand = 0;
     // every warp is past its contraction here, so the staging area (scratch) is free
-    __syncthreads();
+    sync();
     // The block's candidates (often several nodes of one cell, one per node-warp) are packed
     // into the staging area and evaluated by warp 0 alone: one FP64 evaluation per 32
     // candidates instead of one per node-warp holding a candidate.
@@ -344,7 +351,7 @@ __device__ __forceinline__ void stage_combine(const Inst &d, const int stage, co
         c[4] = fb >= 0 ? fmax(ge[6 + 3 * fa], ge[6 + 3 * fb]) : ge[6 + 3 * fa];
       }
     }
-    __syncthreads();
+    sync();
     if (i == 0) {
       const int nc = s_ncand;
       unsigned long long best = 0ull;
@@ -368,7 +375,7 @@ __device__ __forceinline__ void stage_combine(const Inst &d, const int stage, co
     }
     // the block may run another tile next (batched kernel): the staging area and s_wmax are
     // rewritten only after warp 0 has read them
-    __syncthreads();
+    sync();
   }
 }
 
@@ -665,6 +672,8 @@ __global__ void __launch_bounds__(32 * np_of(N), MB) elem_kernel_sym(const Inst 
   elem_tile_sym<N, PW, TC>(d, stage, (tile0 + (int)blockIdx.x) * 32, threadIdx.x, threadIdx.y, Xs);
 }
 
+#include "dg_elem_ws.cuh"
+
 // ---------------------------------------------------------------- per-step finalize
 // Launched with programmatic dependent launch in the step graph: it waits for the last element
 // kernel (whose dt maximum it reads) and lets the next step's face kernel be scheduled meanwhile.
@@ -921,11 +930,41 @@ static void elem_sym_launch(const Inst &d, int stage, int t0, int t1, cudaStream
     elem_kernel_sym<N, TC, MB, false><<<t1 - t0, dim3(32, Np), smem, s>>>(d, stage, t0);
 }
 
+// 1: the tensor-core element form at N = 3, 4 runs as the warp-specialised persistent kernel
+// (dg_elem_ws.cuh) over one block per SM; 2: the same, a launch over a range of tiles taking the
+// range's share of the SMs; 0: one block per tile (elem_kernel_sym).  Bitwise the same results.
+static int g_elem_ws = 1;
+
+static int ws_sm_count() {
+  static int sms[kMaxDevices] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return 1;
+  if (!sms[dev]) cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
+  return sms[dev] > 0 ? sms[dev] : 1;
+}
+
+template <int N>
+static void elem_ws_launch(const Inst &d, int stage, int t0, int t1, cudaStream_t s, bool attr) {
+  const int T = (d.K + 31) / 32, sms = ws_sm_count();
+  int grid = g_elem_ws == 2 ? (int)(((long long)sms * (t1 - t0) + T - 1) / T) : sms;
+  grid = std::max(1, std::min(grid, t1 - t0));
+  const size_t smem = ws_smem(N);
+  if (attr && g_pdl)
+    launch_pdl(elem_kernel_ws<N, true>, dim3(grid), dim3(ws_threads(N)), smem, s, d, stage, t0, t1);
+  else if (attr)
+    launch_pdl(elem_kernel_ws<N, false>, dim3(grid), dim3(ws_threads(N)), smem, s, d, stage, t0, t1);
+  else
+    elem_kernel_ws<N, false><<<grid, ws_threads(N), smem, s>>>(d, stage, t0, t1);
+}
+
 // Element tiles [t0, t1) of one stage in the current form (the even/odd forms; form 0, dense FP64,
 // only as a whole-mesh launch with attr).
 template <int N>
 static void launch_elem_form(const Inst &d, int stage, int t0, int t1, cudaStream_t s, bool attr) {
   if (t1 <= t0) return;
+  if constexpr (ws_used(N)) {
+    if (g_elem_ws && g_elem_variant >= 2) return elem_ws_launch<N>(d, stage, t0, t1, s, attr);
+  }
   if constexpr (ozd_used(N, 2)) {
     if (g_elem_variant == 3) return elem_sym_launch<N, 2, oz_min_blocks(N)>(d, stage, t0, t1, s, attr);
   }
@@ -979,6 +1018,12 @@ static cudaError_t set_smem_attr() {
     both(elem_kernel_sym<N, 1, oz_min_blocks(N), true>, elem_kernel_sym<N, 1, oz_min_blocks(N), false>);
   if constexpr (ozd_used(N, 2))
     both(elem_kernel_sym<N, 2, oz_min_blocks(N), true>, elem_kernel_sym<N, 2, oz_min_blocks(N), false>);
+  if constexpr (ws_used(N)) {
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(elem_kernel_ws<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ws_smem(N));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(elem_kernel_ws<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ws_smem(N));
+  }
   return e;
 }
 
@@ -1173,6 +1218,8 @@ int load_order_constants(int N, std::string &err) {
 int order_constants_loaded(int dev, int N) { return (N < 1 || N > 6) ? -1 : g_order_table.done(dev, N); }
 
 void set_elem_variant(int v) { g_elem_variant = (v >= 0 && v <= 3) ? v : 3; }
+void set_elem_ws(int m) { g_elem_ws = (m >= 0 && m <= 2) ? m : 1; }
+int elem_ws() { return g_elem_ws; }
 int elem_variant() { return g_elem_variant; }
 void set_pdl(int on) { g_pdl = on ? 1 : 0; }
 void set_face_block(int b) { g_face_block = (b >= 32 && b <= 256 && b % 32 == 0) ? b : 64; }

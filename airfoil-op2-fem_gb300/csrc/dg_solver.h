@@ -26,7 +26,8 @@ struct StepState {
   unsigned long long dt1_bits;  // running calc_dt maximum (bits of a non-negative double)
   double cfl;
   unsigned long long step;      // completed steps
-  unsigned err;                 // bit 0: a non-positive or non-finite density was produced
+  unsigned err;                 // bit 0: a non-positive or non-finite density was produced;
+                                // bit 2: a bounded wait of the element kernel ran out
   unsigned pad;
 };
 
@@ -61,6 +62,11 @@ int noalloc_ready(int dev);
 // 1 even/odd FP64, 0 dense FP64.
 void set_elem_variant(int v);
 int elem_variant();
+// The tensor-core element form at N = 3, 4 as the warp-specialised persistent kernel: 1 (default)
+// one block per SM for every launch, 2 a range launch takes its share of the SMs, 0 off (one block
+// per tile).
+void set_elem_ws(int m);
+int elem_ws();
 // Host-only: parity dimensions {NUe, NUo, NRe, NRo}, even/odd operator blocks, row exponents
 // [parity][32] and signed base-256 digits [parity][digit][slot 32][row 32] of the tensor-core
 // contraction of order N.

@@ -27,7 +27,7 @@ enum {
   DG_ERR_ARG = -1,
   DG_ERR_CUDA = -100,
   DG_ERR_NONPHYSICAL = -200, /* a kernel saw a non-positive or non-finite density */
-  DG_ERR_TIMEOUT = -300      /* a bounded wait in a batched kernel gave up (that step is invalid) */
+  DG_ERR_TIMEOUT = -300      /* a bounded wait in a batched or element kernel gave up (that step is invalid) */
 };
 
 const char *dg_last_error(void);
@@ -312,6 +312,15 @@ int dg_kernels_per_step(void);
 void dg_set_elem_variant(int variant);
 /* The current element-kernel form. */
 int dg_elem_variant(void);
+/* How the tensor-core element form runs at orders 3 and 4, for launches and graphs built from now
+ * on: 1 (default) a warp-specialised persistent kernel, one block per SM walking a contiguous range
+ * of 32-cell tiles, node warps staging the next tile and combining the previous one while
+ * contraction warps run the current tile's tensor-core product (double-buffered shared memory,
+ * bounded mbarrier waits: a wait that runs out makes dg_solver_sync report DG_ERR_TIMEOUT);
+ * 2 the same with a launch over a range of tiles taking that range's share of the SMs; 0 one
+ * block per tile.  All compute the same bits. */
+void dg_set_elem_ws(int mode);
+int dg_elem_ws(void);
 /* Host-only (no GPU needed): the tables of the tensor-core contraction of order N (3..5).
  * dims[4] receives NUe, NUo, NRe, NRo; S (NRe*NUe + NRo*NUo doubles, may be NULL) the even then
  * odd operator blocks row-major; fexp (2 x 32 ints, may be NULL) each row's biased binary
