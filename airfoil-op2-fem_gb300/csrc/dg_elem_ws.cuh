@@ -12,8 +12,11 @@
 //     recombination and stage combine ("combine");
 //   contraction warps (8 warps, 256 threads): the operand pre-pass and the contraction of a filled
 //     buffer into its output rows.
-// The staging (X, Y, column exponents, staged W and q) is double-buffered: while the contraction
-// warps work on tile j, the node warps fill tile j+1 and then combine tile j-1.  The two groups
+// The staging (X, Y, column exponents, staged W and q) is triple-buffered.  In their step j the
+// node warps load tile j+1's W and metrics into registers, compute tile j's nodal fluxes (its face
+// fluxes and q were copied in during step j-1), start the asynchronous copies of tile j+1's face
+// fluxes and q, and combine tile j-1, while the contraction warps work on the tile filled last: the
+// node warps' loads are in flight while they compute.  The two groups
 // hand buffers over through mbarriers (full / empty per buffer); every wait is bounded (about
 // 2^28 SM clocks), after which the thread records an error bit in the step state and goes on, so
 // the kernel always ends.  The arithmetic of every tile is that of elem_tile_sym in its
@@ -23,17 +26,19 @@
 constexpr int kWsCtrWarps = 8;  // contraction warps: oz_prep's 256 threads, 2 or 3 units each
 constexpr long long kWsWaitLimit = 1ll << 28;
 
-// Orders with a warp-specialised kernel: the even/odd blocks on the tensor cores at N = 3, 4 (at
-// N = 5 the block would need 29 warps and two buffers of 150 KB).
-constexpr bool ws_used(int N) { return N == 3 || N == 4; }
+// Orders with a warp-specialised kernel: the even/odd blocks on the tensor cores at N = 3 (three
+// buffers of 64 KB; at N = 4 three buffers would exceed the 227 KB of shared memory, and with two
+// the node warps cannot load ahead: measured no faster than one block per tile there).
+constexpr bool ws_used(int N) { return N == 3; }
+constexpr int kWsBufs = 3;
 constexpr int ws_threads(int N) { return 32 * (np_of(N) + kWsCtrWarps); }
 // one staging buffer: X (NK slots), Y (Np rows), 128 column exponents, W and q of every node
 constexpr size_t ws_buf_bytes(int N) {
   return (size_t)(nk_of(N) + np_of(N)) * kElemSlot * sizeof(double) + 128 * sizeof(int) +
          (size_t)4 * 32 * np_of(N) * sizeof(double2);
 }
-constexpr int kWsBars = 12;
-constexpr size_t ws_smem(int N) { return 2 * ws_buf_bytes(N) + kWsBars * sizeof(unsigned long long); }
+constexpr int kWsBars = 16;
+constexpr size_t ws_smem(int N) { return kWsBufs * ws_buf_bytes(N) + kWsBars * sizeof(unsigned long long); }
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
 
@@ -85,33 +90,20 @@ struct WsNodeSync {
   }
 };
 
-// Fill: the tile's W, metrics, q and face fluxes, and the nodal fluxes into the slots (the first
-// part of elem_tile_sym in its tensor-core form).
+// The copies of a tile's face fluxes (into their slots) and, in stages 1 and 2, of q (into the
+// staged W / q area), as one cp.async group of this thread.
 template <int N>
-__device__ __forceinline__ void ws_fill(const Inst &d, const int stage, const int e0, const int lane, const int i,
-                                        double2 *X, double2 *WQ) {
+__device__ __forceinline__ void ws_issue(const Inst &d, const int stage, const int e0, const int lane, const int i,
+                                         double2 *X, double2 *WQ) {
   constexpr int Np = np_of(N), Nfp = N + 1;
   constexpr int kS2 = kElemSlot / 2;
   constexpr int nthr = 32 * Np;
   const int tid = i * 32 + lane;
   const int e = e0 + lane;
-  const bool live = e < d.K;
-  const Phys &P = d.P;
-  double w[4] = {0.0, 0.0, 0.0, 0.0};
-  double g[4] = {0.0, 0.0, 0.0, 0.0};
-  if (live) {
-    const double *wp = d.W + ((size_t)e * Np + i) * 4;
-    const double2 a = ld2(wp), b = ld2(wp + 2);
-    w[0] = a.x; w[1] = a.y; w[2] = b.x; w[3] = b.y;
-    const double2 ga = ld2(d.geo + (size_t)e * 16), gb = ld2(d.geo + (size_t)e * 16 + 2);
-    g[0] = ga.x; g[1] = ga.y; g[2] = gb.x; g[3] = gb.y;
-    WQ[tid] = a;
-    WQ[nthr + tid] = b;
-    if (stage == 1 || stage == 2) {
-      const double *qp = d.q + ((size_t)e * Np + i) * 4;
-      cp_async16(WQ + 2 * nthr + tid, qp, true);
-      cp_async16(WQ + 3 * nthr + tid, qp + 2, true);
-    }
+  if ((stage == 1 || stage == 2) && e < d.K) {
+    const double *qp = d.q + ((size_t)e * Np + i) * 4;
+    cp_async16(WQ + 2 * nthr + tid, qp, true);
+    cp_async16(WQ + 3 * nthr + tid, qp + 2, true);
   }
   for (int j = tid; j < 3 * Nfp * 32; j += nthr) {
     const int f = j >> 5, el = j & 31;
@@ -121,7 +113,43 @@ __device__ __forceinline__ void ws_fill(const Inst &d, const int stage, const in
     cp_async16(X + pf * kS2 + el * 2, fp, ok);
     cp_async16(X + pf * kS2 + el * 2 + 1, fp + 2, ok);
   }
-  const double rx = g[0], ry = g[1], sx = g[2], sy = g[3];
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+// This node's W and the cell's metrics, into registers (loaded a tile ahead of their use).
+template <int N>
+__device__ __forceinline__ void ws_load(const Inst &d, const int e0, const int lane, const int i, double2 w[2],
+                                        double2 g[2]) {
+  constexpr int Np = np_of(N);
+  const int e = e0 + lane;
+  if (e < d.K) {
+    const double *wp = d.W + ((size_t)e * Np + i) * 4;
+    w[0] = ld2(wp);
+    w[1] = ld2(wp + 2);
+    g[0] = ld2(d.geo + (size_t)e * 16);
+    g[1] = ld2(d.geo + (size_t)e * 16 + 2);
+  } else {
+    w[0] = w[1] = g[0] = g[1] = make_double2(0.0, 0.0);
+  }
+}
+
+// The nodal fluxes into the slots and W into the staged area (the first part of elem_tile_sym in
+// its tensor-core form), then the wait for this thread's copies of the tile.
+template <int N>
+__device__ __forceinline__ void ws_compute(const Inst &d, const int e0, const int lane, const int i,
+                                           const double2 wv[2], const double2 gv[2], double2 *X, double2 *WQ) {
+  constexpr int Np = np_of(N);
+  constexpr int kS2 = kElemSlot / 2;
+  constexpr int nthr = 32 * Np;
+  const int tid = i * 32 + lane;
+  const bool live = e0 + lane < d.K;
+  const Phys &P = d.P;
+  const double w[4] = {wv[0].x, wv[0].y, wv[1].x, wv[1].y};
+  if (live) {
+    WQ[tid] = wv[0];
+    WQ[nthr + tid] = wv[1];
+  }
+  const double rx = gv[0].x, ry = gv[0].y, sx = gv[1].x, sy = gv[1].y;
   double fr0 = 0, fr1 = 0, fr2 = 0, fr3 = 0, fs0 = 0, fs1 = 0, fs2 = 0, fs3 = 0;
   if (live) {
     const double ir = rcp(w[0]);
@@ -190,28 +218,31 @@ __global__ void __launch_bounds__(ws_threads(N), 1) elem_kernel_ws(const Inst d,
   constexpr int Np = np_of(N), NK = nk_of(N);
   constexpr int NUe = Sym<N>::NUe, NUo = Sym<N>::NUo, NRe = Sym<N>::NRe, NRo = Sym<N>::NRo;
   constexpr int kS2 = kElemSlot / 2;
+  constexpr int B = kWsBufs;
   constexpr unsigned NN = 32 * Np, NC = 32 * kWsCtrWarps;
   extern __shared__ __align__(16) unsigned char ws_sm[];
-  double2 *X[2], *Y[2], *WQ[2];
-  int *Ems[2];
-  for (int b = 0; b < 2; b++) {
+  double2 *X[B], *Y[B], *WQ[B];
+  int *Ems[B];
+  for (int b = 0; b < B; b++) {
     X[b] = reinterpret_cast<double2 *>(ws_sm + b * ws_buf_bytes(N));
     Y[b] = X[b] + NK * kS2;
     Ems[b] = reinterpret_cast<int *>(Y[b] + Np * kS2);
     WQ[b] = reinterpret_cast<double2 *>(Ems[b] + 128);
   }
-  // 0, 1 X full; 2, 3 X empty; 4, 5 Y full; 6, 7 Y empty; 8 pre-pass done; 9 node barrier
-  unsigned long long *bars = reinterpret_cast<unsigned long long *>(ws_sm + 2 * ws_buf_bytes(N));
+  // per buffer b: X full (b), X empty (B + b), Y full (2B + b), Y empty (3B + b); then the
+  // contraction warps' pre-pass barrier (4B) and the node warps' barrier (4B + 1)
+  unsigned long long *bars = reinterpret_cast<unsigned long long *>(ws_sm + B * ws_buf_bytes(N));
+  unsigned long long *xfull = bars, *xempty = bars + B, *yfull = bars + 2 * B, *yempty = bars + 3 * B;
   const int tid = threadIdx.x;
   if (tid == 0) {
-    for (int b = 0; b < 2; b++) {
-      mbar_init(&bars[0 + b], NN);
-      mbar_init(&bars[2 + b], NC);
-      mbar_init(&bars[4 + b], NC);
-      mbar_init(&bars[6 + b], NN);
+    for (int b = 0; b < B; b++) {
+      mbar_init(&xfull[b], NN);
+      mbar_init(&xempty[b], NC);
+      mbar_init(&yfull[b], NC);
+      mbar_init(&yempty[b], NN);
     }
-    mbar_init(&bars[8], NC);
-    mbar_init(&bars[9], NN);
+    mbar_init(&bars[4 * B], NC);
+    mbar_init(&bars[4 * B + 1], NN);
   }
   __syncthreads();
   pdl_trigger();
@@ -221,34 +252,47 @@ __global__ void __launch_bounds__(ws_threads(N), 1) elem_kernel_ws(const Inst d,
   if (tid < (int)NN) {
     const int i = tid >> 5, lane = tid & 31;
     unsigned nphase = 0;
-    const WsNodeSync sync{&bars[9], &nphase, &d};
+    const WsNodeSync sync{&bars[4 * B + 1], &nphase, &d};
+    // tile j uses buffer j % B for the (j / B)-th time; before its copies start, the contraction of
+    // the buffer's previous tile (j - B) must be done with X
+    auto issue = [&](int j) {
+      const int b = j % B, k = j / B;
+      if (k >= 1 && !mbar_wait(&xempty[b], (unsigned)(k - 1) & 1u, kWsWaitLimit)) ws_fail(d);
+      ws_issue<N>(d, stage, (tb + j) * 32, lane, i, X[b], WQ[b]);
+    };
+    double2 wc[2], gc[2], wn[2], gn[2];
+    wn[0] = wn[1] = gn[0] = gn[1] = make_double2(0.0, 0.0);
+    if (n > 0) ws_load<N>(d, tb * 32, lane, i, wc, gc);
     if constexpr (PW) pdl_wait();
+    if (n > 0) issue(0);
     for (int j = 0; j <= n; j++) {
       if (j < n) {
-        const int b = j & 1, k = j >> 1;
-        if (k >= 1 && !mbar_wait(&bars[2 + b], (unsigned)(k - 1) & 1u, kWsWaitLimit)) ws_fail(d);
-        ws_fill<N>(d, stage, (tb + j) * 32, lane, i, X[b], WQ[b]);
-        mbar_arrive(&bars[0 + b]);
+        const int b = j % B;
+        if (j + 1 < n) ws_load<N>(d, (tb + j + 1) * 32, lane, i, wn, gn);
+        ws_compute<N>(d, (tb + j) * 32, lane, i, wc, gc, X[b], WQ[b]);
+        mbar_arrive(&xfull[b]);
+        if (j + 1 < n) issue(j + 1);
       }
       if (j >= 1) {
-        const int jj = j - 1, b = jj & 1, k = jj >> 1;
-        if (!mbar_wait(&bars[4 + b], (unsigned)k & 1u, kWsWaitLimit)) ws_fail(d);
-        ws_combine<N>(d, stage, (tb + jj) * 32, lane, i, Y[b], WQ[b], &bars[6 + b], sync);
+        const int jj = j - 1, b = jj % B, k = jj / B;
+        if (!mbar_wait(&yfull[b], (unsigned)k & 1u, kWsWaitLimit)) ws_fail(d);
+        ws_combine<N>(d, stage, (tb + jj) * 32, lane, i, Y[b], WQ[b], &yempty[b], sync);
       }
+      wc[0] = wn[0]; wc[1] = wn[1]; gc[0] = gn[0]; gc[1] = gn[1];
     }
   } else {
     const int ct = tid - (int)NN, cw = ct >> 5, lane = ct & 31;
     for (int j = 0; j < n; j++) {
-      const int b = j & 1, k = j >> 1;
-      if (!mbar_wait(&bars[0 + b], (unsigned)k & 1u, kWsWaitLimit)) ws_fail(d);
+      const int b = j % B, k = j / B;
+      if (!mbar_wait(&xfull[b], (unsigned)k & 1u, kWsWaitLimit)) ws_fail(d);
       oz_prep<NUe, NUo, kElemSlot>(reinterpret_cast<double *>(X[b]), Ems[b], ct);
-      mbar_arrive(&bars[8]);
-      if (!mbar_wait(&bars[8], (unsigned)j & 1u, kWsWaitLimit)) ws_fail(d);
-      if (k >= 1 && !mbar_wait(&bars[6 + b], (unsigned)(k - 1) & 1u, kWsWaitLimit)) ws_fail(d);
+      mbar_arrive(&bars[4 * B]);
+      if (!mbar_wait(&bars[4 * B], (unsigned)j & 1u, kWsWaitLimit)) ws_fail(d);
+      if (k >= 1 && !mbar_wait(&yempty[b], (unsigned)(k - 1) & 1u, kWsWaitLimit)) ws_fail(d);
       oz_contract<N, NUe, NUo, NRe, NRo>(reinterpret_cast<const double *>(X[b]), reinterpret_cast<double *>(Y[b]), cw,
                                          kWsCtrWarps, lane, Ems[b]);
-      mbar_arrive(&bars[4 + b]);
-      mbar_arrive(&bars[2 + b]);
+      mbar_arrive(&yfull[b]);
+      mbar_arrive(&xempty[b]);
     }
   }
 }

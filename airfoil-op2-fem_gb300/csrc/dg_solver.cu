@@ -930,7 +930,7 @@ static void elem_sym_launch(const Inst &d, int stage, int t0, int t1, cudaStream
     elem_kernel_sym<N, TC, MB, false><<<t1 - t0, dim3(32, Np), smem, s>>>(d, stage, t0);
 }
 
-// 1: the tensor-core element form at N = 3, 4 runs as the warp-specialised persistent kernel
+// 1: the tensor-core element form at N = 3 runs as the warp-specialised persistent kernel
 // (dg_elem_ws.cuh) over one block per SM; 2: the same, a launch over a range of tiles taking the
 // range's share of the SMs; 0: one block per tile (elem_kernel_sym).  Bitwise the same results.
 static int g_elem_ws = 1;

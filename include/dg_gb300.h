@@ -312,10 +312,10 @@ int dg_kernels_per_step(void);
 void dg_set_elem_variant(int variant);
 /* The current element-kernel form. */
 int dg_elem_variant(void);
-/* How the tensor-core element form runs at orders 3 and 4, for launches and graphs built from now
+/* How the tensor-core element form runs at order 3, for launches and graphs built from now
  * on: 1 (default) a warp-specialised persistent kernel, one block per SM walking a contiguous range
  * of 32-cell tiles, node warps staging the next tile and combining the previous one while
- * contraction warps run the current tile's tensor-core product (double-buffered shared memory,
+ * contraction warps run the current tile's tensor-core product (triple-buffered shared memory,
  * bounded mbarrier waits: a wait that runs out makes dg_solver_sync report DG_ERR_TIMEOUT);
  * 2 the same with a launch over a range of tiles taking that range's share of the SMs; 0 one
  * block per tile.  All compute the same bits. */

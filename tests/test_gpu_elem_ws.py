@@ -1,8 +1,8 @@
 """The warp-specialised persistent element kernel (dg_set_elem_ws): one block per SM walks a
 range of 32-cell tiles, node warps staging and combining while contraction warps run the tensor-
 core product, double-buffered.  Same device functions and operation order as the one-block-per-
-tile kernel, so q, the dt sequence and one right-hand side must be bitwise equal to it: at orders
-3 and 4, with a partial last tile, with fewer tiles than SMs (one tile per block), with many tiles
+tile kernel, so q, the dt sequence and one right-hand side must be bitwise equal to it: at order
+3 (the order it serves), with a partial last tile, with fewer tiles than SMs (one tile per block), with many tiles
 per block, over cell ranges, for the vortex app and for one RHS."""
 import numpy as np
 import pytest
@@ -34,7 +34,7 @@ def steps(pkg, mesh, cfg, n, parts=1):
     return go
 
 
-@pytest.mark.parametrize("N", [3, 4])
+@pytest.mark.parametrize("N", [3])
 @pytest.mark.parametrize("grid", ["small", "large"])
 def test_ws_bitwise_equals_tile_kernel(pkg, N, grid):
     # small: 50 tiles, fewer than the SMs (one tile per block, the last one partial: K = 1584);
@@ -63,7 +63,7 @@ def test_ws_vortex_and_rhs_bitwise(pkg):
     got = with_ws(pkg, 1, steps(pkg, mesh, cfg, 20))
     assert np.array_equal(got[0], ref[0]) and got[2] == ref[2]
     m2 = pkg.Mesh.naca_ogrid(64, 16)
-    c2 = pkg.config(N=4, cfl=0.5)
+    c2 = pkg.config(N=3, cfl=0.5)
 
     def rhs():
         s = pkg.Solver(m2, c2).init()
