@@ -932,8 +932,11 @@ static void elem_sym_launch(const Inst &d, int stage, int t0, int t1, cudaStream
 
 // 1: the tensor-core element form at N = 3 runs as the warp-specialised persistent kernel
 // (dg_elem_ws.cuh) over one block per SM; 2: the same, a launch over a range of tiles taking the
-// range's share of the SMs; 0: one block per tile (elem_kernel_sym).  Bitwise the same results.
-static int g_elem_ws = 1;
+// range's share of the SMs; 0 (default): one block per tile (elem_kernel_sym).  Bitwise the same
+// results.  On the K = 32768 O-grid the warp-specialised kernel measured slower (stages 0 / 1 / 2:
+// 61 / 57 / 74 us against 46 / 51 / 61 us): its 8 contraction warps per SM run the integer-heavy
+// product with too little parallelism, where the one-tile blocks bring 30 warps per SM to it.
+static int g_elem_ws = 0;
 
 static int ws_sm_count() {
   static int sms[kMaxDevices] = {0};
@@ -1218,7 +1221,7 @@ int load_order_constants(int N, std::string &err) {
 int order_constants_loaded(int dev, int N) { return (N < 1 || N > 6) ? -1 : g_order_table.done(dev, N); }
 
 void set_elem_variant(int v) { g_elem_variant = (v >= 0 && v <= 3) ? v : 3; }
-void set_elem_ws(int m) { g_elem_ws = (m >= 0 && m <= 2) ? m : 1; }
+void set_elem_ws(int m) { g_elem_ws = (m >= 0 && m <= 2) ? m : 0; }
 int elem_ws() { return g_elem_ws; }
 int elem_variant() { return g_elem_variant; }
 void set_pdl(int on) { g_pdl = on ? 1 : 0; }

@@ -62,8 +62,8 @@ int noalloc_ready(int dev);
 // 1 even/odd FP64, 0 dense FP64.
 void set_elem_variant(int v);
 int elem_variant();
-// The tensor-core element form at N = 3 as the warp-specialised persistent kernel: 1 (default)
-// one block per SM for every launch, 2 a range launch takes its share of the SMs, 0 off (one block
+// The tensor-core element form at N = 3 as the warp-specialised persistent kernel: 1 one block
+// per SM for every launch, 2 a range launch takes its share of the SMs, 0 (default) off (one block
 // per tile).
 void set_elem_ws(int m);
 int elem_ws();

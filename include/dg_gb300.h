@@ -313,12 +313,12 @@ void dg_set_elem_variant(int variant);
 /* The current element-kernel form. */
 int dg_elem_variant(void);
 /* How the tensor-core element form runs at order 3, for launches and graphs built from now
- * on: 1 (default) a warp-specialised persistent kernel, one block per SM walking a contiguous range
+ * on: 0 (default) one block per 32-cell tile; 1 a warp-specialised persistent kernel, one block per SM walking a contiguous range
  * of 32-cell tiles, node warps staging the next tile and combining the previous one while
  * contraction warps run the current tile's tensor-core product (triple-buffered shared memory,
  * bounded mbarrier waits: a wait that runs out makes dg_solver_sync report DG_ERR_TIMEOUT);
- * 2 the same with a launch over a range of tiles taking that range's share of the SMs; 0 one
- * block per tile.  All compute the same bits. */
+ * 2 the same with a launch over a range of tiles taking that range's share of the SMs.  All
+ * compute the same bits; the persistent kernel measured slower on the benchmark mesh. */
 void dg_set_elem_ws(int mode);
 int dg_elem_ws(void);
 /* Host-only (no GPU needed): the tables of the tensor-core contraction of order N (3..5).

@@ -96,3 +96,20 @@ def test_order_tables_query_without_device(pkg):
     for dev, N in ((-1, 3), (64, 3), (0, 0), (0, 7)):
         assert lib.dg_order_tables_loaded(dev, N) == -1
     assert lib.dg_rhs_noalloc_ready(64) == -1
+
+
+def test_persistent_element_kernel_selector(pkg):
+    """Host logic of the warp-specialised element kernel switch: off (0) by default, 0..2 taken
+    as given, anything else back to off."""
+    lib = pkg.lib()
+    prev = lib.dg_elem_ws()
+    try:
+        assert prev == 0
+        for v in (0, 1, 2):
+            lib.dg_set_elem_ws(v)
+            assert lib.dg_elem_ws() == v
+        for v in (-1, 3, 77):
+            lib.dg_set_elem_ws(v)
+            assert lib.dg_elem_ws() == 0
+    finally:
+        lib.dg_set_elem_ws(prev)

@@ -75,8 +75,8 @@ def test_ws_vortex_and_rhs_bitwise(pkg):
 
 def test_ws_setting(pkg):
     lib = pkg.lib()
-    assert lib.dg_elem_ws() == 1
+    assert lib.dg_elem_ws() == 0
     for v in (-1, 3, 9):
         lib.dg_set_elem_ws(v)
-        assert lib.dg_elem_ws() == 1
-    lib.dg_set_elem_ws(1)
+        assert lib.dg_elem_ws() == 0
+    lib.dg_set_elem_ws(0)
