@@ -312,10 +312,10 @@ __device__ __forceinline__ void stage_combine(const Inst &d, const int stage, co
     // those within 1e-4 of the block's estimated maximum are evaluated in FP64.  The FP32
     // estimate (from bit-truncated copies of the state, f32_trunc) is within ~1e-6 of the FP64
     // value, so the block's true maximum is always a candidate and the result equals the
-    // all-FP64 maximum.  (Measured cost of the whole
-    // reduction on the K=32768, N=3 benchmark: 6.2 us of an 86 us stage-2 launch.)
+    // all-FP64 maximum.  Each node-warp evaluates its own candidates (one FP64 pass if it holds
+    // any) and combines them with one atomicMax: no packing of the candidates and no second
+    // barrier with one warp evaluating for the whole block while the others wait.
     __shared__ float s_wmax[32];
-    __shared__ int s_ncand;
     const int fa = active ? c_dtf[N][2 * i] : -1, fb = active ? c_dtf[N][2 * i + 1] : -1;
     const double *ge = d.geo + (size_t)(live ? e : 0) * 16;
     float est = 0.0f;
@@ -334,48 +334,35 @@ __device__ __forceinline__ void stage_combine(const Inst &d, const int stage, co
       for (int o = 16; o > 0; o >>= 1) wm = fmaxf(wm, __shfl_xor_sync(0xffffffffu, wm, o));
       if (lane == 0) s_wmax[i] = wm;
     }
-    if (i == 0 && lane == 0) s_ncand = 0;
-    // every warp is past its contraction here, so the staging area (scratch) is free
     sync();
-    // The block's candidates (often several nodes of one cell, one per node-warp) are packed
-    // into the staging area and evaluated by warp 0 alone: one FP64 evaluation per 32
-    // candidates instead of one per node-warp holding a candidate.
-    double *cand = reinterpret_cast<double *>(scratch);  // [count][5]: q0..q3, fs
-    if (active && live && fa >= 0) {
+    if (active) {
       float bm = 0.0f;
       for (int k = 0; k < Np; k++) bm = fmaxf(bm, s_wmax[k]);
-      if (est >= bm * 0.9999f) {
-        const int slot = atomicAdd(&s_ncand, 1);
-        double *c = cand + 5 * slot;
-        c[0] = n0; c[1] = n1; c[2] = n2; c[3] = n3;
-        c[4] = fb >= 0 ? fmax(ge[6 + 3 * fa], ge[6 + 3 * fb]) : ge[6 + 3 * fa];
+      const bool cand = live && fa >= 0 && est >= bm * 0.9999f;
+      if (__any_sync(0xffffffffu, cand)) {
+        unsigned long long best = 0ull;
+        if (cand) {
+          const double fs = fb >= 0 ? fmax(ge[6 + 3 * fa], ge[6 + 3 * fb]) : ge[6 + 3 * fa];
+          const double ir = rcp(n0);
+          const double u = n1 * ir, v = n2 * ir;
+          const double v2 = fma(u, u, v * v);
+          const double p = P.gm1 * fma(-0.5 * n0, v2, n3);
+          const double cs = sqrt(fabs(P.gam * p * ir));
+          const double spd = ((N + 1) * (N + 1) * 0.5) * (sqrt(v2) + cs);
+          best = (unsigned long long)__double_as_longlong(spd * fs);
+        }
+        // warp max on the bit patterns of non-negative doubles (all 32 lanes take part)
+        for (int o = 16; o > 0; o >>= 1) {
+          const unsigned long long x = __shfl_xor_sync(0xffffffffu, best, o);
+          best = x > best ? x : best;
+        }
+        if (lane == 0 && best) atomicMax(&d.st->dt1_bits, best);
       }
     }
+    // the block may run another tile next (batched kernel): s_wmax is rewritten only after every
+    // warp has read it
     sync();
-    if (i == 0) {
-      const int nc = s_ncand;
-      unsigned long long best = 0ull;
-      for (int k = lane; k < nc; k += 32) {
-        const double *c = cand + 5 * k;
-        const double ir = rcp(c[0]);
-        const double u = c[1] * ir, v = c[2] * ir;
-        const double v2 = fma(u, u, v * v);
-        const double p = P.gm1 * fma(-0.5 * c[0], v2, c[3]);
-        const double cs = sqrt(fabs(P.gam * p * ir));
-        const double spd = ((N + 1) * (N + 1) * 0.5) * (sqrt(v2) + cs);
-        const unsigned long long b = (unsigned long long)__double_as_longlong(spd * c[4]);
-        best = b > best ? b : best;
-      }
-      // warp max on the bit patterns of non-negative doubles (all 32 lanes take part)
-      for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long x = __shfl_xor_sync(0xffffffffu, best, o);
-        best = x > best ? x : best;
-      }
-      if (lane == 0 && best) atomicMax(&d.st->dt1_bits, best);
-    }
-    // the block may run another tile next (batched kernel): the staging area and s_wmax are
-    // rewritten only after warp 0 has read them
-    sync();
+    (void)scratch;
   }
 }
 
