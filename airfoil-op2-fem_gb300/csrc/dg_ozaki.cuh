@@ -251,37 +251,66 @@ __device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *_
       for (int s = 0; s + j < 7; s++) mma_bf16_16816(acc[j + s], a, __ldg(bfr + (s * 2 + ks) * 32));
     }
   }
-  // C fragment: acc[.][0] (row g, col 2t), [1] (g, 2t+1), [2] (g+8, 2t), [3] (g+8, 2t+1)
+  // C fragment: acc[.][0] (row g, col 2t), [1] (g, 2t+1), [2] (g+8, 2t), [3] (g+8, 2t+1).
+  // One output: the level sums lev[] of (row g + 8 r, operator row n) joined and rounded.
+  auto finish = [&](const float lev[7], const int n, const int r) {
+    long long l[7];
 #pragma unroll
-  for (int r = 0; r < 2; r++)
+    for (int L = 0; L < 7; L++) l[L] = (long long)__float2int_rz(lev[L]);
+    const long long th = l[0] * 65536LL + l[1] * 256LL + l[2];
+    const long long tl = l[3] * 16777216LL + l[4] * 65536LL + l[5] * 256LL + l[6];
+    const int fe = c_ozf[T][NORD][P][n];
+    const int sc = em[r] + fe - 2046 - 62 + (3 - SH);
+    double out;
+    if (em[r] == 0x7FF) {
+      out = __longlong_as_double(0x7FF8000000000000LL);
+    } else if (sc >= -1022 && sc <= 900) {
+      out = oz_round(th, tl, sc);
+    } else if (sc < -1022) {
+      out = 0.0;  // below 2^-1022: negligible against any physical value
+    } else {
+      const double val = fma((double)th, 4294967296.0, (double)tl);
+      const int s1 = sc / 2, s2 = sc - s1;  // each <= 992: two exact power-of-two scalings
+      out = (val * __longlong_as_double((long long)(s1 + 1023) << 52)) *
+            __longlong_as_double((long long)(s2 + 1023) << 52);
+    }
+    Yd[(YROW0 + n) * XST + col + 8 * r] = out;
+  };
+  constexpr int RV = R - 8 * NT;  // operator rows of this n-tile that exist (1..8)
+  if constexpr (RV <= 4) {
+    // Only lanes t = 0, 1 hold outputs (columns 2t + cc < RV): lanes t = 2, 3 take the row-(g + 8)
+    // outputs of lane t - 2 (their level sums by shuffle), so the rounding, the costly part, runs
+    // on all four lanes of a group with half the outputs each.  Same values, same rounding.
+    const bool hi = t >= 2;
+    const int src = hi ? lane - 2 : lane;
+    float lv[2][7];
+#pragma unroll
+    for (int L = 0; L < 7; L++)
+#pragma unroll
+      for (int cc = 0; cc < 2; cc++) {
+        const float x = __shfl_sync(0xffffffffu, acc[L][2 + cc], src);
+        lv[cc][L] = hi ? x : acc[L][cc];
+      }
+    const int tt = hi ? t - 2 : t, r = hi ? 1 : 0;
 #pragma unroll
     for (int cc = 0; cc < 2; cc++) {
-      const int n = 8 * NT + 2 * t + cc;
-      if (n < R) {
-        const int o = 2 * r + cc;
-        long long l[7];
-#pragma unroll
-        for (int L = 0; L < 7; L++) l[L] = (long long)__float2int_rz(acc[L][o]);
-        const long long th = l[0] * 65536LL + l[1] * 256LL + l[2];
-        const long long tl = l[3] * 16777216LL + l[4] * 65536LL + l[5] * 256LL + l[6];
-        const int fe = c_ozf[T][NORD][P][n];
-        const int sc = em[r] + fe - 2046 - 62 + (3 - SH);
-        double out;
-        if (em[r] == 0x7FF) {
-          out = __longlong_as_double(0x7FF8000000000000LL);
-        } else if (sc >= -1022 && sc <= 900) {
-          out = oz_round(th, tl, sc);
-        } else if (sc < -1022) {
-          out = 0.0;  // below 2^-1022: negligible against any physical value
-        } else {
-          const double val = fma((double)th, 4294967296.0, (double)tl);
-          const int s1 = sc / 2, s2 = sc - s1;  // each <= 992: two exact power-of-two scalings
-          out = (val * __longlong_as_double((long long)(s1 + 1023) << 52)) *
-                __longlong_as_double((long long)(s2 + 1023) << 52);
-        }
-        Yd[(YROW0 + n) * XST + col + 8 * r] = out;
-      }
+      const int n = 8 * NT + 2 * tt + cc;
+      if (n < R) finish(lv[cc], n, r);
     }
+  } else {
+#pragma unroll
+    for (int r = 0; r < 2; r++)
+#pragma unroll
+      for (int cc = 0; cc < 2; cc++) {
+        const int n = 8 * NT + 2 * t + cc;
+        if (n < R) {
+          float lev[7];
+#pragma unroll
+          for (int L = 0; L < 7; L++) lev[L] = acc[L][2 * r + cc];
+          finish(lev, n, r);
+        }
+      }
+  }
 }
 
 // Parity 0: K0 staged slots from slot 0 to R0 outputs from row 0; parity 1: K1 slots from SLOT1
