@@ -125,6 +125,8 @@ def lib():
         "dg_kernels_per_step": (C.c_int, []),
         "dg_set_elem_variant": (None, [C.c_int]),
         "dg_set_elem_ws": (None, [C.c_int]),
+        "dg_set_elem_blocks_per_sm": (None, [C.c_int]),
+        "dg_elem_blocks_per_sm": (C.c_int, []),
         "dg_elem_ws": (C.c_int, []),
         "dg_elem_variant": (C.c_int, []),
         "dg_tc_operator_digits": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -675,6 +675,8 @@ int dg_step_graph_flags(void) { return dg::step_graph_flags(); }
 void dg_set_elem_variant(int variant) { dg::set_elem_variant(variant); }
 int dg_elem_variant(void) { return dg::elem_variant(); }
 void dg_set_elem_ws(int mode) { dg::set_elem_ws(mode); }
+void dg_set_elem_blocks_per_sm(int blocks) { dg::set_elem_blocks_per_sm(blocks); }
+int dg_elem_blocks_per_sm(void) { return dg::elem_blocks_per_sm(); }
 int dg_elem_ws(void) { return dg::elem_ws(); }
 
 int dg_tc_operator_digits(int N, int *dims, double *S, int *fexp, int *digits) {

@@ -925,6 +925,11 @@ static void elem_sym_launch(const Inst &d, int stage, int t0, int t1, cudaStream
 // product with too little parallelism, where the one-tile blocks bring 30 warps per SM to it.
 static int g_elem_ws = 0;
 
+// Resident blocks per SM that the order-3 tensor-core element kernel is compiled for: 3 (the
+// default: 64 registers, a small spill) or 2 (more registers, no spill, and room beside two
+// element blocks for face-kernel blocks of another cell range in the step graph).
+static int g_elem_mb = 3;
+
 static int ws_sm_count() {
   static int sms[kMaxDevices] = {0};
   int dev = 0;
@@ -959,6 +964,10 @@ static void launch_elem_form(const Inst &d, int stage, int t0, int t1, cudaStrea
     if (g_elem_variant == 3) return elem_sym_launch<N, 2, oz_min_blocks(N)>(d, stage, t0, t1, s, attr);
   }
   if constexpr (oz_used(N, true)) {
+    if constexpr (N == 3) {
+      // the register budget of two resident blocks per SM instead of three (g_elem_mb)
+      if (g_elem_variant >= 2 && g_elem_mb == 2) return elem_sym_launch<N, 1, 2>(d, stage, t0, t1, s, attr);
+    }
     if (g_elem_variant >= 2) return elem_sym_launch<N, 1, oz_min_blocks(N)>(d, stage, t0, t1, s, attr);
   }
   elem_sym_launch<N, 0, 1>(d, stage, t0, t1, s, attr);
@@ -1006,6 +1015,7 @@ static cudaError_t set_smem_attr() {
   both(elem_kernel_sym<N, 0, 1, true>, elem_kernel_sym<N, 0, 1, false>);
   if constexpr (oz_used(N, true))
     both(elem_kernel_sym<N, 1, oz_min_blocks(N), true>, elem_kernel_sym<N, 1, oz_min_blocks(N), false>);
+  if constexpr (N == 3) both(elem_kernel_sym<N, 1, 2, true>, elem_kernel_sym<N, 1, 2, false>);
   if constexpr (ozd_used(N, 2))
     both(elem_kernel_sym<N, 2, oz_min_blocks(N), true>, elem_kernel_sym<N, 2, oz_min_blocks(N), false>);
   if constexpr (ws_used(N)) {
@@ -1209,6 +1219,8 @@ int order_constants_loaded(int dev, int N) { return (N < 1 || N > 6) ? -1 : g_or
 
 void set_elem_variant(int v) { g_elem_variant = (v >= 0 && v <= 3) ? v : 3; }
 void set_elem_ws(int m) { g_elem_ws = (m >= 0 && m <= 2) ? m : 0; }
+void set_elem_blocks_per_sm(int b) { g_elem_mb = (b == 2) ? 2 : 3; }
+int elem_blocks_per_sm() { return g_elem_mb; }
 int elem_ws() { return g_elem_ws; }
 int elem_variant() { return g_elem_variant; }
 void set_pdl(int on) { g_pdl = on ? 1 : 0; }

@@ -67,6 +67,9 @@ int elem_variant();
 // per tile).
 void set_elem_ws(int m);
 int elem_ws();
+// Resident blocks per SM the order-3 tensor-core element kernel is compiled for (3 default, or 2).
+void set_elem_blocks_per_sm(int b);
+int elem_blocks_per_sm();
 // Host-only: parity dimensions {NUe, NUo, NRe, NRo}, even/odd operator blocks, row exponents
 // [parity][32] and signed base-256 digits [parity][digit][slot 32][row 32] of the tensor-core
 // contraction of order N.

@@ -321,6 +321,11 @@ int dg_elem_variant(void);
  * compute the same bits; the persistent kernel measured slower on the benchmark mesh. */
 void dg_set_elem_ws(int mode);
 int dg_elem_ws(void);
+/* Resident blocks per SM the order-3 tensor-core element kernel (one block per tile) is compiled
+ * for: 3 (default; 64 registers) or 2 (more registers, and room for face-kernel blocks of other
+ * cell ranges beside it in the step graph); other values select 3.  Same bits either way. */
+void dg_set_elem_blocks_per_sm(int blocks);
+int dg_elem_blocks_per_sm(void);
 /* Host-only (no GPU needed): the tables of the tensor-core contraction of order N (3..5).
  * dims[4] receives NUe, NUo, NRe, NRo; S (NRe*NUe + NRo*NUo doubles, may be NULL) the even then
  * odd operator blocks row-major; fexp (2 x 32 ints, may be NULL) each row's biased binary

@@ -80,3 +80,22 @@ def test_ws_setting(pkg):
         lib.dg_set_elem_ws(v)
         assert lib.dg_elem_ws() == 0
     lib.dg_set_elem_ws(0)
+
+
+def test_two_blocks_per_sm_variant_bitwise(pkg):
+    """The order-3 tile kernel compiled for two resident blocks per SM instead of three (more
+    registers): the same bits, chain and cell ranges."""
+    lib = pkg.lib()
+    mesh = pkg.Mesh.naca_ogrid(128, 32)
+    cfg = pkg.config(N=3, cfl=0.5, mach=0.45, alpha_deg=1.0)
+    ref = steps(pkg, mesh, cfg, 10)()
+    prev = lib.dg_elem_blocks_per_sm()
+    lib.dg_set_elem_blocks_per_sm(2)
+    try:
+        assert lib.dg_elem_blocks_per_sm() == 2
+        got = steps(pkg, mesh, cfg, 10)()
+        got4 = steps(pkg, mesh, cfg, 10, parts=4)()
+    finally:
+        lib.dg_set_elem_blocks_per_sm(prev)
+    assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
+    assert np.array_equal(got4[0], ref[0]) and np.array_equal(got4[1], ref[1])
