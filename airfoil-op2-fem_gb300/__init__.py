@@ -132,6 +132,8 @@ def lib():
         "dg_tc_operator_digits": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
         "dg_tc_round": (C.c_int, [C.c_longlong, C.c_longlong, C.c_int, C.c_void_p]),
         "dg_set_face_block": (None, [C.c_int]),
+        "dg_set_face_regs64": (None, [C.c_int]),
+        "dg_face_regs64": (C.c_int, []),
         "dg_set_pdl": (None, [C.c_int]),
         "dg_batch_create": (C.c_int, [C.c_int, C.POINTER(Config), C.POINTER(vp), C.POINTER(vp)]),
         "dg_batch_init": (C.c_int, [vp]),

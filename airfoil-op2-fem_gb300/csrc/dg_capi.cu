@@ -701,6 +701,8 @@ int dg_tc_round(long long th, long long tl, int sc, double *out) {
   return 0;
 }
 void dg_set_face_block(int threads) { dg::set_face_block(threads); }
+void dg_set_face_regs64(int on) { dg::set_face_regs64(on); }
+int dg_face_regs64(void) { return dg::face_regs64(); }
 void dg_set_pdl(int on) { dg::set_pdl(on); }
 
 int dg_order_tables_loaded(int device, int N) { return dg::order_constants_loaded(device, N); }

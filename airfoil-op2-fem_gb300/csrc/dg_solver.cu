@@ -221,6 +221,16 @@ __global__ void __launch_bounds__(256) face_kernel(const Inst d, const int stage
   face_node<N, true>(d, stage, tid);
 }
 
+// The same in 64-thread blocks compiled for 16 resident blocks per SM (at most 64 registers):
+// one such block fits on an SM beside three order-3 element blocks (3 x 20,480 + 4,096 = 65,536
+// registers), so face blocks of one cell range can run next to element blocks of another.
+template <int N>
+__global__ void __launch_bounds__(64, 16) face_kernel_r64(const Inst d, const int stage) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= (d.nE + d.nB) * (N + 1)) return;
+  face_node<N, true>(d, stage, tid);
+}
+
 // double -> float by truncation of the bit pattern, with integer instructions only (the
 // conversion instruction occupies the FP64 pipe).  Relative error below 2^-23; magnitudes below
 // 2^-126 give +-0, above the float range (and inf, NaN) +-inf.  For the dt estimate only.
@@ -854,6 +864,8 @@ __global__ void vertex_fields_kernel(int K, const int *cells, const int *owner, 
 // 64 threads measured 58.5 / 61.8 us per stage at N=3 / N=4 on the K=32768 O-grid against
 // 65.9 / 74.0 us with 256.
 static int g_face_block = 64;
+// 1: 64-thread face blocks use face_kernel_r64 (at most 64 registers).
+static int g_face_r64 = 0;
 
 // 1: face and element kernels of the plain path are launched with programmatic stream
 // serialisation (each may start while its predecessor drains), 0: plain stream order.
@@ -892,7 +904,10 @@ template <int N>
 static void launch_face(const Inst &d, int stage, cudaStream_t s) {
   const long long nf = ((long long)d.nE + d.nB) * (N + 1);
   const int bs = g_face_block;
-  launch_pdl(face_kernel<N>, dim3((unsigned)((nf + bs - 1) / bs)), dim3(bs), 0, s, d, stage);
+  if (g_face_r64 && bs == 64)
+    launch_pdl(face_kernel_r64<N>, dim3((unsigned)((nf + bs - 1) / bs)), dim3(bs), 0, s, d, stage);
+  else
+    launch_pdl(face_kernel<N>, dim3((unsigned)((nf + bs - 1) / bs)), dim3(bs), 0, s, d, stage);
 }
 
 // 3: dense rows on the bf16 tensor cores at N = 1, 2 (dg_ozaki.cuh), form 2 at the other orders
@@ -1224,6 +1239,8 @@ int elem_blocks_per_sm() { return g_elem_mb; }
 int elem_ws() { return g_elem_ws; }
 int elem_variant() { return g_elem_variant; }
 void set_pdl(int on) { g_pdl = on ? 1 : 0; }
+void set_face_regs64(int on) { g_face_r64 = on ? 1 : 0; }
+int face_regs64() { return g_face_r64; }
 void set_face_block(int b) { g_face_block = (b >= 32 && b <= 256 && b % 32 == 0) ? b : 64; }
 
 // ---------------------------------------------------------------- Solver (host)

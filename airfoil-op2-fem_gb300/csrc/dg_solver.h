@@ -80,6 +80,9 @@ int tc_operator_tables(int N, int dims[4], std::vector<double> &S, int fexp[2][3
 double tc_round(long long th, long long tl, int sc);
 // Threads per face-kernel block for launches enqueued from now on (32..256, multiple of 32).
 void set_face_block(int b);
+// 64-thread face blocks compiled for at most 64 registers (1) or unbounded (0, default).
+void set_face_regs64(int on);
+int face_regs64();
 // Programmatic dependent launch of the plain path's face and element kernels (default on).
 void set_pdl(int on);
 // Cell ranges of the step graph (Solver::build_graph): 0 automatic, 1 one range (a chain of

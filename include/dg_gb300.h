@@ -349,6 +349,10 @@ void dg_set_step_graph_flags(int flags);
 int dg_step_graph_flags(void);
 /* Threads per face-kernel block of the plain path (32..256, multiple of 32; default 64). */
 void dg_set_face_block(int threads);
+/* 64-thread face blocks compiled for at most 64 registers (1; one fits beside three order-3 element
+ * blocks on an SM) or without a bound (0, default).  Same bits. */
+void dg_set_face_regs64(int on);
+int dg_face_regs64(void);
 /* Launch the plain path's face and element kernels with programmatic dependent launch (1, the
  * default: each may start while its predecessor drains) or in plain stream order (0).  Both give
  * bit-identical results; applies to launches and graphs built from now on. */

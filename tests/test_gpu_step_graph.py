@@ -130,3 +130,18 @@ def test_step_host_over_ranges_equals_run(pkg, nsteps, pinned):
         b.sync()
         assert np.array_equal(h_out, b.get("q")), call
         assert np.array_equal(a.get("q"), b.get("q")) and a.time() == b.time(), call
+
+
+def test_face_kernel_register_bound_bitwise(pkg):
+    """The face kernel compiled for at most 64 registers: the same bits, chain and ranges."""
+    lib = pkg.lib()
+    mesh = pkg.Mesh.naca_ogrid(96, 24, farfield="characteristic")
+    cfg = pkg.config(N=3, cfl=0.5, mach=0.5, alpha_deg=2.0)
+    q1, dt1, _, _ = run_parts(pkg, mesh, cfg, 1, 20)
+    lib.dg_set_face_regs64(1)
+    try:
+        for P in (1, 4):
+            q, dt, _, _ = run_parts(pkg, mesh, cfg, P, 20)
+            assert np.array_equal(q, q1) and np.array_equal(dt, dt1), P
+    finally:
+        lib.dg_set_face_regs64(0)
