@@ -14,9 +14,16 @@ value   device-resident: CUDA events around each step's graph launch on the
         solver stream, L2 flushed (512 MB write) between steps outside the events.
 e2e     the C-ABI call dg_solver_step_host with pinned host buffers: H2D of q,
         one step, D2H of q, timed with events on the same stream.
-roofline  FP64-bound: algorithmic flops of the dominant kernel per launch over
-        its event-timed launch duration (dg_solver_step_timed), against the DFMA
-        peak measured live on this GPU.
+roofline  the dominant kernel's binding roof: its FP64-pipe instructions (per-unit
+        counts from ncu, FP64_INST_*), algorithmic HBM bytes and mma flops over its
+        event-timed duration (dg_solver_step_timed), against the FP64 pipe rate
+        (half the DFMA peak, measured live), MEASURED_PEAKS.json's copy bandwidth
+        and the mma.sync bf16 rate (measured live); plus the step's FP64-pipe
+        fraction over the graph step time.
+legs    the OP2 drop-in C++ application, the 64-instance batched sweep (and small
+        instances), the adjoint case, the advection app, device mesh set-up and
+        the large vortex case (each --no-<leg> skips it); clocks are sampled over
+        all of them.
 --impl reference  the CPU oracle (the reference's user kernels, restated, driven
         OP2-openmp style on all host cores) on the same workload.
 Multi-GPU: replicas only (the path is one mesh per GPU); each rank runs the
