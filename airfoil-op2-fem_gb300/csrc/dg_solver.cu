@@ -27,6 +27,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstddef>
 #include <cmath>
 #include <cstdint>
@@ -863,17 +864,21 @@ __global__ void vertex_fields_kernel(int K, const int *cells, const int *owner, 
 // (SM active 70 % of the launch).  Small blocks let the block scheduler balance that tail:
 // 64 threads measured 58.5 / 61.8 us per stage at N=3 / N=4 on the K=32768 O-grid against
 // 65.9 / 74.0 us with 256.
-static int g_face_block = 64;
+static std::atomic<int> g_face_block{64};
 // 1: 64-thread face blocks use face_kernel_r64 (at most 64 registers).
-static int g_face_r64 = 0;
+static std::atomic<int> g_face_r64{0};
 
 // 1: face and element kernels of the plain path are launched with programmatic stream
 // serialisation (each may start while its predecessor drains), 0: plain stream order.
-static int g_pdl = 1;
+static std::atomic<int> g_pdl{1};
+// Set by this thread while it enqueues the step graph over cell ranges without programmatic
+// launch (the process-wide setting stays as it is for other threads).
+static thread_local int t_no_pdl = 0;
+static inline bool pdl_on() { return g_pdl.load(std::memory_order_relaxed) && !t_no_pdl; }
 
-// Scheduling priority given to the launches made while g_launch_prio_on is set (the step graph
-// over cell ranges sets it per range; lower numbers are scheduled first).
-static int g_launch_prio_on = 0, g_launch_prio = 0;
+// Scheduling priority given to the launches this thread makes while g_launch_prio_on is set (the
+// step graph over cell ranges sets it per range; lower numbers are scheduled first).
+static thread_local int g_launch_prio_on = 0, g_launch_prio = 0;
 
 template <class... KArgs, class... Args>
 static void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
@@ -885,7 +890,7 @@ static void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t s
   cfg.stream = s;
   cudaLaunchAttribute attr[2];
   int na = 0;
-  if (g_pdl) {
+  if (pdl_on()) {
     attr[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[na].val.programmaticStreamSerializationAllowed = 1;
     na++;
@@ -914,7 +919,7 @@ static void launch_face(const Inst &d, int stage, cudaStream_t s) {
 // (default);
 // 2: even/odd with the contraction on the bf16 tensor cores (at N = 3, 4, 5, the even/odd FP64
 // kernel at the other orders), 1: even/odd element kernel, 0: dense FP64.
-static int g_elem_variant = 3;
+static std::atomic<int> g_elem_variant{3};
 
 // The even/odd element kernel instance for form TC at order N, launched over tiles [t0, t1):
 // with the launch attributes of launch_pdl (attr true) or as a plain launch.  The instance
@@ -924,7 +929,7 @@ template <int N, int TC, int MB>
 static void elem_sym_launch(const Inst &d, int stage, int t0, int t1, cudaStream_t s, bool attr) {
   constexpr int Np = np_of(N);
   const size_t smem = elem_sym_smem(N);
-  if (attr && g_pdl)
+  if (attr && pdl_on())
     launch_pdl(elem_kernel_sym<N, TC, MB, true>, dim3(t1 - t0), dim3(32, Np), smem, s, d, stage, t0);
   else if (attr)
     launch_pdl(elem_kernel_sym<N, TC, MB, false>, dim3(t1 - t0), dim3(32, Np), smem, s, d, stage, t0);
@@ -938,12 +943,12 @@ static void elem_sym_launch(const Inst &d, int stage, int t0, int t1, cudaStream
 // results.  On the K = 32768 O-grid the warp-specialised kernel measured slower (stages 0 / 1 / 2:
 // 61 / 57 / 74 us against 46 / 51 / 61 us): its 8 contraction warps per SM run the integer-heavy
 // product with too little parallelism, where the one-tile blocks bring 30 warps per SM to it.
-static int g_elem_ws = 0;
+static std::atomic<int> g_elem_ws{0};
 
 // Resident blocks per SM that the order-3 tensor-core element kernel is compiled for: 3 (the
 // default: 64 registers, a small spill) or 2 (more registers, no spill, and room beside two
 // element blocks for face-kernel blocks of another cell range in the step graph).
-static int g_elem_mb = 3;
+static std::atomic<int> g_elem_mb{3};
 
 static int ws_sm_count() {
   static int sms[kMaxDevices] = {0};
@@ -959,7 +964,7 @@ static void elem_ws_launch(const Inst &d, int stage, int t0, int t1, cudaStream_
   int grid = g_elem_ws == 2 ? (int)(((long long)sms * (t1 - t0) + T - 1) / T) : sms;
   grid = std::max(1, std::min(grid, t1 - t0));
   const size_t smem = ws_smem(N);
-  if (attr && g_pdl)
+  if (attr && pdl_on())
     launch_pdl(elem_kernel_ws<N, true>, dim3(grid), dim3(ws_threads(N)), smem, s, d, stage, t0, t1);
   else if (attr)
     launch_pdl(elem_kernel_ws<N, false>, dim3(grid), dim3(ws_threads(N)), smem, s, d, stage, t0, t1);
@@ -1431,7 +1436,7 @@ int Solver::build_graph(std::string &err) {
   else enqueue_step(stream);
   cudaError_t ce = cudaStreamEndCapture(stream, &graph);
   if (ce != cudaSuccess) { err = std::string("graph capture: ") + cudaGetErrorString(ce); return -6; }
-  const unsigned long long flags = (parts > 1 && (step_graph_flags() & 2)) ? cudaGraphInstantiateFlagUseNodePriority : 0;
+  const unsigned long long flags = (parts > 1 && (step_graph_flags() & 6)) ? cudaGraphInstantiateFlagUseNodePriority : 0;
   CK(cudaGraphInstantiate(&graph_exec, graph, flags));
   return 0;
 }
@@ -1450,18 +1455,19 @@ int Solver::build_graph(std::string &err) {
 // launch computes exactly what the one-range step computes for its faces and tiles (every face
 // slot has one writer), so the result is bitwise the same for every P.  With a mesh numbered
 // with locality (O-grid rings, square rows) lo_p and hi_p are p-1 and p+1.
-static int g_step_parts = 0;  // 0: automatic (step_parts_for), 1: the single-range chain
+static std::atomic<int> g_step_parts{0};  // 0: automatic (step_parts_for), 1: the single-range chain
+// bit 2: element launches get a higher scheduling priority than face launches.
 // bit 0: launch the ranges' kernels without programmatic dependent launch (the default: with it,
 // dependent launches start early and their waiting blocks hold SM slots the other ranges' kernels
 // could use: 300 vs 267 us per step at 4 ranges); bit 1: give range p's launches a scheduling
 // priority that falls with p (earlier ranges first; measured no faster).
-static int g_step_graph_flags = 1;
-void set_step_graph_flags(int f) { g_step_graph_flags = f & 3; }
+static std::atomic<int> g_step_graph_flags{1};
+void set_step_graph_flags(int f) { g_step_graph_flags = f & 7; }
 int step_graph_flags() { return g_step_graph_flags; }
 
 int step_parts_for(int K) {
-  const int T = (K + 31) / 32;
-  if (g_step_parts >= 1) return std::max(1, std::min(g_step_parts, std::min(kMaxStepParts, T)));
+  const int T = (K + 31) / 32, sp = g_step_parts.load();
+  if (sp >= 1) return std::max(1, std::min(sp, std::min(kMaxStepParts, T)));
   // automatic: ranges of at least 128 tiles, at most 4 (on the K = 32768 O-grid at N = 3, steps of
   // 290 / 267 / 269 / 271 us with 1 / 4 / 8 / 16 ranges; more ranges add launches and edges)
   return std::max(1, std::min(4, T / 128));
@@ -1550,14 +1556,18 @@ void Solver::enqueue_step_parts(cudaStream_t s, const double *q_in, double *q_ou
     c0 = (size_t)ptile0[p] * 32;
     nc = std::min((size_t)ptile0[p + 1] * 32, (size_t)K) - c0;
   };
-  const int pdl_saved = g_pdl;
-  if (g_step_graph_flags & 1) g_pdl = 0;
+  t_no_pdl = (g_step_graph_flags & 1) ? 1 : 0;
   int prio_lo = 0, prio_hi = 0;  // least and greatest priority (numerically: hi <= lo)
   cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
-  auto set_prio = [&](int p) {
-    if (!(g_step_graph_flags & 2)) return;
-    g_launch_prio_on = 1;
-    g_launch_prio = prio_hi + (int)((long long)(prio_lo - prio_hi) * p / std::max(1, P - 1));
+  // bit 1: earlier ranges first; bit 2: element launches before face launches
+  auto set_prio = [&](int p, bool elem) {
+    if (g_step_graph_flags & 2) {
+      g_launch_prio_on = 1;
+      g_launch_prio = prio_hi + (int)((long long)(prio_lo - prio_hi) * p / std::max(1, P - 1));
+    } else if (g_step_graph_flags & 4) {
+      g_launch_prio_on = 1;
+      g_launch_prio = elem ? prio_hi : prio_lo;
+    }
   };
   cudaEvent_t fork = pevents[6 * P];
   auto evF = [&](int st, int p) { return pevents[(2 * st) * P + p]; };
@@ -1590,7 +1600,7 @@ void Solver::enqueue_step_parts(cudaStream_t s, const double *q_in, double *q_ou
       dp.bedges = pbedges + pb0[p];
       dp.nB = pb0[p + 1] - pb0[p];
       dp.bxy = pbxy + (size_t)pb0[p] * Nfp * 2;
-      set_prio(p);
+      set_prio(p, false);
       if (dp.nE + dp.nB > 0) DG_DISPATCH(cfg.N, launch_face<NN>(dp, stage, ps));
       g_launch_prio_on = 0;
       cudaEventRecord(evF(stage, p), ps);
@@ -1598,7 +1608,7 @@ void Solver::enqueue_step_parts(cudaStream_t s, const double *q_in, double *q_ou
     for (int p = 0; p < P; p++) {
       cudaStream_t ps = pstreams[p];
       for (int q = p + 1; q <= phi[p]; q++) cudaStreamWaitEvent(ps, evF(stage, q), 0);
-      set_prio(p);
+      set_prio(p, true);
       DG_DISPATCH(cfg.N, launch_elem_range<NN>(d, stage, ptile0[p], ptile0[p + 1], ps));
       g_launch_prio_on = 0;
       cudaEventRecord(evE(stage, p), ps);
@@ -1615,7 +1625,7 @@ void Solver::enqueue_step_parts(cudaStream_t s, const double *q_in, double *q_ou
     cudaStreamWaitEvent(s, evE(2, p), 0);
   }
   launch_pdl(finalize_kernel, dim3(1), dim3(32), 0, s, d.st, d.dt_mode, d.dt_hist, d.dt_hist_len);
-  g_pdl = pdl_saved;
+  t_no_pdl = 0;
 }
 
 // One step with host buffers through a captured graph over the cell ranges: each range's input

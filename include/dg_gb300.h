@@ -343,8 +343,9 @@ void dg_set_step_parts(int parts);
 int dg_step_parts(void);
 /* Tuning of that graph (more than one range) for graphs built from now on: bit 0 launches its
  * kernels without programmatic dependent launch, bit 1 gives range p's launches a scheduling
- * priority falling with p (earlier ranges scheduled first).  1 by default.  Results are
- * bitwise the same. */
+ * priority falling with p (earlier ranges scheduled first), bit 2 gives element launches a higher
+ * priority than face launches (when bit 1 is clear).  1 by default.  Results are bitwise the
+ * same. */
 void dg_set_step_graph_flags(int flags);
 int dg_step_graph_flags(void);
 /* Threads per face-kernel block of the plain path (32..256, multiple of 32; default 64). */

@@ -37,7 +37,7 @@ def shuffled(m, seed):
     return out
 
 
-@pytest.mark.parametrize("flags", [0, 1, 2, 3])
+@pytest.mark.parametrize("flags", [0, 1, 2, 3, 5])
 def test_graph_flags_bitwise_equal(pkg, flags):
     """With and without programmatic dependent launch between the ranges' kernels, with and
     without per-range priorities: the same bits."""
