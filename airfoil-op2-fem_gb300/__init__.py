@@ -170,6 +170,8 @@ def lib():
         "dg_bf16_mma_peak_gflops": (C.c_double, []),
         "dg_set_step_parts": (None, [C.c_int]),
         "dg_step_parts": (C.c_int, []),
+        "dg_set_steps_per_graph": (None, [C.c_int]),
+        "dg_steps_per_graph": (C.c_int, []),
         "dg_set_step_graph_flags": (None, [C.c_int]),
         "dg_step_graph_flags": (C.c_int, []),
         "dg_boundary_state": (C.c_int, [C.POINTER(Config), C.c_int, C.c_int, dp, dp, dp]),

@@ -670,6 +670,8 @@ double dg_bf16_mma_peak_gflops(void) {
 int dg_kernels_per_step(void) { return 7; }
 void dg_set_step_parts(int parts) { dg::set_step_parts(parts); }
 int dg_step_parts(void) { return dg::step_parts(); }
+void dg_set_steps_per_graph(int steps) { dg::set_steps_per_graph(steps); }
+int dg_steps_per_graph(void) { return dg::steps_per_graph(); }
 void dg_set_step_graph_flags(int flags) { dg::set_step_graph_flags(flags); }
 int dg_step_graph_flags(void) { return dg::step_graph_flags(); }
 void dg_set_elem_variant(int variant) { dg::set_elem_variant(variant); }

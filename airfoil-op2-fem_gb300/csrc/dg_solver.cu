@@ -1271,6 +1271,8 @@ Solver::~Solver() {
   if (graph) cudaGraphDestroy(graph);
   if (io_graph_exec) cudaGraphExecDestroy(io_graph_exec);
   if (io_graph) cudaGraphDestroy(io_graph);
+  if (graphG_exec) cudaGraphExecDestroy(graphG_exec);
+  if (graphG) cudaGraphDestroy(graphG);
   for (void *p : allocs) cudaFree(p);
   if (stream) cudaStreamDestroy(stream);
 }
@@ -1431,13 +1433,20 @@ int Solver::build_graph(std::string &err) {
   } else {
     parts = 1;
   }
-  CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-  if (parts > 1) enqueue_step_parts(stream);
-  else enqueue_step(stream);
-  cudaError_t ce = cudaStreamEndCapture(stream, &graph);
-  if (ce != cudaSuccess) { err = std::string("graph capture: ") + cudaGetErrorString(ce); return -6; }
   const unsigned long long flags = (parts > 1 && (step_graph_flags() & 6)) ? cudaGraphInstantiateFlagUseNodePriority : 0;
-  CK(cudaGraphInstantiate(&graph_exec, graph, flags));
+  // one step, and (over cell ranges) graph_steps steps in one graph
+  graph_steps = parts > 1 ? steps_per_graph() : 1;
+  for (int k = 0; k < (graph_steps > 1 ? 2 : 1); k++) {
+    const int G = k == 0 ? 1 : graph_steps;
+    cudaGraph_t &gr = k == 0 ? graph : graphG;
+    cudaGraphExec_t &ex = k == 0 ? graph_exec : graphG_exec;
+    CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    if (parts > 1) enqueue_step_parts(stream, nullptr, nullptr, G);
+    else enqueue_step(stream);
+    cudaError_t ce = cudaStreamEndCapture(stream, &gr);
+    if (ce != cudaSuccess) { err = std::string("graph capture: ") + cudaGetErrorString(ce); return -6; }
+    CK(cudaGraphInstantiate(&ex, gr, flags));
+  }
   return 0;
 }
 
@@ -1472,6 +1481,12 @@ int step_parts_for(int K) {
   // 290 / 267 / 269 / 271 us with 1 / 4 / 8 / 16 ranges; more ranges add launches and edges)
   return std::max(1, std::min(4, T / 128));
 }
+
+// Steps in one launch of the step graph over cell ranges (run() launches it as often as it fits,
+// then the one-step graph for the rest).
+static std::atomic<int> g_steps_per_graph{2};
+void set_steps_per_graph(int g) { g_steps_per_graph = (g >= 1 && g <= 8) ? g : 2; }
+int steps_per_graph() { return g_steps_per_graph; }
 
 void set_step_parts(int p) { g_step_parts = (p >= 0 && p <= kMaxStepParts) ? p : 0; }
 int step_parts() { return g_step_parts; }
@@ -1529,7 +1544,7 @@ int Solver::build_parts(int P, std::string &err) {
     CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     pstreams.push_back(st);
   }
-  while ((int)pevents.size() < 7 * P + 1) {
+  while ((int)pevents.size() < 7 * P + 2) {
     cudaEvent_t ev = nullptr;
     CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     pevents.push_back(ev);
@@ -1549,7 +1564,7 @@ int Solver::kernels_per_step() const {
   return n;
 }
 
-void Solver::enqueue_step_parts(cudaStream_t s, const double *q_in, double *q_out) {
+void Solver::enqueue_step_parts(cudaStream_t s, const double *q_in, double *q_out, int nsteps) {
   const int P = parts, Nfp = cfg.N + 1;
   const size_t cell_bytes = (size_t)np_of(cfg.N) * 4 * sizeof(double);
   auto cells_of = [&](int p, size_t &c0, size_t &nc) {
@@ -1573,6 +1588,7 @@ void Solver::enqueue_step_parts(cudaStream_t s, const double *q_in, double *q_ou
   auto evF = [&](int st, int p) { return pevents[(2 * st) * P + p]; };
   auto evE = [&](int st, int p) { return pevents[(2 * st + 1) * P + p]; };
   auto evU = [&](int p) { return pevents[6 * P + 1 + p]; };
+  cudaEvent_t fin = pevents[7 * P + 1];  // after the previous step's finalize
   cudaEventRecord(fork, s);
   for (int p = 0; p < P; p++) cudaStreamWaitEvent(pstreams[p], fork, 0);
   if (q_in) {
@@ -1587,13 +1603,19 @@ void Solver::enqueue_step_parts(cudaStream_t s, const double *q_in, double *q_ou
       cudaEventRecord(evU(p), pstreams[p]);
     }
   }
+  // Steps after the first in this graph: the first face launch of range p needs only the previous
+  // step's last element launches of the ranges whose W it reads (and, in the vortex app, the time
+  // the finalize kernel advanced); the first element launch also needs the new dt.  So the next
+  // step's face launches overlap the previous step's last element launches.
+  for (int step = 0; step < nsteps; step++) {
   for (int stage = 0; stage < 3; stage++) {
     for (int p = 0; p < P; p++) {
       cudaStream_t ps = pstreams[p];
-      if (stage > 0)
-        for (int q = plo[p]; q < p; q++) cudaStreamWaitEvent(ps, evE(stage - 1, q), 0);
+      if (stage > 0 || step > 0)
+        for (int q = plo[p]; q < p; q++) cudaStreamWaitEvent(ps, evE(stage > 0 ? stage - 1 : 2, q), 0);
       else if (q_in)
         for (int q = plo[p]; q < p; q++) cudaStreamWaitEvent(ps, evU(q), 0);  // the W it reads
+      if (stage == 0 && step > 0 && d.app == 1) cudaStreamWaitEvent(ps, fin, 0);
       Inst dp = d;
       dp.edges = pedges + pe0[p];
       dp.nE = pe0[p + 1] - pe0[p];
@@ -1608,6 +1630,7 @@ void Solver::enqueue_step_parts(cudaStream_t s, const double *q_in, double *q_ou
     for (int p = 0; p < P; p++) {
       cudaStream_t ps = pstreams[p];
       for (int q = p + 1; q <= phi[p]; q++) cudaStreamWaitEvent(ps, evF(stage, q), 0);
+      if (stage == 0 && step > 0) cudaStreamWaitEvent(ps, fin, 0);  // this step's dt
       set_prio(p, true);
       DG_DISPATCH(cfg.N, launch_elem_range<NN>(d, stage, ptile0[p], ptile0[p + 1], ps));
       g_launch_prio_on = 0;
@@ -1625,6 +1648,8 @@ void Solver::enqueue_step_parts(cudaStream_t s, const double *q_in, double *q_ou
     cudaStreamWaitEvent(s, evE(2, p), 0);
   }
   launch_pdl(finalize_kernel, dim3(1), dim3(32), 0, s, d.st, d.dt_mode, d.dt_hist, d.dt_hist_len);
+  cudaEventRecord(fin, s);
+  }
   t_no_pdl = 0;
 }
 
@@ -1734,7 +1759,10 @@ int Solver::step_io(const double *q_in, double *q_out, std::string &err) {
 int Solver::step(int nsteps, bool use_graph, std::string &err) {
   if (use_graph) {
     if (int rc = build_graph(err)) return rc;
-    for (int i = 0; i < nsteps; i++) CK(cudaGraphLaunch(graph_exec, stream));
+    int i = 0;
+    if (graph_steps > 1 && graphG_exec)
+      for (; i + graph_steps <= nsteps; i += graph_steps) CK(cudaGraphLaunch(graphG_exec, stream));
+    for (; i < nsteps; i++) CK(cudaGraphLaunch(graph_exec, stream));
   } else {
     for (int i = 0; i < nsteps; i++) enqueue_step(stream);
     CK(cudaGetLastError());

@@ -90,6 +90,9 @@ void set_pdl(int on);
 // graphs built from now on.
 constexpr int kMaxStepParts = 32;
 void set_step_parts(int p);
+// Steps per launch of the step graph over cell ranges (1..8, default 2).
+void set_steps_per_graph(int g);
+int steps_per_graph();
 // Tuning of that graph: bit 0 no programmatic dependent launch between its kernels, bit 1
 // per-range scheduling priorities (earlier ranges first).
 void set_step_graph_flags(int f);
@@ -127,13 +130,18 @@ struct Solver {
   int build_parts(int P, std::string &err);
   // One step of the ranges' DAG on s; with q_in, the input is uploaded range by range first, with
   // q_out the result is downloaded range by range (host buffers, pinned).
-  void enqueue_step_parts(cudaStream_t s, const double *q_in = nullptr, double *q_out = nullptr);
+  void enqueue_step_parts(cudaStream_t s, const double *q_in = nullptr, double *q_out = nullptr, int nsteps = 1);
+  cudaGraph_t graphG = nullptr;  // graph_steps steps in one graph (over cell ranges)
+  cudaGraphExec_t graphG_exec = nullptr;
+  int graph_steps = 1;
   int step_io_parts(const double *q_in, double *q_out, bool &done, std::string &err);
   // Forget the captured step graphs (rebuilt on the next run), e.g. after a pointer they hold
   // changed.
   void drop_graphs() {
     if (graph_exec) { cudaGraphExecDestroy(graph_exec); graph_exec = nullptr; }
     if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
+    if (graphG_exec) { cudaGraphExecDestroy(graphG_exec); graphG_exec = nullptr; }
+    if (graphG) { cudaGraphDestroy(graphG); graphG = nullptr; }
     if (io_graph_exec) { cudaGraphExecDestroy(io_graph_exec); io_graph_exec = nullptr; }
     if (io_graph) { cudaGraphDestroy(io_graph); io_graph = nullptr; }
     io_in = nullptr;

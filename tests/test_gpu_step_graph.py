@@ -145,3 +145,27 @@ def test_face_kernel_register_bound_bitwise(pkg):
             assert np.array_equal(q, q1) and np.array_equal(dt, dt1), P
     finally:
         lib.dg_set_face_regs64(0)
+
+
+@pytest.mark.parametrize("G", [1, 2, 3])
+@pytest.mark.parametrize("app", ["airfoil", "vortex"])
+def test_steps_per_graph_bitwise(pkg, G, app):
+    """Several steps in one graph launch (the next step's face launches overlapping the previous
+    step's element launches), with a step count that leaves a remainder of one-step graphs: the
+    same q, dt sequence and time as one chain of launches per step."""
+    lib = pkg.lib()
+    if app == "vortex":
+        mesh = pkg.Mesh.vortex_square(64)
+        cfg = pkg.config(N=3, app=pkg.APP_VORTEX, dt_mode=pkg.DT_FROZEN, cfl=0.5, vortex_x0=0.0, vortex_y0=0.0,
+                         vortex_beta=5.0)
+    else:
+        mesh = pkg.Mesh.naca_ogrid(96, 24, farfield="characteristic")
+        cfg = pkg.config(N=3, cfl=0.5, mach=0.5, alpha_deg=2.0)
+    q1, dt1, t1, _ = run_parts(pkg, mesh, cfg, 1, 7)
+    prev = lib.dg_steps_per_graph()
+    lib.dg_set_steps_per_graph(G)
+    try:
+        q, dt, t, _ = run_parts(pkg, mesh, cfg, 4, 7)
+    finally:
+        lib.dg_set_steps_per_graph(prev)
+    assert np.array_equal(q, q1) and np.array_equal(dt, dt1) and t == t1
