@@ -1483,9 +1483,10 @@ int step_parts_for(int K) {
 }
 
 // Steps in one launch of the step graph over cell ranges (run() launches it as often as it fits,
-// then the one-step graph for the rest).
-static std::atomic<int> g_steps_per_graph{2};
-void set_steps_per_graph(int g) { g_steps_per_graph = (g >= 1 && g <= 8) ? g : 2; }
+// then the one-step graph for the rest).  On the K = 32768 O-grid at N = 3, 40 steps in one run():
+// 254.3 / 245.9 / 241.6 / 239.4 us per step with 1 / 2 / 4 / 8 steps per graph.
+static std::atomic<int> g_steps_per_graph{8};
+void set_steps_per_graph(int g) { g_steps_per_graph = (g >= 1 && g <= 8) ? g : 8; }
 int steps_per_graph() { return g_steps_per_graph; }
 
 void set_step_parts(int p) { g_step_parts = (p >= 0 && p <= kMaxStepParts) ? p : 0; }

@@ -90,7 +90,7 @@ void set_pdl(int on);
 // graphs built from now on.
 constexpr int kMaxStepParts = 32;
 void set_step_parts(int p);
-// Steps per launch of the step graph over cell ranges (1..8, default 2).
+// Steps per launch of the step graph over cell ranges (1..8, default 8).
 void set_steps_per_graph(int g);
 int steps_per_graph();
 // Tuning of that graph: bit 0 no programmatic dependent launch between its kernels, bit 1

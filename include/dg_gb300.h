@@ -341,7 +341,7 @@ int dg_tc_round(long long th, long long tl, int sc, double *out);
  * launches as one chain), 2..32 that many ranges (fewer if the mesh has fewer tiles). */
 void dg_set_step_parts(int parts);
 int dg_step_parts(void);
-/* Steps in one launch of that graph (1..8, default 2; other values select 2), for graphs built from
+/* Steps in one launch of that graph (1..8, default 8; other values select 8), for graphs built from
  * now on: the next step's first face launches of a range then wait only for the element launches
  * whose cells they read (its first element launches for the new dt), so they overlap the previous
  * step's last element launches.  dg_solver_run launches it as often as it fits, then one-step
