@@ -40,10 +40,11 @@ def test_headline_1000_steps_own_geometry(pkg, orc, oops, omesh):
     assert np.abs(s.dt_history(1000) / dts - 1).max() < 1e-10
 
 
-@pytest.mark.parametrize("N", [2, 5])
+@pytest.mark.parametrize("N", [1, 2, 4, 5, 6])
 def test_other_orders_1000_steps_own_geometry(pkg, orc, oops, omesh, N):
-    """N = 2 (dense rows on the tensor cores) and N = 5 (even/odd blocks on the tensor cores, one
-    block per SM) on the 128 x 32 O-grid (K = 8192), M = 0.5, alpha = 2 deg, 1000 steps."""
+    """Every other order on the 128 x 32 O-grid (K = 8192), M = 0.5, alpha = 2 deg, 1000 steps:
+    N = 1, 2 (dense rows on the tensor cores), 4, 5 (even/odd blocks on the tensor cores) and 6
+    (even/odd blocks in FP64)."""
     m = omesh.naca_ogrid(128, 32, farfield="characteristic")
     s, o = own_geometry_pair(pkg, orc, oops, m, N, 0.5, orc.freestream(0.5, 2.0), mach=0.5, alpha_deg=2.0)
     s.record_dt(1000)
