@@ -206,7 +206,10 @@ struct Batch {
     }
     maxNp = np_of(maxN);
     std::vector<Inst> insts;
-    for (Solver *s : solvers) insts.push_back(s->d);
+    for (Solver *s : solvers) {
+      insts.push_back(s->d);
+      insts.back().dt_est = nullptr;  // the element kernel takes the dt maximum itself
+    }
     if (cudaMalloc(&d_insts, sizeof(Inst) * insts.size()) != cudaSuccess ||
         cudaMalloc(&d_bar, sizeof(GridBarrier)) != cudaSuccess) {
       err = "cudaMalloc failed";

@@ -244,6 +244,21 @@ __device__ __forceinline__ float f32_trunc(const double x) {
   return __uint_as_float(sign | mag);
 }
 
+// src/calc_dt.h for one node in FP64: (N+1)^2 / 2 (|v| + c) fs as the bit pattern of a
+// non-negative double (fs the larger fscale of the node's faces).  The element kernel and
+// dt_finalize_kernel evaluate it with the same operations, so either gives the same maximum.
+template <int N>
+__device__ __forceinline__ unsigned long long dt_speed_bits(const double n0, const double n1, const double n2,
+                                                            const double n3, const double fs, const Phys &P) {
+  const double ir = rcp(n0);
+  const double u = n1 * ir, v = n2 * ir;
+  const double v2 = fma(u, u, v * v);
+  const double p = P.gm1 * fma(-0.5 * n0, v2, n3);
+  const double cs = sqrt(fabs(P.gam * p * ir));
+  const double spd = ((N + 1) * (N + 1) * 0.5) * (sqrt(v2) + cs);
+  return (unsigned long long)__double_as_longlong(spd * fs);
+}
+
 // SSPRK3 stage combine of one node's right-hand side (r0..r3), and in the last stage the
 // calc_dt maximum.  Every thread of the block calls it: `active` is false for warps beyond the
 // Np node-warps of a wider block (they only take part in the barrier), `live` is false for
@@ -340,6 +355,21 @@ __device__ __forceinline__ void stage_combine(const Inst &d, const int stage, co
       est = ((N + 1) * (N + 1) * 0.5f) * (sqrtf(v2) + cs) * fsf;
       if (!(est == est) || est > 3.0e38f) est = 3.0e38f;  // non-finite: always a candidate
     }
+    if (d.dt_est) {
+      // deferred: the node-warp's largest estimate goes to HBM and dt_finalize_kernel takes the
+      // FP64 maximum over the candidates of the whole mesh; no barrier, no FP64 here (a chain of
+      // ~35 FP64 instructions at the end of every tile, waiting behind the other blocks' FP64
+      // work, held each block ~9k clocks)
+      if (active) {
+        float wm = est;
+        for (int o = 16; o > 0; o >>= 1) wm = fmaxf(wm, __shfl_xor_sync(0xffffffffu, wm, o));
+        if (lane == 0) {
+          d.dt_est[(size_t)(e >> 5) * Np + i] = wm;
+          atomicMax(&d.st->dt_est_max, __float_as_uint(wm));  // non-negative: ordered as integers
+        }
+      }
+      return;
+    }
     if (active) {
       float wm = est;
       for (int o = 16; o > 0; o >>= 1) wm = fmaxf(wm, __shfl_xor_sync(0xffffffffu, wm, o));
@@ -354,13 +384,7 @@ __device__ __forceinline__ void stage_combine(const Inst &d, const int stage, co
         unsigned long long best = 0ull;
         if (cand) {
           const double fs = fb >= 0 ? fmax(ge[6 + 3 * fa], ge[6 + 3 * fb]) : ge[6 + 3 * fa];
-          const double ir = rcp(n0);
-          const double u = n1 * ir, v = n2 * ir;
-          const double v2 = fma(u, u, v * v);
-          const double p = P.gm1 * fma(-0.5 * n0, v2, n3);
-          const double cs = sqrt(fabs(P.gam * p * ir));
-          const double spd = ((N + 1) * (N + 1) * 0.5) * (sqrt(v2) + cs);
-          best = (unsigned long long)__double_as_longlong(spd * fs);
+          best = dt_speed_bits<N>(n0, n1, n2, n3, fs, P);
         }
         // warp max on the bit patterns of non-negative doubles (all 32 lanes take part)
         for (int o = 16; o > 0; o >>= 1) {
@@ -682,11 +706,77 @@ __global__ void finalize_kernel(StepState *st, int dt_mode, double *dt_hist, uns
   if (dt_hist && st->step < dt_hist_len) dt_hist[st->step] = st->dt;
   st->t += st->dt;
   st->step += 1;
+  st->dt_est_max = 0u;  // a stage-2 element kernel with deferred estimates may have run (dt frozen)
   if (dt_mode == 0) {
     const double dt1 = __longlong_as_double((long long)st->dt1_bits);
     st->dt = (1.0 / dt1) * st->cfl;
     st->dt1_bits = 0ull;
   }
+}
+
+// The per-step finalize with the deferred calc_dt maximum (Inst::dt_est): with M the largest
+// single-precision estimate of the mesh (the element kernel's node-warps combine theirs into the
+// step state by atomicMax), the grid's warps share the node-warps whose estimate is within 1e-4
+// of M and evaluate those
+// nodes in FP64 from the new q (the estimates are within ~1e-6 of the FP64 values, so the node
+// of the FP64 maximum is always among them and the result is the exact maximum, the same as the
+// element kernel's per-block evaluation gives), combined with atomicMax; the last block to finish
+// (a counter in the step state, no waiting) then advances t and sets the new dt.
+template <int N>
+__global__ void __launch_bounds__(256) dt_finalize_kernel(const Inst d) {
+  constexpr int Np = np_of(N);
+  pdl_wait();
+  pdl_trigger();
+  const int n = ((d.K + 31) >> 5) * Np;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __shared__ int s_last;
+  StepState *st = d.st;
+  const float thr = __uint_as_float(st->dt_est_max) * 0.9999f;
+  // warp w of the grid takes the estimates w, w + G, w + 2G, ... (G warps in the grid): its lanes
+  // read 32 of them at once, and the candidates among them are evaluated one after the other,
+  // each by the whole warp (lane = cell of the tile)
+  unsigned long long best = 0ull;
+  const int gs = gridDim.x * nw;
+  for (int base = blockIdx.x * nw + warp; base < n; base += 32 * gs) {
+    const int jl = base + lane * gs;
+    unsigned cand = __ballot_sync(0xffffffffu, jl < n && d.dt_est[jl] >= thr);
+    while (cand) {
+      const int k = __ffs((int)cand) - 1;
+      cand &= cand - 1u;
+      const int j = base + k * gs;
+      const int tile = j / Np, i = j - tile * Np, e = tile * 32 + lane;
+      const int fa = c_dtf[N][2 * i], fb = c_dtf[N][2 * i + 1];
+      if (e < d.K && fa >= 0) {
+        const double *ge = d.geo + (size_t)e * 16;
+        const double fs = fb >= 0 ? fmax(ge[6 + 3 * fa], ge[6 + 3 * fb]) : ge[6 + 3 * fa];
+        const double2 a = ld2(d.q + ((size_t)e * Np + i) * 4), b = ld2(d.q + ((size_t)e * Np + i) * 4 + 2);
+        const unsigned long long v = dt_speed_bits<N>(a.x, a.y, b.x, b.y, fs, d.P);
+        best = v > best ? v : best;
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long x = __shfl_xor_sync(0xffffffffu, best, o);
+    best = x > best ? x : best;
+  }
+  if (lane == 0 && best) atomicMax(&st->dt1_bits, best);
+  // the step state's other fields are not written by this kernel before the last block's update
+  const double dt0 = st->dt, t0 = st->t, cfl = st->cfl;
+  const unsigned long long step0 = st->step;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(&st->dt_blocks, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!s_last || threadIdx.x) return;
+  __threadfence();
+  st->dt_blocks = 0u;
+  st->dt_est_max = 0u;
+  if (d.dt_hist && step0 < d.dt_hist_len) d.dt_hist[step0] = dt0;
+  st->t = t0 + dt0;
+  st->step = step0 + 1;
+  const double dt1 = __longlong_as_double((long long)atomicAdd(&st->dt1_bits, 0ull));
+  st->dt = (1.0 / dt1) * cfl;
+  st->dt1_bits = 0ull;
 }
 
 // ---------------------------------------------------------------- set-up kernels
@@ -1361,6 +1451,12 @@ int Solver::create(const Config &c, const Mesh &m, std::string &err) {
   int *fm = (int *)dalloc(sizeof(int) * 3 * Nfp);
   d.fmask = fm;
   d.st = (StepState *)dalloc(sizeof(StepState));
+  d.dt_est = (float *)dalloc((size_t)((K + 31) / 32) * Np * sizeof(float));
+  {
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev));
+  }
   coords_d = (double *)dalloc(m.coords.size() * 8);
   cells_d = (int *)dalloc(m.cell2nodes.size() * 4);
   double *bxy = (double *)dalloc((size_t)d.nB * Nfp * 2 * 8);
@@ -1409,7 +1505,21 @@ int Solver::set_dt_from_max(std::string &err) {
 
 void Solver::enqueue_step(cudaStream_t s) {
   DG_DISPATCH(cfg.N, (launch_stage<NN>(d, 0, s), launch_stage<NN>(d, 1, s), launch_stage<NN>(d, 2, s)));
-  launch_pdl(finalize_kernel, dim3(1), dim3(32), 0, s, d.st, d.dt_mode, d.dt_hist, d.dt_hist_len);
+  enqueue_finalize(s, true);
+}
+
+void Solver::enqueue_finalize(cudaStream_t s, bool pdl) {
+  if (d.dt_mode == 0 && d.dt_est) {
+    // one block per SM at most, at least 8 estimates per block
+    const int n = ((K + 31) / 32) * np_of(cfg.N);
+    const int g = std::max(1, std::min(sm_count > 0 ? sm_count : 1, (n + 7) / 8));
+    DG_DISPATCH(cfg.N, pdl ? launch_pdl(dt_finalize_kernel<NN>, dim3(g), dim3(256), 0, s, d)
+                           : (dt_finalize_kernel<NN><<<g, 256, 0, s>>>(d), void()));
+  } else if (pdl) {
+    launch_pdl(finalize_kernel, dim3(1), dim3(32), 0, s, d.st, d.dt_mode, d.dt_hist, d.dt_hist_len);
+  } else {
+    finalize_kernel<<<1, 32, 0, s>>>(d.st, d.dt_mode, d.dt_hist, d.dt_hist_len);
+  }
 }
 
 // One step with an event recorded after each of its seven kernels (ev[0] is recorded by the
@@ -1421,7 +1531,7 @@ void Solver::enqueue_step_events(cudaStream_t s, cudaEvent_t *ev) {
     DG_DISPATCH(cfg.N, launch_elem<NN>(d, stage, s));
     cudaEventRecord(ev[2 + 2 * stage], s);
   }
-  finalize_kernel<<<1, 32, 0, s>>>(d.st, d.dt_mode, d.dt_hist, d.dt_hist_len);
+  enqueue_finalize(s, false);
   cudaEventRecord(ev[7], s);
 }
 
@@ -1648,7 +1758,7 @@ void Solver::enqueue_step_parts(cudaStream_t s, const double *q_in, double *q_ou
     cudaEventRecord(evE(2, p), pstreams[p]);  // after the range's copy too
     cudaStreamWaitEvent(s, evE(2, p), 0);
   }
-  launch_pdl(finalize_kernel, dim3(1), dim3(32), 0, s, d.st, d.dt_mode, d.dt_hist, d.dt_hist_len);
+  enqueue_finalize(s, true);
   cudaEventRecord(fin, s);
   }
   t_no_pdl = 0;
@@ -1727,7 +1837,7 @@ int Solver::step_io(const double *q_in, double *q_out, std::string &err) {
   DG_DISPATCH(N, (launch_stage<NN>(d, 1, stream), launch_face<NN>(d, 2, stream)));
   if (!q_out) {
     DG_DISPATCH(N, launch_elem<NN>(d, 2, stream));
-    launch_pdl(finalize_kernel, dim3(1), dim3(32), 0, stream, d.st, d.dt_mode, d.dt_hist, d.dt_hist_len);
+    enqueue_finalize(stream, true);
     CK(cudaGetLastError());
     return 0;
   }
@@ -1751,7 +1861,7 @@ int Solver::step_io(const double *q_in, double *q_out, std::string &err) {
     CK(cudaEventRecord(io_copy[c], cs));
   }
   for (int c = 0; c < kOutChunks; c++) CK(cudaStreamWaitEvent(stream, io_kern[c], 0));
-  finalize_kernel<<<1, 32, 0, stream>>>(d.st, d.dt_mode, d.dt_hist, d.dt_hist_len);
+  enqueue_finalize(stream, false);
   CK(cudaGetLastError());
   for (int c = 0; c < kOutChunks; c++) CK(cudaStreamWaitEvent(stream, io_copy[c], 0));
   return 0;

@@ -28,6 +28,8 @@ struct StepState {
   unsigned long long step;      // completed steps
   unsigned err;                 // bit 0: a non-positive or non-finite density was produced;
                                 // bit 2: a bounded wait of the element kernel ran out
+  unsigned dt_blocks;           // blocks of the step's dt kernel that are done (reset by the last)
+  unsigned dt_est_max;          // bits of the largest dt estimate of the step (Inst::dt_est)
   unsigned pad;
 };
 
@@ -45,6 +47,10 @@ struct Inst {
   StepState *st;
   double *dt_hist;
   unsigned long long dt_hist_len;
+  // Per 32-cell tile and node, the largest single-precision calc_dt estimate of the node-warp
+  // ([tiles][Np]), written by the last stage's element kernel when non-null: the FP64 maximum is
+  // then taken over the candidates by dt_finalize_kernel.  Null: the element kernel takes it.
+  float *dt_est;
   Phys P;
 };
 
@@ -117,6 +123,10 @@ struct Solver {
   int init(std::string &err);
   int set_dt_from_max(std::string &err);
   void enqueue_step(cudaStream_t s);
+  // The step's last launch: t += dt, step += 1 and, with dt recomputed, the new dt (pdl: with
+  // programmatic dependence on the last element kernel).
+  void enqueue_finalize(cudaStream_t s, bool pdl);
+  int sm_count = 0;
   void enqueue_step_events(cudaStream_t s, cudaEvent_t *ev);
   int build_graph(std::string &err);
   // The step graph as a DAG of cell ranges (build_graph with more than one range).

@@ -102,6 +102,22 @@ def test_steps_every_order_match_oracle(pkg, orc, oops, omesh, N):
     assert np.abs(s.dt_history(100) / dts - 1).max() < 1e-12
 
 
+@pytest.mark.parametrize("n", [32, 128])
+def test_dt_with_tied_estimates_matches_oracle(pkg, orc, oops, omesh, n):
+    """Freestream on a uniform square mesh with inflow boundaries: the calc_dt estimates of the
+    nodes on the largest-fscale faces of every cell tie, so the step's finalize evaluates a large
+    share of all node-warps in FP64 (n = 128: 32768 cells, the step graph over cell ranges).  The
+    dt sequence must equal the oracle's."""
+    m = omesh.vortex_square(n)
+    s, o = solver_and_oracle(pkg, orc, oops, m, 3, 0.5)
+    s.record_dt(5)
+    s.run(5)
+    s.sync()
+    dts = o.run(5, nthreads=0)
+    assert np.abs(s.dt_history(5) / dts - 1).max() < 1e-13
+    assert orc.rel_l2(s.get("q"), o.get("q")) < 1e-13
+
+
 def test_vortex_config_matches_oracle(pkg, orc, oops, omesh):
     """The vortex case: [-5,5]^2, 2048 cells, N=3, beta=5, dt = 0.5/dt1 frozen."""
     m = omesh.vortex_square(32)
