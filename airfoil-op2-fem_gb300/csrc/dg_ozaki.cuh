@@ -277,7 +277,27 @@ __device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *_
     Yd[(YROW0 + n) * XST + col + 8 * r] = out;
   };
   constexpr int RV = R - 8 * NT;  // operator rows of this n-tile that exist (1..8)
-  if constexpr (RV <= 4) {
+  if constexpr (RV == 6) {
+    // Lanes t = 0..2 hold four outputs each (columns 2t, 2t + 1 of rows g, g + 8), lane t = 3 none:
+    // lane 3 takes the (row g + 8, column 2t' + 1) output of lanes t' = 0, 1, 2 (their level sums by
+    // shuffle), so every lane rounds three outputs instead of three lanes rounding four.  Same
+    // values, same rounding.
+    const bool hi = t == 3;
+    float x[3][7];
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+#pragma unroll
+      for (int L = 0; L < 7; L++) x[k][L] = __shfl_sync(0xffffffffu, acc[L][3], (lane & ~3) | k);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      float lev[7];
+#pragma unroll
+      for (int L = 0; L < 7; L++) lev[L] = hi ? x[k][L] : acc[L][k];
+      // k = 0, 1: row g, columns 2t, 2t + 1; k = 2: row g + 8, column 2t
+      const int n = 8 * NT + (hi ? 2 * k + 1 : 2 * t + (k & 1));
+      finish(lev, n, hi || k == 2 ? 1 : 0);
+    }
+  } else if constexpr (RV <= 4) {
     // Only lanes t = 0, 1 hold outputs (columns 2t + cc < RV): lanes t = 2, 3 take the row-(g + 8)
     // outputs of lane t - 2 (their level sums by shuffle), so the rounding, the costly part, runs
     // on all four lanes of a group with half the outputs each.  Same values, same rounding.
