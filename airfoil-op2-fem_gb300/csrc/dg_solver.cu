@@ -12,9 +12,10 @@
 //                (operators in constant memory, warp-uniform rows) against
 //                [Fr ; Fs ; flux] staged in shared memory (src/euler_rhs.h:226-247,284-286),
 //                then the SSPRK3 stage combine in registers (src/set_workingQ.h,
-//                src/update_Q.h, in Shu-Osher form) and, in the last stage, the calc_dt
-//                maximum (src/calc_dt.h) on the new state.
-// plus a one-thread finalize kernel per step (t += dt; dt = (1/dt1)*cfl).  dt never leaves the
+//                src/update_Q.h, in Shu-Osher form) and, in the last stage, single-precision
+//                calc_dt estimates (src/calc_dt.h) on the new state, one maximum per node-warp.
+// plus a finalize kernel per step: the exact FP64 calc_dt maximum over the candidate nodes the
+// estimates single out (dt_finalize_kernel), then t += dt; dt = (1/dt1)*cfl.  dt never leaves the
 // device, so a whole step is a fixed launch sequence that is captured once in a CUDA graph.
 //
 // Data layout in HBM (K cells, order N, Np=(N+1)(N+2)/2, Nfp=N+1):
@@ -24,6 +25,7 @@
 //                    fscale again as floats in the last 16 bytes (the dt estimate)
 //   edges  int4 {cL, cR, fL | fR << 2 | reverse << 4, 0};  bedges int4 {cell, face, type, 0}
 //   bxy    [nB][Nfp][2] boundary face-node coordinates (vortex boundary)
+//   dt_est [tiles][Np] floats: each node-warp's largest calc_dt estimate of the last stage
 #include <cuda_runtime.h>
 
 #include <algorithm>

@@ -108,9 +108,12 @@ int dg_solver_l2_error(dg_solver_t *s, double *err4);
 int dg_solver_record_dt(dg_solver_t *s, int max_steps);
 int dg_solver_dt_history(dg_solver_t *s, double *out, int n);
 /* End-to-end call with host buffers: q_in -> device, nsteps steps, device -> q_out.
- * Either pointer may be NULL to skip that copy.  Synchronous.  With q_out, the last step's
- * final element kernel runs as four ranges of cells and each range is copied back while the
- * later ones compute (pinned q_out overlaps; results equal dg_solver_run's bit for bit). */
+ * Either pointer may be NULL to skip that copy.  Synchronous.  With pinned buffers on a mesh that
+ * runs the step graph over cell ranges, a one-step call is one captured graph: each range's q is
+ * uploaded on its own stream before the range's first face launch, and each range's new q is
+ * downloaded as soon as its last element launch is done, while the other ranges compute; otherwise
+ * the last step's final element kernel runs as four ranges of cells and each range is copied
+ * back while the later ones compute.  Results equal dg_solver_run's bit for bit. */
 int dg_solver_step_host(dg_solver_t *s, const double *q_in, int nsteps, double *q_out);
 void *dg_solver_device_ptr(dg_solver_t *s, const char *name);
 void *dg_solver_stream(dg_solver_t *s);
