@@ -141,11 +141,6 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 
 #include "dg_ozaki.cuh"
 
-// Orders whose element kernels keep each node's W and q for the stage combine in shared memory
-// (copied there while the tile is staged) instead of reading them again from HBM after the
-// contraction.  At N = 1, 2 the extra shared memory would cost resident blocks.
-constexpr bool elem_staged(int N) { return N >= 3; }
-
 // ---------------------------------------------------------------- face kernel
 // One face node (tid in [0, (nB + nE) * Nfp)): boundary face nodes come first.  PDL: the kernel
 // was launched with programmatic dependent launch; the edge records, node indices and face
@@ -502,10 +497,8 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
   constexpr int kS2 = kElemSlot / 2;  // double2 per staged slot
   constexpr bool DENSE = ozd_used(N, TC);           // dense rows, slots in natural order
   constexpr bool SYMTC = !DENSE && oz_used(N, TC != 0);  // even/odd blocks on the tensor cores
-  constexpr bool STG = elem_staged(N);  // W and q of the stage combine kept in shared memory
   double2 *Y = X + NK * kS2;
   int *Ems = reinterpret_cast<int *>(Y + Np * kS2);  // column exponents of the prepared operands
-  double2 *WQ = reinterpret_cast<double2 *>(Ems + 128);  // [4][32 Np]: W 0-1, W 2-3, q 0-1, q 2-3
   const int nthr = 32 * Np, tid = i * 32 + lane;
   const bool active = i < Np;
   const int e = e0 + lane;
@@ -532,16 +525,6 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
     w[0] = a.x; w[1] = a.y; w[2] = b.x; w[3] = b.y;
     double2 ga = ld2(d.geo + (size_t)e * 16), gb = ld2(d.geo + (size_t)e * 16 + 2);
     g[0] = ga.x; g[1] = ga.y; g[2] = gb.x; g[3] = gb.y;
-    if constexpr (STG) {
-      WQ[tid] = a;
-      WQ[nthr + tid] = b;
-      // q (stages 1, 2) is not the face kernel's output: copied before the launch wait
-      if (stage == 1 || stage == 2) {
-        const double *qp = d.q + ((size_t)e * Np + i) * 4;
-        cp_async16(WQ + 2 * nthr + tid, qp, true);
-        cp_async16(WQ + 3 * nthr + tid, qp + 2, true);
-      }
-    }
   }
   // Without programmatic launch the face fluxes are ready: their copies overlap the nodal fluxes.
   if constexpr (!PDL) stage_face_fluxes();
@@ -651,36 +634,26 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
     }
   }
   if constexpr (DENSE || SYMTC) {
-    // this node's W again rather than held in registers through the contraction: from shared
-    // memory where it was staged, else from W (the node is written only below, by this thread)
+    // this node's W again from HBM (L2) rather than held in registers through the contraction
+    // (the node is written only below, by this thread).  Keeping W and q of every node of the
+    // tile in shared memory instead (+20.5 KB per block at N = 3) measured slightly slower in the
+    // step graph over cell ranges (N = 3 / 4 / 5: 234.6 / 382.2 / 611 against 232.3 / 380.2 / 607 us
+    // per step in runs of 40 steps; same bits).
     if (live) {
-      double2 a, b;
-      if constexpr (STG) {
-        a = WQ[tid];
-        b = WQ[nthr + tid];
-      } else {
-        const double *wp = d.W + ((size_t)e * Np + i) * 4;
-        a = ld2(wp);
-        b = ld2(wp + 2);
-      }
+      const double *wp = d.W + ((size_t)e * Np + i) * 4;
+      const double2 a = ld2(wp), b = ld2(wp + 2);
       w[0] = a.x; w[1] = a.y; w[2] = b.x; w[3] = b.y;
     }
   }
-  if constexpr (STG)
-    stage_combine<N>(d, stage, e, active, live, i, lane, w, r0, r1, r2, r3, X,
-                     (stage == 1 || stage == 2) ? WQ + 2 * nthr + tid : nullptr, nthr);
-  else
-    stage_combine<N>(d, stage, e, active, live, i, lane, w, r0, r1, r2, r3, X);
+  stage_combine<N>(d, stage, e, active, live, i, lane, w, r0, r1, r2, r3, X);
   // X and Y are rewritten by the next tile only after every warp is past this point
   __syncthreads();
 }
 
-// Dynamic shared memory of the even/odd element kernels: NK staged slots, Np output rows, the
-// 128 column exponents of the prepared tensor-core operands and, at N >= 3, W and q of every node
-// of the tile for the stage combine (elem_staged).
+// Dynamic shared memory of the even/odd element kernels: NK staged slots, Np output rows and the
+// 128 column exponents of the prepared tensor-core operands.
 constexpr size_t elem_sym_smem(int N) {
-  return (size_t)(nk_of(N) + np_of(N)) * kElemSlot * sizeof(double) + 128 * sizeof(int) +
-         (elem_staged(N) ? (size_t)4 * 32 * np_of(N) * 16 : 0);
+  return (size_t)(nk_of(N) + np_of(N)) * kElemSlot * sizeof(double) + 128 * sizeof(int);
 }
 
 // MB: minimum resident blocks per SM the register allocation must allow (oz_min_blocks for the
