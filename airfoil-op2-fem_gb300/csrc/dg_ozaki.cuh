@@ -401,10 +401,13 @@ __device__ __forceinline__ void oz_prep(double *Xd, int *Ems, const int tid) {
 }
 
 // Doubles per staged slot (and per output row) in the element kernel's shared memory: 32 cells x 4
-// variables plus 4 doubles of padding.  With 128 the four k-rows a fragment load touches (lanes
-// t = 0..3, rows 2t + ...) start on the same bank, so every half-warp's 64-bit load met a 4-way
-// bank conflict; a row offset of 132 doubles (8 banks) spreads them over all 32 banks.
-constexpr int kElemSlot = 132;
+// variables plus 2 doubles of padding (a slot stays 16-byte aligned for the asynchronous copies).
+// A half-warp's 64-bit fragment load reads lanes g = 0..3 (consecutive doubles) of the rows 2t,
+// t = 0..3, i.e. doubles 2t * XST + g: with XST = 128 all four rows start on the same bank (4-way
+// conflict), with 132 rows t and t + 2 do (2-way; ~1 M conflicts per launch at N = 3), with 130
+// the rows start 8 banks apart and the 16 lanes cover all 32 banks once.  Step 232.3 -> 231.2 us
+// at N = 3 and 379.9 -> 377.7 us at N = 4 (runs of 40 steps; same bits).
+constexpr int kElemSlot = 130;
 
 // The element kernel's contraction: Y rows 0..NRe-1 = S_e, Y rows NRe.. = S_o, on the operands
 // oz_prep made from the staged pairs (sums below slot NUe, differences from slot NUe on).  Earlier
