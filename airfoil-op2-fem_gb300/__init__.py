@@ -167,7 +167,7 @@ def lib():
         "dg_adjoint_last_error": (cp, []),
         "dg_order_tables_loaded": (C.c_int, [C.c_int, C.c_int]),
         "dg_solver_kernels_per_step": (C.c_int, [vp]),
-        "dg_bf16_mma_peak_gflops": (C.c_double, []),
+        "dg_f16_mma_peak_gflops": (C.c_double, []),
         "dg_set_step_parts": (None, [C.c_int]),
         "dg_step_parts": (C.c_int, []),
         "dg_set_steps_per_graph": (None, [C.c_int]),
@@ -703,8 +703,8 @@ def fp64_peak_gflops():
     return lib().dg_fp64_peak_gflops()
 
 
-def bf16_mma_peak_gflops():
-    return lib().dg_bf16_mma_peak_gflops()
+def f16_mma_peak_gflops():
+    return lib().dg_f16_mma_peak_gflops()
 
 
 def fp64_mma_peak_gflops():

@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(32 * np_of(N)) advec_elem_kernel_sym(const Adv
   }
 }
 
-// The element kernel with the even/odd contraction on the bf16 tensor cores (the exact integer
+// The element kernel with the even/odd contraction on the tensor cores (the exact integer
 // product of dg_ozaki.cuh): one variable per column, so a 32-cell tile is two row tiles of 16
 // cells and the units are (row tile, n-tile of outputs).  Staging, butterfly and alignment
 // (oz_prep over 64 threads), the contraction, the recombination and the RK4 combine follow

@@ -69,10 +69,10 @@ __global__ void dmma_peak_kernel(double *out, int iters, double a, double b) {
   out[blockIdx.x * blockDim.x + threadIdx.x] = acc;
 }
 
-// bf16 tensor-core throughput probe for the warp-level mma.sync.m16n8k16 (f32 accumulate) the
+// fp16 tensor-core throughput probe for the warp-level mma.sync.m16n8k16 (f32 accumulate) the
 // element kernel's contraction issues: four independent accumulator chains per warp.  4096 flops
 // per mma.
-__global__ void bf16_mma_peak_kernel(float *out, int iters, uint32_t a0, uint32_t b0) {
+__global__ void f16_mma_peak_kernel(float *out, int iters, uint32_t a0, uint32_t b0) {
   float c[4][4];
   for (int k = 0; k < 4; k++)
     for (int j = 0; j < 4; j++) c[k][j] = 0.0f;
@@ -82,7 +82,7 @@ __global__ void bf16_mma_peak_kernel(float *out, int iters, uint32_t a0, uint32_
 #pragma unroll
     for (int k = 0; k < 4; k++)
       asm volatile(
-          "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+          "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
           "{%0,%1,%2,%3};"
           : "+f"(c[k][0]), "+f"(c[k][1]), "+f"(c[k][2]), "+f"(c[k][3])
           : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
@@ -653,7 +653,7 @@ double dg_fp64_mma_peak_gflops(void) {
   cudaFree(out);
   return g;
 }
-double dg_bf16_mma_peak_gflops(void) {
+double dg_f16_mma_peak_gflops(void) {
   int dev = 0, sms = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return -1.0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -661,8 +661,8 @@ double dg_bf16_mma_peak_gflops(void) {
   float *out = nullptr;
   if (cudaMalloc(&out, sizeof(float) * blocks * threads) != cudaSuccess) return -1.0;
   const double warps = (double)blocks * threads / 32;
-  // bf16 1.0 = 0x3F80 in both halves: small values, no overflow over the iterations
-  const double g = time_peak([&] { bf16_mma_peak_kernel<<<blocks, threads>>>(out, iters, 0x3F803F80u, 0x3C003C00u); },
+  // fp16 1.0 = 0x3C00 and 2^-7 = 0x2000 in both halves: small values, no overflow over the iterations
+  const double g = time_peak([&] { f16_mma_peak_kernel<<<blocks, threads>>>(out, iters, 0x3C003C00u, 0x20002000u); },
                              4096.0 * 4 * iters * warps);
   cudaFree(out);
   return g;

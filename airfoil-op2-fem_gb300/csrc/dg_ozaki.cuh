@@ -1,7 +1,7 @@
-// Element-kernel contraction on the bf16 tensor cores, exact to FP64 accuracy (included by
+// Element-kernel contraction on the tensor cores (fp16 digit operands), exact to FP64 accuracy (included by
 // dg_solver.cu inside namespace dg).
 //
-// On GB300 the FP64 pipe issues about 2 DFMA lanes per clock per SM, while mma.sync on bf16
+// On GB300 the FP64 pipe issues about 2 DFMA lanes per clock per SM, while mma.sync on 16-bit
 // operands runs at ~600 TFLOP/s with FP32 accumulation.  The even/odd contraction of the
 // element kernel, Y_p = S_p X_p for the even (p = 0) and odd (p = 1) halves (rows of the operator
 // S_p, columns of X_p = one (cell, variable) over the staged slots), is therefore done as an
@@ -14,7 +14,7 @@
 //    every operator row by its own F likewise (done once on the host).  In the element kernel
 //    oz_prep does this once per staged value and forms the even/odd sums and differences exactly
 //    from values aligned to 2^(E-54).  m is written in base 256 as seven signed digits d_0..d_6
-//    (|d| <= 255, all with the sign of x), each exact in bf16.
+//    (|d| <= 255, all with the sign of x), each exact in fp16 (the mma operands).
 //  * digit products d_j c_s with j + s = L are summed into one FP32 accumulator per level L
 //    (L = 0..6; the levels L >= 7 lie below 2^-56 of the leading term and are dropped).  A level
 //    sums at most 7 pairs x 32 slots x 255^2 < 2^24, so every accumulation is an exact integer
@@ -63,26 +63,28 @@ constexpr int elem_min_blocks(int N, int TC) {
   return (ozd_used(N, TC) || oz_used(N, TC != 0)) ? oz_min_blocks(N) : 1;
 }
 
-__device__ __forceinline__ void mma_bf16_16816(float c[4], const uint32_t a[4], const uint2 b) {
+__device__ __forceinline__ void mma_f16_16816(float c[4], const uint32_t a[4], const uint2 b) {
   asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
       "{%0,%1,%2,%3};"
       : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b.x), "r"(b.y));
 }
 
-// Digit j (0 = most significant) of a magnitude m (hi:lo, < 2^56) as a float: byte (6 - j) goes
-// below the float 2^23, and subtracting 2^23 leaves exactly d.
-__device__ __forceinline__ float oz_digit(const uint32_t hi, const uint32_t lo, const int j) {
-  const uint32_t w = j < 3 ? hi : lo;
+// Digit j (0 = most significant) of the magnitudes (hi:lo, < 2^56) of two values, low k first,
+// as an fp16 pair with the values' signs (v = 0x64006400 | signs, bit 15 the low value's, bit 31
+// the high value's): one byte permute puts byte (6 - j) of each magnitude into the mantissa of
+// the fp16 1024 (bits 0x6400 | d), the mask and v keep those bytes and add the signs, and
+// subtracting v (+-1024 in each half) leaves exactly +-d (|d| <= 255).  Three instructions per
+// pair of digits (as two floats made from the bytes and packed: six).
+__device__ __forceinline__ uint32_t oz_pair(const uint32_t hl, const uint32_t ll, const uint32_t hh,
+                                            const uint32_t lh, const int j, const uint32_t v) {
+  const uint32_t wl = j < 3 ? hl : ll, wh = j < 3 ? hh : lh;
   const uint32_t b = j < 3 ? (uint32_t)(2 - j) : (uint32_t)(6 - j);
-  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7650u | b)) - 8388608.0f;
-}
-
-// The upper halves (bf16) of two floats holding small integers, low k first, with the sign
-// pattern of the pair (bit 15: low, bit 31: high) applied.
-__device__ __forceinline__ uint32_t oz_pack(const float f_lo, const float f_hi, const uint32_t sign) {
-  return __byte_perm(__float_as_uint(f_lo), __float_as_uint(f_hi), 0x7632u) ^ sign;
+  const uint32_t r = (__byte_perm(wl, wh, b | ((4u + b) << 8)) & 0x00FF00FFu) | v;
+  uint32_t out;
+  asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(out) : "r"(r), "r"(v));
+  return out;
 }
 
 // (th 2^32 + tl) 2^sc rounded to the nearest double (ties to even), with integer instructions only:
@@ -237,18 +239,18 @@ __device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *_
         hi[r][q] = (uint32_t)(m >> 32);
         lo[r][q] = (uint32_t)m;
       }
+    uint32_t v[4];
+#pragma unroll
+    for (int m = 0; m < 4; m++) v[m] = 0x64006400u | sgn[m];
 #pragma unroll
     for (int j = 0; j < 7; j++) {
-      float f[2][4];
-#pragma unroll
-      for (int r = 0; r < 2; r++)
-#pragma unroll
-        for (int q = 0; q < 4; q++) f[r][q] = oz_digit(hi[r][q], lo[r][q], j);
       // A fragment (row-major 16 x 16): rows g / g+8, slots 2t..2t+1 / 2t+8..2t+9
-      const uint32_t a[4] = {oz_pack(f[0][0], f[0][1], sgn[0]), oz_pack(f[1][0], f[1][1], sgn[1]),
-                             oz_pack(f[0][2], f[0][3], sgn[2]), oz_pack(f[1][2], f[1][3], sgn[3])};
+      const uint32_t a[4] = {oz_pair(hi[0][0], lo[0][0], hi[0][1], lo[0][1], j, v[0]),
+                             oz_pair(hi[1][0], lo[1][0], hi[1][1], lo[1][1], j, v[1]),
+                             oz_pair(hi[0][2], lo[0][2], hi[0][3], lo[0][3], j, v[2]),
+                             oz_pair(hi[1][2], lo[1][2], hi[1][3], lo[1][3], j, v[3])};
 #pragma unroll
-      for (int s = 0; s + j < 7; s++) mma_bf16_16816(acc[j + s], a, __ldg(bfr + (s * 2 + ks) * 32));
+      for (int s = 0; s + j < 7; s++) mma_f16_16816(acc[j + s], a, __ldg(bfr + (s * 2 + ks) * 32));
     }
   }
   // C fragment: acc[.][0] (row g, col 2t), [1] (g, 2t+1), [2] (g+8, 2t), [3] (g+8, 2t+1).
@@ -441,11 +443,13 @@ __device__ __forceinline__ void oz_contract_t(const double *Xd, double *Yd, cons
 // ---------------------------------------------------------------- host: operator digits
 // Digits and B fragments of the two parity blocks of S (even rows NRe x NUe, then odd rows
 // NRo x NUo, row-major) for the tensor-core contraction.
-static uint32_t oz_bf16_bits(int d) {
-  const float f = (float)d;  // |d| <= 255: exact, and exact in the upper 16 bits
-  uint32_t u;
-  std::memcpy(&u, &f, 4);
-  return u >> 16;
+static uint32_t oz_f16_bits(int d) {  // |d| <= 255: exact in fp16
+  if (d == 0) return 0u;
+  const uint32_t sign = d < 0 ? 0x8000u : 0u;
+  const uint32_t m = (uint32_t)(d < 0 ? -d : d);
+  int e = 0;
+  while ((m >> (e + 1)) != 0u) e++;  // floor(log2 m), 0..7
+  return sign | ((uint32_t)(e + 15) << 10) | ((m << (10 - e)) & 0x3FFu);
 }
 
 // Column exponents F (biased, per parity and operator row) and signed base-256 digits
@@ -518,8 +522,8 @@ static int oz_upload(int N, const std::vector<double> &S, int NUe, int NUo, int 
             for (int lane = 0; lane < 32; lane++) {
               const int g = lane >> 2, t = lane & 3, k0 = 16 * ks + 2 * t;
               auto D = [&](int k) { return dig[(((size_t)p * 7 + s) * 32 + k) * kOzRows + 8 * nt + g]; };
-              frag[T][p][nt][s][ks][lane].x = oz_bf16_bits(D(k0)) | (oz_bf16_bits(D(k0 + 1)) << 16);
-              frag[T][p][nt][s][ks][lane].y = oz_bf16_bits(D(k0 + 8)) | (oz_bf16_bits(D(k0 + 9)) << 16);
+              frag[T][p][nt][s][ks][lane].x = oz_f16_bits(D(k0)) | (oz_f16_bits(D(k0 + 1)) << 16);
+              frag[T][p][nt][s][ks][lane].y = oz_f16_bits(D(k0 + 8)) | (oz_f16_bits(D(k0 + 9)) << 16);
             }
   }
   cudaError_t ce = cudaSuccess;

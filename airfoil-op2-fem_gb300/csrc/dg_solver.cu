@@ -980,9 +980,9 @@ static void launch_face(const Inst &d, int stage, cudaStream_t s) {
     launch_pdl(face_kernel<N>, dim3((unsigned)((nf + bs - 1) / bs)), dim3(bs), 0, s, d, stage);
 }
 
-// 3: dense rows on the bf16 tensor cores at N = 1, 2 (dg_ozaki.cuh), form 2 at the other orders
+// 3: dense rows on the tensor cores at N = 1, 2 (dg_ozaki.cuh), form 2 at the other orders
 // (default);
-// 2: even/odd with the contraction on the bf16 tensor cores (at N = 3, 4, 5, the even/odd FP64
+// 2: even/odd with the contraction on the tensor cores (at N = 3, 4, 5, the even/odd FP64
 // kernel at the other orders), 1: even/odd element kernel, 0: dense FP64.
 static std::atomic<int> g_elem_variant{3};
 

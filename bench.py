@@ -18,7 +18,7 @@ roofline  the dominant kernel's binding roof: its FP64-pipe instructions (per-un
         counts from ncu, FP64_INST_*), algorithmic HBM bytes and mma flops over its
         event-timed duration (dg_solver_step_timed), against the FP64 pipe rate
         (half the DFMA peak, measured live), MEASURED_PEAKS.json's copy bandwidth
-        and the mma.sync bf16 rate (measured live); plus the step's FP64-pipe
+        and the mma.sync fp16 rate (measured live); plus the step's FP64-pipe
         fraction over the graph step time.
 legs    the OP2 drop-in C++ application, the 64-instance batched sweep (and small
         instances), the adjoint case, the advection app, device mesh set-up and
@@ -121,7 +121,7 @@ FP64_INST_PER_FACE_NODE = {3: 110.3}
 FP64_INST_PER_CELL_STAGE = {3: 405.3}
 
 
-def roofline(K, nf, face_ms, elem_ms, step_ms, peak_tf, hbm_peak, bf16_mma_tf=None):
+def roofline(K, nf, face_ms, elem_ms, step_ms, peak_tf, hbm_peak, mma_tf=None):
     """Which roof binds, per kernel and for the overlapped step.
 
     The path is FP64 bound: the FP64 pipe issues one thread instruction per lane slot at the rate
@@ -129,7 +129,7 @@ def roofline(K, nf, face_ms, elem_ms, step_ms, peak_tf, hbm_peak, bf16_mma_tf=No
     its FP64-pipe instructions (per unit, above) over its event-timed duration against that
     rate; its HBM fraction its algorithmic bytes over the same time against the measured copy
     bandwidth; the element kernel's tensor fraction its mma flops against the measured mma.sync
-    bf16 rate.  frac is the largest (the binding roof) of the dominant kernel."""
+    fp16 rate.  frac is the largest (the binding roof) of the dominant kernel."""
     N = N_ORDER
     inst_rate = peak_tf * 1e12 / 2
     face_s, elem_s = face_ms * 1e-3, elem_ms * 1e-3
@@ -140,7 +140,7 @@ def roofline(K, nf, face_ms, elem_ms, step_ms, peak_tf, hbm_peak, bf16_mma_tf=No
     elem_hbm = elem_bytes(N) * K / elem_s * 1e-9 / hbm_peak
     tiles = (K + 31) // 32
     elem_tensor_tf = elem_mma(N) * tiles * 4096 / elem_s * 1e-12
-    elem_tensor = elem_tensor_tf / bf16_mma_tf if bf16_mma_tf else None
+    elem_tensor = elem_tensor_tf / mma_tf if mma_tf else None
     step_fp64 = ((3 * (fi * nf + ei * K)) / (step_ms * 1e-3) / inst_rate) if (fi and ei) else None
     # The dominant kernel: the element kernel unless the face kernel is clearly the longer (by more
     # than 2 %).  Separately launched they take about the same time per stage; inside the step graph
@@ -161,19 +161,19 @@ def roofline(K, nf, face_ms, elem_ms, step_ms, peak_tf, hbm_peak, bf16_mma_tf=No
         per = elem_bytes(N) if dominant == "elem_kernel" else face_bytes(N)
         achieved, peak, unit = per * units / t * 1e-9, hbm_peak, "GB/s"
     else:
-        achieved, peak, unit = elem_tensor_tf, bf16_mma_tf, "TFLOP/s"
+        achieved, peak, unit = elem_tensor_tf, mma_tf, "TFLOP/s"
     return {
         "bound": bound, "kernel": dominant, "achieved": achieved, "peak": peak, "unit": unit,
         "frac": achieved / peak, "traffic": None,
         "traffic_note": "DRAM bytes need hardware counters: measured by ncu, not in this run (profiles/)",
         "peak_source": {"fp64": "DFMA peak measured live on this GPU / 2 (instructions)",
-                        "hbm": "MEASURED_PEAKS.json hbm_gbs", "tensor": "mma.sync bf16 measured live"}[bound],
+                        "hbm": "MEASURED_PEAKS.json hbm_gbs", "tensor": "mma.sync fp16 measured live"}[bound],
         "hbm_frac": elem_hbm if dominant == "elem_kernel" else face_hbm,
         "fp64_pipe_frac": elem_fp64 if dominant == "elem_kernel" else face_fp64,
         "tensor_pipe_frac": elem_tensor if dominant == "elem_kernel" else 0.0,
         "face_fp64_pipe_frac": face_fp64, "face_hbm_frac": face_hbm,
         "elem_fp64_pipe_frac": elem_fp64, "elem_hbm_frac": elem_hbm, "elem_tensor_pipe_frac": elem_tensor,
-        "elem_tensor_tflops": elem_tensor_tf, "bf16_mma_peak_tflops": bf16_mma_tf,
+        "elem_tensor_tflops": elem_tensor_tf, "f16_mma_peak_tflops": mma_tf,
         "step_fp64_pipe_frac": step_fp64,
         "step_note": "the graph step overlaps face and element launches of different cell ranges; "
                      "step_fp64_pipe_frac is both kernels' FP64-pipe instructions over the graph step time",
@@ -696,7 +696,7 @@ def main():
     except (OSError, KeyError, ValueError):
         hbm_peak, hbm_src = 6800.0, "fallback"
     peak_tf = peak_gflops * 1e-3
-    roof = roofline(K, nf, face_ms, elem_ms, ms_per_step, peak_tf, hbm_peak, pkg.bf16_mma_peak_gflops() * 1e-3)
+    roof = roofline(K, nf, face_ms, elem_ms, ms_per_step, peak_tf, hbm_peak, pkg.f16_mma_peak_gflops() * 1e-3)
 
     # end to end through the C ABI with pinned host buffers
     nq = K * Np * 4

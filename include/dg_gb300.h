@@ -301,13 +301,13 @@ int dg_l2_flush(void *stream);
 double dg_fp64_peak_gflops(void);
 /* Measured FP64 tensor-core (mma.sync m8n8k4 f64) throughput of this GPU, GFLOP/s. */
 double dg_fp64_mma_peak_gflops(void);
-/* Measured bf16 tensor-core throughput of this GPU for mma.sync.m16n8k16 with FP32 accumulation
+/* Measured fp16 tensor-core throughput of this GPU for mma.sync.m16n8k16 with FP32 accumulation
  * (the element kernel's contraction instruction), GFLOP/s. */
-double dg_bf16_mma_peak_gflops(void);
+double dg_f16_mma_peak_gflops(void);
 /* Number of kernels one dg_solver_run step launches. */
 int dg_kernels_per_step(void);
 /* Element-kernel form for launches and graphs built from now on: 3 (default) the dense rows
- * [Drw | Dsw | -LIFT] on the bf16 tensor cores as an exact integer product at orders N = 1, 2 and
+ * [Drw | Dsw | -LIFT] on the tensor cores as an exact integer product at orders N = 1, 2 and
  * form 2 at the other orders; 2 the even/odd split of those rows with its contraction on the
  * tensor cores at orders N = 3, 4, 5 and in FP64 at the other orders; 1 the even/odd split in
  * FP64; 0 dense FP64 rows.  All compute the same right-hand side to rounding (the tensor-core

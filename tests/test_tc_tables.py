@@ -1,7 +1,7 @@
 """Host-side tables of the element contraction on the tensor cores (no GPU needed).
 
 The operator blocks of the even/odd form are written, row by row, as signed base-256 digits
-(|d| <= 255, exact in bf16) of the 56-bit truncation of each entry scaled by the row's largest
+(|d| <= 255, exact in bf16 and fp16) of the 56-bit truncation of each entry scaled by the row's largest
 binary exponent.  These tests rebuild every entry from its digits with exact rational arithmetic.
 """
 from fractions import Fraction
