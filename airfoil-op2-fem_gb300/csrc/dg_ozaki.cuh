@@ -219,11 +219,10 @@ __device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *_
 #pragma unroll
   for (int ks = 0; ks < KST; ks++) {
     // this k-step's values at slots 16 ks + {2t, 2t+1, 2t+8, 2t+9}: aligned magnitudes
-    // m = M 2^(e - E + SH) (M the 53-bit significand; with PRE oz_prep's integers) and the sign
-    // pattern of every A-fragment register (pairs (g: q0 q1), (g+8: q0 q1), (g: q2 q3),
-    // (g+8: q2 q3))
-    // sgn[r + 2 (q >> 1)]: bit 15 the sign of value (r, q) for even q, bit 31 for odd q
-    uint32_t hi[2][4], lo[2][4], sgn[4] = {0u, 0u, 0u, 0u};
+    // m = M 2^(e - E + SH) (M the 53-bit significand; with PRE oz_prep's integers, whose sign
+    // bit 63 stays in hi: the digits use bytes 0..6 only) and, in sw, the word holding each
+    // value's sign in bit 31
+    uint32_t hi[2][4], lo[2][4], sw[2][4];
 #pragma unroll
     for (int r = 0; r < 2; r++)
 #pragma unroll
@@ -231,17 +230,25 @@ __device__ __forceinline__ void oz_tile(const double *__restrict__ Xd, double *_
         const int k = 16 * ks + 2 * t + (q & 1) + ((q >> 1) << 3);
         const double x = k < K ? Xd[(SLOT0 + k) * XST + col + 8 * r] : 0.0;
         const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-        const uint32_t sbit = (uint32_t)(b >> 32) & 0x80000000u;
-        sgn[r + 2 * (q >> 1)] |= (q & 1) ? sbit : (sbit >> 16);
+        sw[r][q] = (uint32_t)(b >> 32);
         unsigned long long m;
-        if constexpr (PRE) m = b & 0x00FFFFFFFFFFFFFFull;
+        if constexpr (PRE) m = b;
         else m = (unsigned long long)oz_align<SH>(b & 0x7FFFFFFFFFFFFFFFull, em[r]);
         hi[r][q] = (uint32_t)(m >> 32);
         lo[r][q] = (uint32_t)m;
       }
+    // the fp16 pair constant of every A-fragment register (pairs (g: q0 q1), (g+8: q0 q1),
+    // (g: q2 q3), (g+8: q2 q3)): 0x6400 in both halves with the low value's sign in bit 15 and
+    // the high value's in bit 31 (prmt with the sign-replicating selectors 0xB and 0xF copies
+    // bit 31 of each word over bytes 1 and 3)
     uint32_t v[4];
 #pragma unroll
-    for (int m = 0; m < 4; m++) v[m] = 0x64006400u | sgn[m];
+    for (int m = 0; m < 4; m++) {
+      const int r = m & 1, qa = (m >> 1) * 2;
+      uint32_t s2;
+      asm("prmt.b32 %0, %1, %2, 0xF0B0;" : "=r"(s2) : "r"(sw[r][qa]), "r"(sw[r][qa + 1]));
+      v[m] = (s2 & 0x80008000u) | 0x64006400u;
+    }
 #pragma unroll
     for (int j = 0; j < 7; j++) {
       // A fragment (row-major 16 x 16): rows g / g+8, slots 2t..2t+1 / 2t+8..2t+9
