@@ -256,18 +256,20 @@ __device__ __forceinline__ unsigned long long dt_speed_bits(const double n0, con
   return (unsigned long long)__double_as_longlong(spd * fs);
 }
 
-// SSPRK3 stage combine of one node's right-hand side (r0..r3), and in the last stage the
-// calc_dt maximum.  Every thread of the block calls it: `active` is false for warps beyond the
-// Np node-warps of a wider block (they only take part in the barrier), `live` is false for
-// lanes past the last cell (they take part in the warp reductions).
+// SSPRK3 stage combine of one node's right-hand side (r0..r3), and in the last stage the calc_dt
+// part: with Inst::dt_est each node-warp's largest single-precision estimate (the step's finalize
+// takes the FP64 maximum), without it the FP64 maximum over the block's candidates itself (the
+// batched kernels; two barriers).  Every thread of the block calls it: `active` is false for warps
+// beyond the Np node-warps of a wider block (they only take part in the barriers), `live` is false
+// for lanes past the last cell (they take part in the warp reductions).
 // The barrier among the threads that run the stage combine: the whole block here; the
 // warp-specialised element kernel passes its own (the node warps only, bounded waits).
 struct BlockSync {
   __device__ __forceinline__ void operator()() const { __syncthreads(); }
 };
 
-// qs: this node's q staged in shared memory (qs[0] variables 0, 1 and qs[qstride] variables 2, 3)
-// or null to read it from q.  sync: see BlockSync.
+// qs: this node's q staged in shared memory (qs[0] variables 0, 1 and qs[qstride] variables 2, 3;
+// the warp-specialised kernel) or null to read it from q.  sync: see BlockSync.
 template <int N, class SyncF = BlockSync>
 __device__ __forceinline__ void stage_combine(const Inst &d, const int stage, const int e, const bool active,
                                               const bool live, const int i, const int lane, const double w[4],
