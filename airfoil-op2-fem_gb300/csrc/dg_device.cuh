@@ -76,14 +76,16 @@ __device__ __forceinline__ void roe_flux2(const double qm[4], const double qp[4]
   const double c2 = P.gm1 * fma(-0.5, q2, H);
   const double rc = rsqrt(c2);
   const double c = c2 * rc;
-  const double ic2 = rc * rc;
-  // wave strengths
+  // wave strengths, with the 1/2 of dW1 and dW4 carried by rch = rc / 2: scaling by a power of
+  // two is exact, so dpc2h = dp / (2 c^2) and ah = a / 2 round exactly as dp / c^2 and a do, and
+  // dW1 = dpc2h - ah is the reference's (dp / c^2 - a) / 2 bit for bit, one multiply fewer
+  const double rch = 0.5 * rc;
   const double dp = pR - pL;
-  const double a = (rho * (uR - uL)) * rc;
-  const double dpc2 = dp * ic2;
-  double dW1 = 0.5 * (dpc2 - a);
-  double dW4 = 0.5 * (dpc2 + a);
-  double dW2 = (qp[0] - qm[0]) - dpc2;
+  const double ah = (rho * (uR - uL)) * rch;
+  const double dpc2h = dp * (rc * rch);
+  double dW1 = dpc2h - ah;
+  double dW4 = dpc2h + ah;
+  double dW2 = fma(-2.0, dpc2h, qp[0] - qm[0]);
   double dW3 = rho * (vR - vL);
   dW1 *= fabs(u - c);
   dW4 *= fabs(u + c);
