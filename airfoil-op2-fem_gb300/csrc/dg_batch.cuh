@@ -117,15 +117,70 @@ __global__ void __launch_bounds__(32 * np_of(N), elem_min_blocks(N, TC)) batch_e
   elem_tile_sym<N, false, TC>(insts[et.x], stage, et.y, threadIdx.x & 31, threadIdx.x >> 5, Xg);
 }
 
-__global__ void batch_finalize_kernel(const Inst *insts, const int n) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  StepState *st = insts[k].st;
-  st->t += st->dt;
-  st->step += 1;
-  if (insts[k].dt_mode == 0) {
-    const double dt1 = __longlong_as_double((long long)st->dt1_bits);
-    st->dt = (1.0 / dt1) * st->cfl;
+// calc_dt of node i of cell e (src/calc_dt.h) in FP64 from q, as the bit pattern of a non-negative
+// double; 0 for a cell past the last or a node without face points.
+template <int N>
+__device__ __forceinline__ unsigned long long dt_node_bits(const Inst &d, const int e, const int i) {
+  constexpr int Np = np_of(N);
+  const int fa = c_dtf[N][2 * i], fb = c_dtf[N][2 * i + 1];
+  if (e >= d.K || fa < 0) return 0ull;
+  const double *ge = d.geo + (size_t)e * 16;
+  const double fs = fb >= 0 ? fmax(ge[6 + 3 * fa], ge[6 + 3 * fb]) : ge[6 + 3 * fa];
+  const double *qp = d.q + ((size_t)e * Np + i) * 4;
+  const double2 a = ld2(qp), b = ld2(qp + 2);
+  return dt_speed_bits<N>(a.x, a.y, b.x, b.y, fs, d.P);
+}
+
+// The step's finalize of every instance, with the calc_dt maximum taken from the element
+// kernels' single-precision estimates as dt_finalize_kernel does for one solver: fblocks[b] =
+// {instance k, first estimate of the block, blocks of instance k, 0}; each block's 8 warps read
+// 32 estimates each (one ballot), evaluate the candidates within 1e-4 of the instance's largest
+// estimate in FP64 (each by the whole warp), combine them by atomicMax, and the instance's last
+// block (the counter in its step state, no waiting) advances its t and sets its dt.  Instances
+// with a frozen dt get one block that advances t.
+__global__ void __launch_bounds__(256) batch_dt_finalize_kernel(const Inst *insts, const int4 *fblocks) {
+  const int4 fb = fblocks[blockIdx.x];
+  const Inst &d = insts[fb.x];
+  StepState *st = d.st;
+  __shared__ int s_last;
+  if (d.dt_mode == 0) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int Np = np_of(d.N), n = ((d.K + 31) >> 5) * Np;
+    const float thr = __uint_as_float(st->dt_est_max) * 0.9999f;
+    const int base = fb.y + warp * 32;
+    unsigned cand = __ballot_sync(0xffffffffu, base + lane < n && d.dt_est[base + lane] >= thr);
+    unsigned long long best = 0ull;
+    while (cand) {
+      const int k = __ffs((int)cand) - 1;
+      cand &= cand - 1u;
+      const int j = base + k, tile = j / Np, i = j - tile * Np, e = tile * 32 + lane;
+      unsigned long long v = 0ull;
+      DG_DISPATCH_RT(d.N, (v = dt_node_bits<NN>(d, e, i)));
+      best = v > best ? v : best;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long x = __shfl_xor_sync(0xffffffffu, best, o);
+      best = x > best ? x : best;
+    }
+    if (lane == 0 && best) atomicMax(&st->dt1_bits, best);
+  }
+  // the step state's other fields are not written by this kernel before the last block's update
+  const double dt0 = st->dt, t0 = st->t, cfl = st->cfl;
+  const unsigned long long step0 = st->step;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(&st->dt_blocks, 1u) == (unsigned)fb.z - 1u;
+  __syncthreads();
+  if (!s_last || threadIdx.x) return;
+  __threadfence();
+  st->dt_blocks = 0u;
+  st->dt_est_max = 0u;
+  if (d.dt_hist && step0 < d.dt_hist_len) d.dt_hist[step0] = dt0;
+  st->t = t0 + dt0;
+  st->step = step0 + 1;
+  if (d.dt_mode == 0) {
+    const double dt1 = __longlong_as_double((long long)atomicAdd(&st->dt1_bits, 0ull));
+    st->dt = (1.0 / dt1) * cfl;
     st->dt1_bits = 0ull;
   }
 }
@@ -173,6 +228,8 @@ struct Batch {
   Inst *d_insts = nullptr;
   int4 *d_ftiles = nullptr, *d_etiles = nullptr;
   int nft = 0, net = 0;
+  int4 *d_fblocks = nullptr;  // blocks of batch_dt_finalize_kernel
+  int nfb = 0;
   int ord_first[7] = {0}, ord_count[7] = {0};  // element tiles of each order (contiguous)
   GridBarrier *d_bar = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
@@ -185,6 +242,7 @@ struct Batch {
     if (d_insts) cudaFree(d_insts);
     if (d_ftiles) cudaFree(d_ftiles);
     if (d_etiles) cudaFree(d_etiles);
+    if (d_fblocks) cudaFree(d_fblocks);
     if (d_bar) cudaFree(d_bar);
     for (Solver *s : solvers) delete s;
     if (stream) cudaStreamDestroy(stream);
@@ -206,9 +264,19 @@ struct Batch {
     }
     maxNp = np_of(maxN);
     std::vector<Inst> insts;
-    for (Solver *s : solvers) {
-      insts.push_back(s->d);
-      insts.back().dt_est = nullptr;  // the element kernel takes the dt maximum itself
+    std::vector<int4> fbs;  // the finalize's blocks: 256 estimates each, one for a frozen dt
+    for (size_t k = 0; k < solvers.size(); k++) {
+      const Inst &d = solvers[k]->d;
+      insts.push_back(d);
+      const int n = ((d.K + 31) / 32) * np_of(d.N);
+      const int g = d.dt_mode == 0 ? std::max(1, (n + 255) / 256) : 1;
+      for (int b = 0; b < g; b++) fbs.push_back(make_int4((int)k, 256 * b, g, 0));
+    }
+    nfb = (int)fbs.size();
+    if (cudaMalloc(&d_fblocks, sizeof(int4) * fbs.size()) != cudaSuccess ||
+        cudaMemcpy(d_fblocks, fbs.data(), sizeof(int4) * fbs.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+      err = "cudaMalloc failed";
+      return -100;
     }
     if (cudaMalloc(&d_insts, sizeof(Inst) * insts.size()) != cudaSuccess ||
         cudaMalloc(&d_bar, sizeof(GridBarrier)) != cudaSuccess) {
@@ -353,8 +421,7 @@ struct Batch {
       cudaError_t ce = sh.variant == kGroupedVariant ? launch_grouped(sh, stage, s) : launch_stage(sh, stage, s);
       if (ce != cudaSuccess) return ce;
     }
-    const int n = (int)solvers.size();
-    batch_finalize_kernel<<<(n + 127) / 128, 128, 0, s>>>(d_insts, n);
+    batch_dt_finalize_kernel<<<nfb, 256, 0, s>>>(d_insts, d_fblocks);
     return cudaGetLastError();
   }
 
@@ -479,12 +546,12 @@ struct Batch {
       prev = node;
     }
     if (ce == cudaSuccess) {
-      const int n = (int)solvers.size();
-      void *fargs[2] = {(void *)&a0, (void *)&n};
+      const int4 *fbp = d_fblocks;
+      void *fargs[2] = {(void *)&a0, (void *)&fbp};
       cudaKernelNodeParams kp = {};
-      kp.func = (void *)batch_finalize_kernel;
-      kp.gridDim = dim3((n + 127) / 128);
-      kp.blockDim = dim3(128);
+      kp.func = (void *)batch_dt_finalize_kernel;
+      kp.gridDim = dim3(nfb);
+      kp.blockDim = dim3(256);
       kp.kernelParams = fargs;
       cudaGraphNode_t node;
       ce = cudaGraphAddKernelNode(&node, g, &prev, 1, &kp);

@@ -77,19 +77,6 @@ __device__ __forceinline__ void ws_fail(const Inst &d) {
   if (d.st) atomicOr(&d.st->err, 4u);
 }
 
-// The node warps' barrier inside the stage combine (the dt maximum of the last stage): an
-// mbarrier over the node threads, bounded like the others.
-struct WsNodeSync {
-  unsigned long long *bar;
-  unsigned *phase;
-  const Inst *d;
-  __device__ __forceinline__ void operator()() const {
-    mbar_arrive(bar);
-    if (!mbar_wait(bar, *phase & 1u, kWsWaitLimit)) ws_fail(*d);
-    (*phase)++;
-  }
-};
-
 // The copies of a tile's face fluxes (into their slots) and, in stages 1 and 2, of q (into the
 // staged W / q area), as one cp.async group of this thread.
 template <int N>
@@ -178,8 +165,7 @@ __device__ __forceinline__ void ws_compute(const Inst &d, const int e0, const in
 // with the staged W and q (the last part of elem_tile_sym).  Arrives on yempty once Y is read.
 template <int N>
 __device__ __forceinline__ void ws_combine(const Inst &d, const int stage, const int e0, const int lane, const int i,
-                                           const double2 *Y, double2 *WQ, unsigned long long *yempty,
-                                           const WsNodeSync &sync) {
+                                           const double2 *Y, double2 *WQ, unsigned long long *yempty) {
   constexpr int Np = np_of(N);
   constexpr int kS2 = kElemSlot / 2;
   constexpr int nthr = 32 * Np;
@@ -203,10 +189,8 @@ __device__ __forceinline__ void ws_combine(const Inst &d, const int stage, const
     const double2 a = WQ[tid], b = WQ[nthr + tid];
     w[0] = a.x; w[1] = a.y; w[2] = b.x; w[3] = b.y;
   }
-  // the candidates of the last stage's dt maximum go to this buffer's W / q area: every node thread
-  // has read its W and q before the combine's first barrier
-  stage_combine<N, WsNodeSync>(d, stage, e, true, live, i, lane, w, r0, r1, r2, r3, WQ,
-                               (stage == 1 || stage == 2) ? WQ + 2 * nthr + tid : nullptr, nthr, sync);
+  stage_combine<N>(d, stage, e, true, live, i, lane, w, r0, r1, r2, r3,
+                   (stage == 1 || stage == 2) ? WQ + 2 * nthr + tid : nullptr, nthr);
 }
 
 // Tiles [t0, t1) of one stage over the grid's blocks, each block a contiguous range of tiles.
@@ -230,7 +214,7 @@ __global__ void __launch_bounds__(ws_threads(N), 1) elem_kernel_ws(const Inst d,
     WQ[b] = reinterpret_cast<double2 *>(Ems[b] + 128);
   }
   // per buffer b: X full (b), X empty (B + b), Y full (2B + b), Y empty (3B + b); then the
-  // contraction warps' pre-pass barrier (4B) and the node warps' barrier (4B + 1)
+  // contraction warps' pre-pass barrier (4B)
   unsigned long long *bars = reinterpret_cast<unsigned long long *>(ws_sm + B * ws_buf_bytes(N));
   unsigned long long *xfull = bars, *xempty = bars + B, *yfull = bars + 2 * B, *yempty = bars + 3 * B;
   const int tid = threadIdx.x;
@@ -242,7 +226,6 @@ __global__ void __launch_bounds__(ws_threads(N), 1) elem_kernel_ws(const Inst d,
       mbar_init(&yempty[b], NN);
     }
     mbar_init(&bars[4 * B], NC);
-    mbar_init(&bars[4 * B + 1], NN);
   }
   __syncthreads();
   pdl_trigger();
@@ -251,8 +234,6 @@ __global__ void __launch_bounds__(ws_threads(N), 1) elem_kernel_ws(const Inst d,
   const int n = t0 + (int)((long long)nt * (blockIdx.x + 1) / G) - tb;
   if (tid < (int)NN) {
     const int i = tid >> 5, lane = tid & 31;
-    unsigned nphase = 0;
-    const WsNodeSync sync{&bars[4 * B + 1], &nphase, &d};
     // tile j uses buffer j % B for the (j / B)-th time; before its copies start, the contraction of
     // the buffer's previous tile (j - B) must be done with X
     auto issue = [&](int j) {
@@ -276,7 +257,7 @@ __global__ void __launch_bounds__(ws_threads(N), 1) elem_kernel_ws(const Inst d,
       if (j >= 1) {
         const int jj = j - 1, b = jj % B, k = jj / B;
         if (!mbar_wait(&yfull[b], (unsigned)k & 1u, kWsWaitLimit)) ws_fail(d);
-        ws_combine<N>(d, stage, (tb + jj) * 32, lane, i, Y[b], WQ[b], &yempty[b], sync);
+        ws_combine<N>(d, stage, (tb + jj) * 32, lane, i, Y[b], WQ[b], &yempty[b]);
       }
       wc[0] = wn[0]; wc[1] = wn[1]; gc[0] = gn[0]; gc[1] = gn[1];
     }

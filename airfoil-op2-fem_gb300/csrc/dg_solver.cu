@@ -256,26 +256,17 @@ __device__ __forceinline__ unsigned long long dt_speed_bits(const double n0, con
   return (unsigned long long)__double_as_longlong(spd * fs);
 }
 
-// SSPRK3 stage combine of one node's right-hand side (r0..r3), and in the last stage the calc_dt
-// part: with Inst::dt_est each node-warp's largest single-precision estimate (the step's finalize
-// takes the FP64 maximum), without it the FP64 maximum over the block's candidates itself (the
-// batched kernels; two barriers).  Every thread of the block calls it: `active` is false for warps
-// beyond the Np node-warps of a wider block (they only take part in the barriers), `live` is false
-// for lanes past the last cell (they take part in the warp reductions).
-// The barrier among the threads that run the stage combine: the whole block here; the
-// warp-specialised element kernel passes its own (the node warps only, bounded waits).
-struct BlockSync {
-  __device__ __forceinline__ void operator()() const { __syncthreads(); }
-};
-
-// qs: this node's q staged in shared memory (qs[0] variables 0, 1 and qs[qstride] variables 2, 3;
-// the warp-specialised kernel) or null to read it from q.  sync: see BlockSync.
-template <int N, class SyncF = BlockSync>
+// SSPRK3 stage combine of one node's right-hand side (r0..r3), and in the last stage each
+// node-warp's largest single-precision calc_dt estimate (Inst::dt_est; the step's finalize takes
+// the FP64 maximum).  Every thread of the node-warps calls it: `active` is false for warps beyond
+// the Np node-warps of a wider block, `live` is false for lanes past the last cell (they take part
+// in the warp reductions).  qs: this node's q staged in shared memory (qs[0] variables 0, 1 and
+// qs[qstride] variables 2, 3; the warp-specialised kernel) or null to read it from q.
+template <int N>
 __device__ __forceinline__ void stage_combine(const Inst &d, const int stage, const int e, const bool active,
                                               const bool live, const int i, const int lane, const double w[4],
-                                              double r0, double r1, double r2, double r3, double2 *scratch,
-                                              const double2 *qs = nullptr, const int qstride = 0,
-                                              const SyncF &sync = SyncF()) {
+                                              double r0, double r1, double r2, double r3,
+                                              const double2 *qs = nullptr, const int qstride = 0) {
   constexpr int Np = np_of(N);
   const Phys &P = d.P;
   const size_t off = ((size_t)(live ? e : 0) * Np + (active ? i : 0)) * 4;
@@ -331,21 +322,20 @@ __device__ __forceinline__ void stage_combine(const Inst &d, const int stage, co
     st2(wp + 2, n2, n3);
     if (bad_density(n0)) atomicOr(&d.st->err, 1u);
   }
-  if (d.dt_mode == 0) {
+  if (d.dt_mode == 0 && d.dt_est) {
     // src/calc_dt.h: (N+1)^2 * 0.5 * fscale * (|v| + c) at the face points of this node, maximised
-    // over the block.  A single-precision estimate finds the block's candidates first; only
-    // those within 1e-4 of the block's estimated maximum are evaluated in FP64.  The FP32
-    // estimate (from bit-truncated copies of the state, f32_trunc) is within ~1e-6 of the FP64
-    // value, so the block's true maximum is always a candidate and the result equals the
-    // all-FP64 maximum.  Each node-warp evaluates its own candidates (one FP64 pass if it holds
-    // any) and combines them with one atomicMax: no packing of the candidates and no second
-    // barrier with one warp evaluating for the whole block while the others wait.
-    __shared__ float s_wmax[32];
+    // over the mesh.  Here only a single-precision estimate (from bit-truncated copies of the
+    // state, f32_trunc, and single-precision copies of fscale and gamma), within ~1e-6 of the FP64
+    // value: each node-warp stores its largest estimate and combines it into the step state's
+    // maximum estimate; the step's finalize (dt_finalize_kernel, batch_dt_finalize_kernel)
+    // evaluates in FP64 the nodes whose estimate is within 1e-4 of that maximum, among them the
+    // node of the FP64 maximum.  No barrier and no FP64 instruction here: evaluating a block's
+    // candidates in this kernel (a barrier, a ~35-long FP64 chain waiting behind the other blocks'
+    // FP64 work, a second barrier) held every stage-2 tile ~9k clocks.
     const int fa = active ? c_dtf[N][2 * i] : -1, fb = active ? c_dtf[N][2 * i + 1] : -1;
-    const double *ge = d.geo + (size_t)(live ? e : 0) * 16;
     float est = 0.0f;
     if (live && fa >= 0) {
-      const float *gf = reinterpret_cast<const float *>(ge + 14);  // fscale per face, single precision
+      const float *gf = reinterpret_cast<const float *>(d.geo + (size_t)e * 16 + 14);  // fscale, f32
       const float fsf = fb >= 0 ? fmaxf(gf[fa], gf[fb]) : gf[fa];
       const float rho = f32_trunc(n0), ir = 1.0f / rho, u = f32_trunc(n1) * ir, v = f32_trunc(n2) * ir;
       const float v2 = u * u + v * v;
@@ -354,56 +344,21 @@ __device__ __forceinline__ void stage_combine(const Inst &d, const int stage, co
       est = ((N + 1) * (N + 1) * 0.5f) * (sqrtf(v2) + cs) * fsf;
       if (!(est == est) || est > 3.0e38f) est = 3.0e38f;  // non-finite: always a candidate
     }
-    if (d.dt_est) {
-      // deferred: the node-warp's largest estimate goes to HBM and dt_finalize_kernel takes the
-      // FP64 maximum over the candidates of the whole mesh; no barrier, no FP64 here (a chain of
-      // ~35 FP64 instructions at the end of every tile, waiting behind the other blocks' FP64
-      // work, held each block ~9k clocks)
-      if (active) {
-        float wm = est;
-        for (int o = 16; o > 0; o >>= 1) wm = fmaxf(wm, __shfl_xor_sync(0xffffffffu, wm, o));
-        if (lane == 0) {
-          d.dt_est[(size_t)(e >> 5) * Np + i] = wm;
-          atomicMax(&d.st->dt_est_max, __float_as_uint(wm));  // non-negative: ordered as integers
-        }
-      }
-      return;
-    }
     if (active) {
       float wm = est;
       for (int o = 16; o > 0; o >>= 1) wm = fmaxf(wm, __shfl_xor_sync(0xffffffffu, wm, o));
-      if (lane == 0) s_wmax[i] = wm;
-    }
-    sync();
-    if (active) {
-      float bm = 0.0f;
-      for (int k = 0; k < Np; k++) bm = fmaxf(bm, s_wmax[k]);
-      const bool cand = live && fa >= 0 && est >= bm * 0.9999f;
-      if (__any_sync(0xffffffffu, cand)) {
-        unsigned long long best = 0ull;
-        if (cand) {
-          const double fs = fb >= 0 ? fmax(ge[6 + 3 * fa], ge[6 + 3 * fb]) : ge[6 + 3 * fa];
-          best = dt_speed_bits<N>(n0, n1, n2, n3, fs, P);
-        }
-        // warp max on the bit patterns of non-negative doubles (all 32 lanes take part)
-        for (int o = 16; o > 0; o >>= 1) {
-          const unsigned long long x = __shfl_xor_sync(0xffffffffu, best, o);
-          best = x > best ? x : best;
-        }
-        if (lane == 0 && best) atomicMax(&d.st->dt1_bits, best);
+      if (lane == 0) {
+        d.dt_est[(size_t)(e >> 5) * Np + i] = wm;
+        atomicMax(&d.st->dt_est_max, __float_as_uint(wm));  // non-negative: ordered as integers
       }
     }
-    // the block may run another tile next (batched kernel): s_wmax is rewritten only after every
-    // warp has read it
-    sync();
-    (void)scratch;
   }
 }
 
 // ---------------------------------------------------------------- element kernel
 // stage 0: W = W + dt*L           (W holds q at the start of a step)
 // stage 1: W = 3/4 q + 1/4 (W + dt*L)
-// stage 2: q = W = 1/3 q + 2/3 (W + dt*L), then the calc_dt maximum over the new q
+// stage 2: q = W = 1/3 q + 2/3 (W + dt*L), then the calc_dt estimates of the new q
 // stage 3: rhs_out = L (one right-hand side, no combine)
 template <int N>
 __global__ void __launch_bounds__(32 * np_of(N)) elem_kernel(const Inst d, const int stage) {
@@ -475,7 +430,7 @@ __global__ void __launch_bounds__(32 * np_of(N)) elem_kernel(const Inst d, const
     r2 = fma(c, x23.x, r2);
     r3 = fma(c, x23.y, r3);
   }
-  stage_combine<N>(d, stage, e, true, live, i, lane, w, r0, r1, r2, r3, X);
+  stage_combine<N>(d, stage, e, true, live, i, lane, w, r0, r1, r2, r3);
 }
 
 // The element kernel in even/odd form.  The reflection sigma: (r,s) -> (s,r) of the reference
@@ -647,7 +602,7 @@ __device__ __forceinline__ void elem_tile_sym(const Inst &d, const int stage, co
       w[0] = a.x; w[1] = a.y; w[2] = b.x; w[3] = b.y;
     }
   }
-  stage_combine<N>(d, stage, e, active, live, i, lane, w, r0, r1, r2, r3, X);
+  stage_combine<N>(d, stage, e, active, live, i, lane, w, r0, r1, r2, r3);
   // X and Y are rewritten by the next tile only after every warp is past this point
   __syncthreads();
 }
