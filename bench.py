@@ -12,6 +12,9 @@ initial state (the reference publishes no benchmark data set).
 
 value   device-resident: CUDA events around each step's graph launch on the
         solver stream, L2 flushed (512 MB write) between steps outside the events.
+value_one_run  the same K steps as one dg_solver_run call (graphs of several steps,
+        the next step's face launches overlapping the previous step's element
+        launches), L2 flushed once before it; reported beside value.
 e2e     the C-ABI call dg_solver_step_host with pinned host buffers: H2D of q,
         one step, D2H of q, timed with events on the same stream.
 roofline  the dominant kernel's binding roof: its FP64-pipe instructions (per-unit
