@@ -71,6 +71,28 @@ def test_batch_every_shape_equals_plain(pkg, shape):
         assert np.array_equal(b.get(k, "q"), ref[k][0]), k
 
 
+@pytest.mark.parametrize("shape", [(0, 512), (99, 64)])
+def test_batch_tied_dt_estimates_equal_plain(pkg, shape):
+    """Freestream on uniform square meshes with inflow boundaries (dt recomputed every step): the
+    calc_dt estimates of every cell tie, so the batched finalize evaluates a large share of each
+    instance's node-warps in FP64 over several blocks per instance.  Bitwise the plain solvers'
+    q, time and dt."""
+    meshes, cfgs = [], []
+    for n, N in ((24, 3), (16, 4), (32, 3)):
+        m = pkg.Mesh.vortex_square(n)
+        m.set_bedge_type(np.zeros(m.size("bedges"), dtype=np.int32))
+        meshes.append(m)
+        cfgs.append(pkg.config(N=N, cfl=0.5, mach=0.4))
+    ref = plain(pkg, meshes, cfgs, 6)
+    b = pkg.Batch(meshes, cfgs).init()
+    b.use_shape(*shape)
+    b.run(6)
+    b.sync()
+    for k in range(len(cfgs)):
+        assert np.array_equal(b.get(k, "q"), ref[k][0]), k
+        assert b.time(k) == ref[k][1], k
+
+
 def test_batch_reports_nonphysical(pkg):
     meshes, cfgs = instances(pkg)
     b = pkg.Batch(meshes[:2], cfgs[:2]).init()
