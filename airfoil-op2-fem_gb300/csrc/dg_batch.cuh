@@ -117,20 +117,6 @@ __global__ void __launch_bounds__(32 * np_of(N), elem_min_blocks(N, TC)) batch_e
   elem_tile_sym<N, false, TC>(insts[et.x], stage, et.y, threadIdx.x & 31, threadIdx.x >> 5, Xg);
 }
 
-// calc_dt of node i of cell e (src/calc_dt.h) in FP64 from q, as the bit pattern of a non-negative
-// double; 0 for a cell past the last or a node without face points.
-template <int N>
-__device__ __forceinline__ unsigned long long dt_node_bits(const Inst &d, const int e, const int i) {
-  constexpr int Np = np_of(N);
-  const int fa = c_dtf[N][2 * i], fb = c_dtf[N][2 * i + 1];
-  if (e >= d.K || fa < 0) return 0ull;
-  const double *ge = d.geo + (size_t)e * 16;
-  const double fs = fb >= 0 ? fmax(ge[6 + 3 * fa], ge[6 + 3 * fb]) : ge[6 + 3 * fa];
-  const double *qp = d.q + ((size_t)e * Np + i) * 4;
-  const double2 a = ld2(qp), b = ld2(qp + 2);
-  return dt_speed_bits<N>(a.x, a.y, b.x, b.y, fs, d.P);
-}
-
 // The step's finalize of every instance, with the calc_dt maximum taken from the element
 // kernels' single-precision estimates as dt_finalize_kernel does for one solver: fblocks[b] =
 // {instance k, first estimate of the block, blocks of instance k, 0}; each block's 8 warps read
@@ -141,48 +127,23 @@ __device__ __forceinline__ unsigned long long dt_node_bits(const Inst &d, const 
 __global__ void __launch_bounds__(256) batch_dt_finalize_kernel(const Inst *insts, const int4 *fblocks) {
   const int4 fb = fblocks[blockIdx.x];
   const Inst &d = insts[fb.x];
-  StepState *st = d.st;
-  __shared__ int s_last;
+  unsigned long long best = 0ull;
   if (d.dt_mode == 0) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int Np = np_of(d.N), n = ((d.K + 31) >> 5) * Np;
-    const float thr = __uint_as_float(st->dt_est_max) * 0.9999f;
+    const float thr = __uint_as_float(d.st->dt_est_max) * 0.9999f;
     const int base = fb.y + warp * 32;
     unsigned cand = __ballot_sync(0xffffffffu, base + lane < n && d.dt_est[base + lane] >= thr);
-    unsigned long long best = 0ull;
     while (cand) {
       const int k = __ffs((int)cand) - 1;
       cand &= cand - 1u;
-      const int j = base + k, tile = j / Np, i = j - tile * Np, e = tile * 32 + lane;
+      const int j = base + k, tile = j / Np;
       unsigned long long v = 0ull;
-      DG_DISPATCH_RT(d.N, (v = dt_node_bits<NN>(d, e, i)));
+      DG_DISPATCH_RT(d.N, (v = dt_node_bits<NN>(d, tile * 32 + lane, j - tile * Np)));
       best = v > best ? v : best;
     }
-    for (int o = 16; o > 0; o >>= 1) {
-      const unsigned long long x = __shfl_xor_sync(0xffffffffu, best, o);
-      best = x > best ? x : best;
-    }
-    if (lane == 0 && best) atomicMax(&st->dt1_bits, best);
   }
-  // the step state's other fields are not written by this kernel before the last block's update
-  const double dt0 = st->dt, t0 = st->t, cfl = st->cfl;
-  const unsigned long long step0 = st->step;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) s_last = atomicAdd(&st->dt_blocks, 1u) == (unsigned)fb.z - 1u;
-  __syncthreads();
-  if (!s_last || threadIdx.x) return;
-  __threadfence();
-  st->dt_blocks = 0u;
-  st->dt_est_max = 0u;
-  if (d.dt_hist && step0 < d.dt_hist_len) d.dt_hist[step0] = dt0;
-  st->t = t0 + dt0;
-  st->step = step0 + 1;
-  if (d.dt_mode == 0) {
-    const double dt1 = __longlong_as_double((long long)atomicAdd(&st->dt1_bits, 0ull));
-    st->dt = (1.0 / dt1) * cfl;
-    st->dt1_bits = 0ull;
-  }
+  finalize_block_end(d, best, (unsigned)fb.z);
 }
 
 // Kernel variants the autotuner chooses among: block size x minimum resident blocks (the

@@ -654,6 +654,53 @@ __global__ void finalize_kernel(StepState *st, int dt_mode, double *dt_hist, uns
 // of the FP64 maximum is always among them and the result is the exact maximum, the same as the
 // element kernel's per-block evaluation gives), combined with atomicMax; the last block to finish
 // (a counter in the step state, no waiting) then advances t and sets the new dt.
+// calc_dt of node i of cell e (src/calc_dt.h) in FP64 from q, as the bit pattern of a non-negative
+// double; 0 for a cell past the last or a node without face points.
+template <int N>
+__device__ __forceinline__ unsigned long long dt_node_bits(const Inst &d, const int e, const int i) {
+  constexpr int Np = np_of(N);
+  const int fa = c_dtf[N][2 * i], fb = c_dtf[N][2 * i + 1];
+  if (e >= d.K || fa < 0) return 0ull;
+  const double *ge = d.geo + (size_t)e * 16;
+  const double fs = fb >= 0 ? fmax(ge[6 + 3 * fa], ge[6 + 3 * fb]) : ge[6 + 3 * fa];
+  const double *qp = d.q + ((size_t)e * Np + i) * 4;
+  const double2 a = ld2(qp), b = ld2(qp + 2);
+  return dt_speed_bits<N>(a.x, a.y, b.x, b.y, fs, d.P);
+}
+
+// The end of a finalize block: its warps' FP64 maxima go into the step state by atomicMax, and the
+// last of the nblocks blocks of this instance's finalize (a counter in the step state, no waiting)
+// advances t and the step count, records the step's dt, and sets the new dt from the maximum
+// (dt recomputed) or leaves it (frozen).  The step state's other fields are not written by any
+// block before that last block's update, so every block reads them first.
+__device__ __forceinline__ void finalize_block_end(const Inst &d, unsigned long long best, const unsigned nblocks) {
+  StepState *st = d.st;
+  __shared__ int s_last;
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long x = __shfl_xor_sync(0xffffffffu, best, o);
+    best = x > best ? x : best;
+  }
+  if ((threadIdx.x & 31) == 0 && best) atomicMax(&st->dt1_bits, best);
+  const double dt0 = st->dt, t0 = st->t, cfl = st->cfl;
+  const unsigned long long step0 = st->step;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(&st->dt_blocks, 1u) == nblocks - 1u;
+  __syncthreads();
+  if (!s_last || threadIdx.x) return;
+  __threadfence();
+  st->dt_blocks = 0u;
+  st->dt_est_max = 0u;
+  if (d.dt_hist && step0 < d.dt_hist_len) d.dt_hist[step0] = dt0;
+  st->t = t0 + dt0;
+  st->step = step0 + 1;
+  if (d.dt_mode == 0) {
+    const double dt1 = __longlong_as_double((long long)atomicAdd(&st->dt1_bits, 0ull));
+    st->dt = (1.0 / dt1) * cfl;
+    st->dt1_bits = 0ull;
+  }
+}
+
 template <int N>
 __global__ void __launch_bounds__(256) dt_finalize_kernel(const Inst d) {
   constexpr int Np = np_of(N);
@@ -661,9 +708,7 @@ __global__ void __launch_bounds__(256) dt_finalize_kernel(const Inst d) {
   pdl_trigger();
   const int n = ((d.K + 31) >> 5) * Np;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  __shared__ int s_last;
-  StepState *st = d.st;
-  const float thr = __uint_as_float(st->dt_est_max) * 0.9999f;
+  const float thr = __uint_as_float(d.st->dt_est_max) * 0.9999f;
   // warp w of the grid takes the estimates w, w + G, w + 2G, ... (G warps in the grid): its lanes
   // read 32 of them at once, and the candidates among them are evaluated one after the other,
   // each by the whole warp (lane = cell of the tile)
@@ -675,40 +720,12 @@ __global__ void __launch_bounds__(256) dt_finalize_kernel(const Inst d) {
     while (cand) {
       const int k = __ffs((int)cand) - 1;
       cand &= cand - 1u;
-      const int j = base + k * gs;
-      const int tile = j / Np, i = j - tile * Np, e = tile * 32 + lane;
-      const int fa = c_dtf[N][2 * i], fb = c_dtf[N][2 * i + 1];
-      if (e < d.K && fa >= 0) {
-        const double *ge = d.geo + (size_t)e * 16;
-        const double fs = fb >= 0 ? fmax(ge[6 + 3 * fa], ge[6 + 3 * fb]) : ge[6 + 3 * fa];
-        const double2 a = ld2(d.q + ((size_t)e * Np + i) * 4), b = ld2(d.q + ((size_t)e * Np + i) * 4 + 2);
-        const unsigned long long v = dt_speed_bits<N>(a.x, a.y, b.x, b.y, fs, d.P);
-        best = v > best ? v : best;
-      }
+      const int j = base + k * gs, tile = j / Np;
+      const unsigned long long v = dt_node_bits<N>(d, tile * 32 + lane, j - tile * Np);
+      best = v > best ? v : best;
     }
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long x = __shfl_xor_sync(0xffffffffu, best, o);
-    best = x > best ? x : best;
-  }
-  if (lane == 0 && best) atomicMax(&st->dt1_bits, best);
-  // the step state's other fields are not written by this kernel before the last block's update
-  const double dt0 = st->dt, t0 = st->t, cfl = st->cfl;
-  const unsigned long long step0 = st->step;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) s_last = atomicAdd(&st->dt_blocks, 1u) == gridDim.x - 1;
-  __syncthreads();
-  if (!s_last || threadIdx.x) return;
-  __threadfence();
-  st->dt_blocks = 0u;
-  st->dt_est_max = 0u;
-  if (d.dt_hist && step0 < d.dt_hist_len) d.dt_hist[step0] = dt0;
-  st->t = t0 + dt0;
-  st->step = step0 + 1;
-  const double dt1 = __longlong_as_double((long long)atomicAdd(&st->dt1_bits, 0ull));
-  st->dt = (1.0 / dt1) * cfl;
-  st->dt1_bits = 0ull;
+  finalize_block_end(d, best, gridDim.x);
 }
 
 // ---------------------------------------------------------------- set-up kernels
